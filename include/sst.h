@@ -1,0 +1,212 @@
+/*
+ * sst.h -- C ABI of libsst, the GB300 (sm_103a) wavefront path tracer that drops in for
+ * SeeSharp's unidirectional PathTracer.
+ *
+ * Every entry point returns an int status: SST_OK (0) or a negative error class.  A message for
+ * the last failure on the calling thread is available from sst_last_error().  No C++ exception
+ * crosses this boundary.  Handles are opaque.  Caller-owned input arrays are copied; the scene
+ * and context own their device memory.  Buffers passed with SST_MEM_DEVICE are CUDA device
+ * pointers on the context's device; SST_MEM_HOST buffers are ordinary host memory.
+ *
+ * One host thread at a time per context.  Calls are synchronous: they return after the GPU work
+ * they issued has finished.
+ *
+ * Each declaration names the SeeSharp interface it replaces (paths relative to the SeeSharp
+ * project root).  The C# binding a maintainer adds to SeeSharp is shown in INTEGRATION.md.
+ */
+#ifndef SST_H
+#define SST_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SST_OK 0
+#define SST_ERR_INVALID_ARGUMENT (-1) /* ArgumentException in SeeSharp */
+#define SST_ERR_INVALID_SCENE (-2)    /* InvalidOperationException from Scene.Prepare */
+#define SST_ERR_CUDA (-3)
+#define SST_ERR_OUT_OF_MEMORY (-4)
+#define SST_ERR_NOT_COMMITTED (-5)    /* scene used before sst_scene_commit */
+#define SST_ERR_DEVICE_LIMIT (-6)     /* a device-side iteration or stack limit was reached */
+#define SST_ERR_UNSUPPORTED (-7)
+
+#define SST_MEM_HOST 0
+#define SST_MEM_DEVICE 1
+
+#define SST_BORDER_REPEAT 0 /* ImageTexture.BorderHandling.Repeat (Images/ImageTexture.cs:12-21) */
+#define SST_BORDER_CLAMP 1  /* ImageTexture.BorderHandling.Clamp */
+
+typedef struct sst_ctx sst_ctx;
+typedef struct sst_scene sst_scene;
+
+/* GenericMaterial.Parameters (Shading/Materials/GenericMaterial.cs:25-61).  A texture index < 0
+ * selects the constant value. */
+typedef struct SstGenericMaterial {
+    float baseColor[3];
+    int32_t baseColorTexture;
+    float roughness;
+    int32_t roughnessTexture;
+    float metallic;
+    float specularTintStrength;
+    float anisotropic;
+    float specularTransmittance;
+    float indexOfRefraction;
+} SstGenericMaterial;
+
+/* TinyEmbree Ray: origin, MinDistance, direction, and the far end of the valid interval. */
+typedef struct SstRay {
+    float org[3];
+    float tmin;
+    float dir[3];
+    float tmax;
+} SstRay;
+
+/* TinyEmbree Hit (as wrapped by Geometry/SurfacePoint.cs:7-77).  meshId < 0 means no hit. */
+typedef struct SstHit {
+    float distance;
+    float u, v; /* barycentrics: u weights the second, v the third vertex */
+    int32_t primId;
+    int32_t meshId;
+    float errorOffset;
+    float position[3];
+    float normal[3];
+} SstHit;
+
+/* PathTracerBase public settings (Integrators/PathTracer.cs:16-49, Integrator.cs:10-16) plus the
+ * frame buffer size and flags (Images/FrameBuffer.cs:101-133). */
+typedef struct SstPathTracerParams {
+    int32_t width, height;
+    int32_t totalSpp;
+    int32_t maxDepth;
+    int32_t minDepth;
+    uint32_t baseSeed;
+    int32_t numShadowRays;
+    int32_t enableBsdfDI;
+    int32_t ignoreNanAndInf;    /* FrameBuffer.Flags.IgnoreNanAndInf */
+    int32_t firstIteration;     /* iterations already averaged into `film` (resume); 0 = fresh */
+    int64_t maximumRenderTimeMs; /* <= 0: no limit (PathTracer.cs:27, :221-227) */
+} SstPathTracerParams;
+
+/* FrameBuffer.MetaData entries written by PathTracer.Render (PathTracer.cs:254-257). */
+typedef struct SstRenderStats {
+    double renderTimeMs;      /* GPU time of the iterations, frame-buffer work excluded */
+    double frameBufferTimeMs; /* film initialisation / copies */
+    int32_t numIterations;
+    int32_t reserved;
+    uint64_t numRays;       /* RayTracerStats.NumRays */
+    uint64_t numShadowRays; /* RayTracerStats.NumShadowRays */
+    uint64_t numNanOrInf;   /* FrameBuffer.NaNWarnings count */
+    int32_t nanPixel[4];    /* first logged (pixel index) entries, -1 if unused */
+    int32_t nanIteration[4];
+} SstRenderStats;
+
+/* ---- library / context --------------------------------------------------------------------- */
+int sst_version(int32_t* major, int32_t* minor);
+/* Copies the calling thread's last error message (NUL-terminated, truncated to size). */
+int sst_last_error(char* buffer, size_t size);
+
+/* Creates a context on a CUDA device: one stream, the device kernels, scratch pools. */
+int sst_create(int32_t device, sst_ctx** out);
+int sst_destroy(sst_ctx* ctx);
+
+/* ---- scene (Scene.cs:26-58 members, Scene.Prepare :103-164) ---------------------------------- */
+int sst_scene_create(sst_ctx* ctx, sst_scene** out);
+int sst_scene_destroy(sst_scene* scene);
+
+/* RgbImage / MonochromeImage used as TextureRgb / TextureMono (Images/TextureRgb.cs:16-21,
+ * TextureMono.cs:47-58).  data: row-major, top row first, `channels` floats per texel (1 or 3). */
+int sst_scene_add_texture(sst_scene* scene, const float* data, int32_t width, int32_t height, int32_t channels,
+                          int32_t border, int32_t* outTexture);
+
+/* new DiffuseMaterial(Parameters) (Shading/Materials/DiffuseMaterial.cs:10-28). */
+int sst_scene_add_material_diffuse(sst_scene* scene, const float baseColor[3], int32_t baseColorTexture,
+                                   int32_t transmitter, int32_t* outMaterial);
+/* new GenericMaterial(Parameters) (Shading/Materials/GenericMaterial.cs:20). */
+int sst_scene_add_material_generic(sst_scene* scene, const SstGenericMaterial* params, int32_t* outMaterial);
+/* Replaces the parameters of an existing generic material (before or after commit). */
+int sst_scene_update_material_generic(sst_scene* scene, int32_t material, const SstGenericMaterial* params);
+
+/* new Mesh(vertices, indices, shadingNormals, textureCoordinates) + Mesh.Material
+ * (Geometry/Mesh.cs:28-41).  vertices: numVertices*3 floats; indices: numTriangles*3;
+ * shadingNormals (numVertices*3) and textureCoordinates (numVertices*2) may be NULL. */
+int sst_scene_add_mesh(sst_scene* scene, const float* vertices, int32_t numVertices, const int32_t* indices,
+                       int32_t numTriangles, const float* shadingNormals, const float* textureCoordinates,
+                       int32_t material, int32_t* outMesh);
+
+/* Scene.Emitters.AddRange(DiffuseEmitter.MakeFromMesh(mesh, radiance)) when glossyExponent < 0,
+ * GlossyEmitter.MakeFromMesh(mesh, radiance, exponent) otherwise (Shading/Emitters/
+ * DiffuseEmitter.cs:21-31, GlossyEmitter.cs:24-34).  faces == NULL: every face of the mesh,
+ * zero-area faces skipped; otherwise exactly the listed faces, and a zero-area face is an error
+ * (Geometry/Triangle.cs:32-33).  Emitters are appended in order; outFirst receives the index of
+ * the first one, outCount how many were added. */
+int sst_scene_add_emitters(sst_scene* scene, int32_t mesh, const int32_t* faces, int32_t numFaces,
+                           const float radiance[3], float glossyExponent, int32_t* outFirst, int32_t* outCount);
+/* Overwrites the radiance of emitters [first, first + count) (rgb: count*3 floats). */
+int sst_scene_set_emitter_radiance(sst_scene* scene, int32_t first, int32_t count, const float* rgb);
+
+/* Scene.Background = new EnvironmentMap(image) (Shading/Background/EnvironmentMap.cs:14-17).
+ * rgb: width*height*3 floats, top row first. */
+int sst_scene_set_envmap(sst_scene* scene, const float* rgb, int32_t width, int32_t height);
+
+/* Scene.Camera = new PerspectiveCamera(worldToCamera, verticalFieldOfView)
+ * (Cameras/PerspectiveCamera.cs:32-37).  worldToCamera: System.Numerics.Matrix4x4 in row-major
+ * order M11..M44 (row-vector convention). */
+int sst_scene_set_camera(sst_scene* scene, const float worldToCamera[16], float verticalFovDegrees);
+
+/* Scene.Prepare() with FrameBuffer (width, height): validates, uploads, builds the BVH and the
+ * environment-map sampling tables, and updates the camera resolution. */
+int sst_scene_commit(sst_scene* scene, int32_t width, int32_t height);
+
+/* Number of emitters / triangles / BVH nodes in a committed scene (any pointer may be NULL). */
+int sst_scene_info(sst_scene* scene, int32_t* numEmitters, int32_t* numTriangles, int32_t* numBvhNodes);
+
+/* ---- ray queries (TinyEmbree Raytracer.Trace / IsOccluded, PathTracer.cs:319,467) ----------- */
+int sst_trace(sst_scene* scene, const SstRay* rays, int32_t n, SstHit* hits, int32_t memory);
+int sst_occluded(sst_scene* scene, const SstRay* rays, int32_t n, int32_t* occluded, int32_t memory);
+
+/* ---- rendering (PathTracerBase.Render, PathTracer.cs:199-267) -------------------------------- */
+/* Renders iterations [firstIteration, totalSpp) into film (width*height*3 floats, row-major,
+ * top row first) with the frame buffer's running mean.  When firstIteration > 0 the film must
+ * hold the mean of the first `firstIteration` iterations.  stats may be NULL. */
+int sst_render(sst_scene* scene, const SstPathTracerParams* params, float* film, int32_t memory,
+               SstRenderStats* stats);
+
+/* One render job of a batch. */
+typedef struct SstRenderJob {
+    sst_scene* scene;
+    SstPathTracerParams params;
+    float* film;
+    int32_t memory;
+    int32_t reserved;
+} SstRenderJob;
+/* Renders many independent jobs (uneven resolutions, spp and depths) in one persistent
+ * wavefront: all jobs' paths share the ray queues.  Films as in sst_render. */
+int sst_render_batch(sst_ctx* ctx, const SstRenderJob* jobs, int32_t numJobs, SstRenderStats* stats);
+
+/* ---- function-level entry points used by the parity tests --------------------------------------
+ * Each runs the device code of one reference function on a batch of inputs (host arrays). */
+/* Material.EvaluateWithCosine + Material.Pdf (Material.cs:80-83).  points: n*11 floats
+ * (position 3, face normal 3, shading normal 3, uv 2); out/in dirs: n*3; values n*3; pdfs n*2. */
+int sst_debug_material_eval(sst_scene* scene, int32_t material, int32_t n, const float* points, const float* outDirs,
+                            const float* inDirs, float* values, float* pdfs);
+/* Material.Sample (GenericMaterial.cs:92-150, DiffuseMaterial.cs:127-164).  u: n*3 (component,
+ * direction x, direction y); dirs n*3, pdfs n*2, weights n*3. */
+int sst_debug_material_sample(sst_scene* scene, int32_t material, int32_t n, const float* points, const float* outDirs,
+                              const float* u, float* dirs, float* pdfs, float* weights);
+/* EnvironmentMap.SampleDirection / DirectionPdf / EmittedRadiance (EnvironmentMap.cs:19-85).
+ * u: n*2 -> dirs n*3, pdfs n, weights n*3; queryDirs n*3 -> radiance n*3, queryPdfs n. */
+int sst_debug_envmap(sst_scene* scene, int32_t n, const float* u, float* dirs, float* pdfs, float* weights,
+                     const float* queryDirs, float* radiance, float* queryPdfs);
+/* RNG(baseSeed, pixels[i], sampleIndex) followed by `draws` Next() calls (Sampling/RNG.cs). */
+int sst_debug_rng(uint32_t baseSeed, uint32_t sampleIndex, int32_t n, const uint32_t* pixels, int32_t draws,
+                  uint32_t* out);
+/* PerspectiveCamera.GenerateRay for film positions (n*2) -> origins, directions (n*3 each). */
+int sst_debug_camera(sst_scene* scene, int32_t n, const float* filmPos, float* origins, float* directions);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SST_H */

@@ -1,0 +1,15 @@
+"""seesharp_gb300: SeeSharp's unidirectional PathTracer as a GB300 (sm_103a) wavefront renderer.
+
+The Python classes mirror SeeSharp's scene and integrator API; rendering and ray queries run in
+libsst.so (CUDA, C ABI in include/sst.h).
+"""
+from .images import (BorderHandling, FrameBuffer, MonochromeImage, RgbColor, RgbImage, TextureMono, TextureRgb, mean_rgb,
+                     rel_mse)
+from .integrators import Integrator, PathTracer
+from .scene import (ArgumentException, DiffuseEmitter, DiffuseMaterial, EnvironmentMap, GenericMaterial, GlossyEmitter,
+                    InvalidOperationException, Matrix4x4, Mesh, PerspectiveCamera, Scene, Triangle)
+
+__all__ = ["BorderHandling", "FrameBuffer", "MonochromeImage", "RgbColor", "RgbImage", "TextureMono", "TextureRgb", "mean_rgb",
+           "rel_mse", "Integrator", "PathTracer", "ArgumentException", "DiffuseEmitter", "DiffuseMaterial", "EnvironmentMap",
+           "GenericMaterial", "GlossyEmitter", "InvalidOperationException", "Matrix4x4", "Mesh", "PerspectiveCamera", "Scene",
+           "Triangle"]

@@ -1,0 +1,315 @@
+"""ctypes binding of libsst.so (declarations in include/sst.h).
+
+The library is built in-tree by seesharp_gb300/build.py.  Loading fails loudly when it is
+missing or when no CUDA device can be opened: there is no CPU fallback behind this package.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import threading
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libsst.so")
+
+SST_MEM_HOST = 0
+SST_MEM_DEVICE = 1
+
+_ERRORS = {
+    -1: "invalid argument",
+    -2: "invalid scene",
+    -3: "CUDA error",
+    -4: "out of memory",
+    -5: "scene not committed",
+    -6: "device limit reached",
+    -7: "unsupported",
+}
+
+
+class SstError(RuntimeError):
+    def __init__(self, code, message):
+        super().__init__(f"libsst error {code} ({_ERRORS.get(code, '?')}): {message}")
+        self.code = code
+
+
+class SstGenericMaterial(ctypes.Structure):
+    _fields_ = [("baseColor", ctypes.c_float * 3), ("baseColorTexture", ctypes.c_int32), ("roughness", ctypes.c_float),
+                ("roughnessTexture", ctypes.c_int32), ("metallic", ctypes.c_float), ("specularTintStrength", ctypes.c_float),
+                ("anisotropic", ctypes.c_float), ("specularTransmittance", ctypes.c_float), ("indexOfRefraction", ctypes.c_float)]
+
+
+class SstRay(ctypes.Structure):
+    _fields_ = [("org", ctypes.c_float * 3), ("tmin", ctypes.c_float), ("dir", ctypes.c_float * 3), ("tmax", ctypes.c_float)]
+
+
+class SstHit(ctypes.Structure):
+    _fields_ = [("distance", ctypes.c_float), ("u", ctypes.c_float), ("v", ctypes.c_float), ("primId", ctypes.c_int32),
+                ("meshId", ctypes.c_int32), ("errorOffset", ctypes.c_float), ("position", ctypes.c_float * 3),
+                ("normal", ctypes.c_float * 3)]
+
+
+class SstPathTracerParams(ctypes.Structure):
+    _fields_ = [("width", ctypes.c_int32), ("height", ctypes.c_int32), ("totalSpp", ctypes.c_int32), ("maxDepth", ctypes.c_int32),
+                ("minDepth", ctypes.c_int32), ("baseSeed", ctypes.c_uint32), ("numShadowRays", ctypes.c_int32),
+                ("enableBsdfDI", ctypes.c_int32), ("ignoreNanAndInf", ctypes.c_int32), ("firstIteration", ctypes.c_int32),
+                ("maximumRenderTimeMs", ctypes.c_int64)]
+
+
+class SstRenderStats(ctypes.Structure):
+    _fields_ = [("renderTimeMs", ctypes.c_double), ("frameBufferTimeMs", ctypes.c_double), ("numIterations", ctypes.c_int32),
+                ("reserved", ctypes.c_int32), ("numRays", ctypes.c_uint64), ("numShadowRays", ctypes.c_uint64),
+                ("numNanOrInf", ctypes.c_uint64), ("nanPixel", ctypes.c_int32 * 4), ("nanIteration", ctypes.c_int32 * 4)]
+
+
+class SstRenderJob(ctypes.Structure):
+    _fields_ = [("scene", ctypes.c_void_p), ("params", SstPathTracerParams), ("film", ctypes.c_void_p), ("memory", ctypes.c_int32),
+                ("reserved", ctypes.c_int32)]
+
+
+# Every exported symbol with its argument types (restype int unless noted).
+_P = ctypes.POINTER
+_vp = ctypes.c_void_p
+_i32 = ctypes.c_int32
+_u32 = ctypes.c_uint32
+_f = ctypes.c_float
+_fp = _P(ctypes.c_float)
+SIGNATURES = {
+    "sst_version": [_P(_i32), _P(_i32)],
+    "sst_last_error": [ctypes.c_char_p, ctypes.c_size_t],
+    "sst_create": [_i32, _P(_vp)],
+    "sst_destroy": [_vp],
+    "sst_scene_create": [_vp, _P(_vp)],
+    "sst_scene_destroy": [_vp],
+    "sst_scene_add_texture": [_vp, _vp, _i32, _i32, _i32, _i32, _P(_i32)],
+    "sst_scene_add_material_diffuse": [_vp, _fp, _i32, _i32, _P(_i32)],
+    "sst_scene_add_material_generic": [_vp, _P(SstGenericMaterial), _P(_i32)],
+    "sst_scene_update_material_generic": [_vp, _i32, _P(SstGenericMaterial)],
+    "sst_scene_add_mesh": [_vp, _vp, _i32, _vp, _i32, _vp, _vp, _i32, _P(_i32)],
+    "sst_scene_add_emitters": [_vp, _i32, _vp, _i32, _fp, _f, _P(_i32), _P(_i32)],
+    "sst_scene_set_emitter_radiance": [_vp, _i32, _i32, _vp],
+    "sst_scene_set_envmap": [_vp, _vp, _i32, _i32],
+    "sst_scene_set_camera": [_vp, _fp, _f],
+    "sst_scene_commit": [_vp, _i32, _i32],
+    "sst_scene_info": [_vp, _P(_i32), _P(_i32), _P(_i32)],
+    "sst_trace": [_vp, _vp, _i32, _vp, _i32],
+    "sst_occluded": [_vp, _vp, _i32, _vp, _i32],
+    "sst_render": [_vp, _P(SstPathTracerParams), _vp, _i32, _P(SstRenderStats)],
+    "sst_render_batch": [_vp, _P(SstRenderJob), _i32, _P(SstRenderStats)],
+    "sst_debug_material_eval": [_vp, _i32, _i32, _vp, _vp, _vp, _vp, _vp],
+    "sst_debug_material_sample": [_vp, _i32, _i32, _vp, _vp, _vp, _vp, _vp, _vp],
+    "sst_debug_envmap": [_vp, _i32, _vp, _vp, _vp, _vp, _vp, _vp, _vp],
+    "sst_debug_rng": [_u32, _u32, _i32, _vp, _i32, _vp],
+    "sst_debug_camera": [_vp, _i32, _vp, _vp, _vp],
+}
+
+_lib = None
+_lib_lock = threading.Lock()
+
+
+def load_library(path=None):
+    """Loads libsst.so and declares its prototypes.  Raises if the library is absent."""
+    global _lib
+    with _lib_lock:
+        if _lib is not None:
+            return _lib
+        p = path or LIB_PATH
+        if not os.path.exists(p):
+            raise ImportError(f"libsst.so not found at {p}; build it with `python -m seesharp_gb300.build`")
+        lib = ctypes.CDLL(p)
+        for name, args in SIGNATURES.items():
+            fn = getattr(lib, name)
+            fn.argtypes = args
+            fn.restype = ctypes.c_int
+        _lib = lib
+        return lib
+
+
+def last_error():
+    buf = ctypes.create_string_buffer(1024)
+    load_library().sst_last_error(buf, len(buf))
+    return buf.value.decode(errors="replace")
+
+
+def check(code):
+    if code != 0:
+        raise SstError(code, last_error())
+    return code
+
+
+def ptr(a):
+    """Host pointer of a contiguous numpy array (or None)."""
+    if a is None:
+        return None
+    assert a.flags["C_CONTIGUOUS"]
+    return ctypes.c_void_p(a.ctypes.data)
+
+
+def fptr(a):
+    return a.ctypes.data_as(ctypes.POINTER(ctypes.c_float))
+
+
+class Context:
+    """An sst_ctx on one CUDA device."""
+
+    def __init__(self, device=0):
+        self.lib = load_library()
+        h = ctypes.c_void_p()
+        check(self.lib.sst_create(int(device), ctypes.byref(h)))
+        self.handle = h
+        self.device = device
+
+    def close(self):
+        if self.handle:
+            self.lib.sst_destroy(self.handle)
+            self.handle = None
+
+
+_contexts = {}
+
+
+def default_context(device=0):
+    ctx = _contexts.get(device)
+    if ctx is None:
+        ctx = Context(device)
+        _contexts[device] = ctx
+    return ctx
+
+
+class SceneHandle:
+    """An sst_scene: thin wrappers of the sst_scene_* calls for the Python scene model."""
+
+    def __init__(self, ctx):
+        self.ctx = ctx
+        self.lib = ctx.lib
+        h = ctypes.c_void_p()
+        check(self.lib.sst_scene_create(ctx.handle, ctypes.byref(h)))
+        self.handle = h
+        self._textures = {}
+
+    def close(self):
+        if self.handle:
+            self.lib.sst_scene_destroy(self.handle)
+            self.handle = None
+
+    # -- textures and materials --
+    def add_texture(self, image, border):
+        key = (id(image), int(border))
+        if key in self._textures:
+            return self._textures[key]
+        d = np.ascontiguousarray(image.data, np.float32)
+        out = ctypes.c_int32()
+        check(self.lib.sst_scene_add_texture(self.handle, ptr(d), d.shape[1], d.shape[0], d.shape[2], int(border), ctypes.byref(out)))
+        self._textures[key] = out.value
+        return out.value
+
+    def _tex_rgb(self, tex):
+        if tex.Image is None:
+            return tex.constColor.array(), -1
+        return np.zeros(3, np.float32), self.add_texture(tex.Image, tex.Border)
+
+    def _tex_mono(self, tex):
+        if tex.Image is None:
+            return tex.constColor, -1
+        return 0.0, self.add_texture(tex.Image, tex.Border)
+
+    def generic_params(self, p):
+        s = SstGenericMaterial()
+        c, t = self._tex_rgb(p.BaseColor)
+        s.baseColor[:] = [float(x) for x in c]
+        s.baseColorTexture = t
+        r, rt = self._tex_mono(p.Roughness)
+        s.roughness = r
+        s.roughnessTexture = rt
+        s.metallic = p.Metallic
+        s.specularTintStrength = p.SpecularTintStrength
+        s.anisotropic = p.Anisotropic
+        s.specularTransmittance = p.SpecularTransmittance
+        s.indexOfRefraction = p.IndexOfRefraction
+        return s
+
+    def add_material(self, mat):
+        from .scene import DiffuseMaterial, GenericMaterial
+        out = ctypes.c_int32()
+        if isinstance(mat, DiffuseMaterial):
+            c, t = self._tex_rgb(mat.MaterialParameters.BaseColor)
+            c = np.ascontiguousarray(c, np.float32)
+            check(self.lib.sst_scene_add_material_diffuse(self.handle, fptr(c), t, int(mat.MaterialParameters.Transmitter), ctypes.byref(out)))
+        elif isinstance(mat, GenericMaterial):
+            s = self.generic_params(mat.MaterialParameters)
+            check(self.lib.sst_scene_add_material_generic(self.handle, ctypes.byref(s), ctypes.byref(out)))
+        else:
+            raise TypeError(f"unsupported material type {type(mat).__name__}")
+        return out.value
+
+    def update_generic(self, material_id, params):
+        s = self.generic_params(params)
+        check(self.lib.sst_scene_update_material_generic(self.handle, int(material_id), ctypes.byref(s)))
+
+    def add_mesh(self, mesh, material_id):
+        out = ctypes.c_int32()
+        check(self.lib.sst_scene_add_mesh(self.handle, ptr(mesh.Vertices), mesh.NumVertices, ptr(mesh.Indices), mesh.NumFaces,
+                                          ptr(mesh.ShadingNormals), ptr(mesh.TextureCoordinates), int(material_id), ctypes.byref(out)))
+        return out.value
+
+    def add_emitters(self, mesh_id, faces, radiance, exponent):
+        first, count = ctypes.c_int32(), ctypes.c_int32()
+        rad = np.ascontiguousarray(radiance, np.float32)
+        fa = None if faces is None else np.ascontiguousarray(faces, np.int32)
+        n = 0 if fa is None else fa.size
+        check(self.lib.sst_scene_add_emitters(self.handle, int(mesh_id), ptr(fa), n, fptr(rad), float(exponent), ctypes.byref(first),
+                                              ctypes.byref(count)))
+        return first.value
+
+    def set_emitter_radiance(self, first, rgb):
+        rgb = np.ascontiguousarray(rgb, np.float32).reshape(-1, 3)
+        check(self.lib.sst_scene_set_emitter_radiance(self.handle, int(first), rgb.shape[0], ptr(rgb)))
+
+    def set_envmap(self, data):
+        d = np.ascontiguousarray(data, np.float32)
+        check(self.lib.sst_scene_set_envmap(self.handle, ptr(d), d.shape[1], d.shape[0]))
+
+    def set_camera(self, m, fov):
+        mm = np.ascontiguousarray(np.asarray(m, np.float32).reshape(16))
+        check(self.lib.sst_scene_set_camera(self.handle, fptr(mm), float(fov)))
+
+    def commit(self, width, height):
+        check(self.lib.sst_scene_commit(self.handle, int(width), int(height)))
+
+    def info(self):
+        a, b, c = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32()
+        check(self.lib.sst_scene_info(self.handle, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)))
+        return {"emitters": a.value, "triangles": b.value, "bvh_nodes": c.value}
+
+    # -- queries --
+    def trace(self, rays):
+        """rays: (n, 8) float32 (org, tmin, dir, tmax) -> structured hits (n, 12) float32 view."""
+        rays = np.ascontiguousarray(rays, np.float32).reshape(-1, 8)
+        hits = np.zeros((rays.shape[0], 12), np.float32)
+        check(self.lib.sst_trace(self.handle, ptr(rays), rays.shape[0], ptr(hits), SST_MEM_HOST))
+        return hits
+
+    def occluded(self, rays):
+        rays = np.ascontiguousarray(rays, np.float32).reshape(-1, 8)
+        occ = np.zeros(rays.shape[0], np.int32)
+        check(self.lib.sst_occluded(self.handle, ptr(rays), rays.shape[0], ptr(occ), SST_MEM_HOST))
+        return occ
+
+    def render(self, params, film, memory=SST_MEM_HOST):
+        stats = SstRenderStats()
+        check(self.lib.sst_render(self.handle, ctypes.byref(params), ctypes.c_void_p(film), int(memory), ctypes.byref(stats)))
+        return stats
+
+
+def make_params(width, height, totalSpp, maxDepth, minDepth=1, baseSeed=0xC030114, numShadowRays=1, enableBsdfDI=True,
+                ignoreNanAndInf=True, firstIteration=0, maximumRenderTimeMs=0):
+    p = SstPathTracerParams()
+    p.width, p.height, p.totalSpp, p.maxDepth, p.minDepth = width, height, totalSpp, maxDepth, minDepth
+    p.baseSeed = baseSeed & 0xFFFFFFFF
+    p.numShadowRays = numShadowRays
+    p.enableBsdfDI = int(bool(enableBsdfDI))
+    p.ignoreNanAndInf = int(bool(ignoreNanAndInf))
+    p.firstIteration = firstIteration
+    p.maximumRenderTimeMs = int(maximumRenderTimeMs or 0)
+    return p

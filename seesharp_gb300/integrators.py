@@ -1,0 +1,90 @@
+"""Integrator plugin API and the GPU PathTracer.
+
+Mirrors SeeSharp's abstract Integrator (Integrators/Integrator.cs:6-30) and the public settings of
+PathTracerBase (Integrators/PathTracer.cs:16-49).  Render() runs the whole progressive loop on the
+GPU through sst_render; the per-event observer hooks of the reference are not called per path.
+A subclass that overrides a behaviour-changing hook is rejected, because the GPU kernels cannot
+run Python code per path (the reference's hooks at PathTracer.cs:277-530).
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from . import _native
+
+
+class Integrator:
+    """Integrators/Integrator.cs:6-30."""
+
+    def __init__(self):
+        self.MaxDepth = 100
+        self.MinDepth = 1
+
+    def Render(self, scene):
+        raise NotImplementedError
+
+
+_BEHAVIOUR_HOOKS = ("ComputeSurvivalProbability", "RenderPixel", "EstimateIncidentRadiance", "OnBackgroundHit", "OnLightHit",
+                    "PerformBackgroundNextEvent", "PerformNextEventEstimation", "DirectionPdf", "SampleDirection")
+
+
+class PathTracer(Integrator):
+    """Unidirectional path tracer with next-event estimation and balance-heuristic MIS."""
+
+    def __init__(self, **kw):
+        super().__init__()
+        self.BaseSeed = 0xC030114
+        self.TotalSpp = 20
+        self.MaximumRenderTimeMs = None
+        self.NumShadowRays = 1
+        self.EnableBsdfDI = True
+        self.RenderTechniquePyramid = False
+        # The reference denoises the last iteration with Open Image Denoise by default; denoising
+        # is outside this library, so the flag is accepted and has no effect.
+        self.EnableDenoiser = True
+        for k, v in kw.items():
+            if not hasattr(self, k):
+                raise AttributeError(k)
+            setattr(self, k, v)
+
+    # Behaviour-changing hooks exist so that overriding them can be detected.
+    def ComputeSurvivalProbability(self, *a):
+        raise NotImplementedError
+
+    RenderPixel = EstimateIncidentRadiance = OnBackgroundHit = OnLightHit = ComputeSurvivalProbability
+    PerformBackgroundNextEvent = PerformNextEventEstimation = DirectionPdf = SampleDirection = ComputeSurvivalProbability
+
+    def _check_hooks(self):
+        for name in _BEHAVIOUR_HOOKS:
+            if getattr(type(self), name) is not getattr(PathTracer, name):
+                raise NotImplementedError(f"PathTracer.{name} is overridden; the GPU path tracer runs the reference behaviour only")
+        if self.RenderTechniquePyramid:
+            raise NotImplementedError("RenderTechniquePyramid is not supported by the GPU path tracer")
+
+    def params(self, scene):
+        fb = scene.FrameBuffer
+        return _native.make_params(fb.Width, fb.Height, int(self.TotalSpp), int(self.MaxDepth), int(self.MinDepth), int(self.BaseSeed),
+                                   int(self.NumShadowRays), bool(self.EnableBsdfDI), fb.IgnoreNanAndInf, int(fb.CurIteration),
+                                   int(self.MaximumRenderTimeMs or 0))
+
+    def Render(self, scene):
+        """PathTracerBase.Render (PathTracer.cs:199-267): TotalSpp iterations into scene.FrameBuffer."""
+        self._check_hooks()
+        fb = scene.FrameBuffer
+        p = self.params(scene)
+        if fb.CurIteration >= self.TotalSpp:
+            return
+        film = fb.Image.data
+        assert film.dtype == np.float32 and film.flags["C_CONTIGUOUS"]
+        stats = scene.native.render(p, film.ctypes.data)
+        fb.CurIteration = fb.CurIteration + stats.numIterations
+        fb.MetaData["NumIterations"] = fb.CurIteration
+        fb.MetaData["RenderTime"] = stats.renderTimeMs
+        fb.MetaData["FrameBufferTime"] = stats.frameBufferTimeMs
+        fb.MetaData["RayTracerStats"] = {"NumRays": int(stats.numRays), "NumShadowRays": int(stats.numShadowRays)}
+        for k in range(min(4, int(stats.numNanOrInf))):
+            px = stats.nanPixel[k]
+            if px >= 0:
+                fb.NaNWarnings.append((px % fb.Width, px // fb.Width, stats.nanIteration[k]))
+        fb.MetaData["NumNaNOrInf"] = int(stats.numNanOrInf)
+        self.last_stats = stats
