@@ -1,0 +1,345 @@
+"""Benchmark: SeeSharp PathTracer throughput (Msamples/s) on the 1M-triangle sphere field.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference] [--config 1]
+
+A step is one full PathTracer render of the workload (all iterations).  The default workload is
+the 1M-triangle configuration: 200 seeded displaced icospheres (5120 triangles each), 50 emissive
+triangles, a 512x256 procedural HDR sky, 1024x1024 pixels, 64 spp, max depth 8; inputs are
+synthetic and seeded.  `value` is device-timed (CUDA events on the renderer's stream) with the
+scene resident in HBM; `e2e` is measured through the public API (Scene.Prepare + PathTracer.Render
+with host buffers: geometry upload, BVH build, render, film read-back) per step.
+`--impl reference` times the CPU restatement of the reference PathTracer (the oracle) on all
+host cores over a bounded sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+CONFIGS = {
+    0: dict(name="cornell_box_36tri_256x256_16spp_depth5", builder="cornell", W=256, H=256, spp=16, depth=5),
+    1: dict(name="sphere_field_1Mtri_1024x1024_64spp_depth8", builder="spheres", spheres=200, W=1024, H=1024, spp=64, depth=8),
+}
+
+
+def make_scene(cfg):
+    from seesharp_gb300 import workloads
+    if cfg["builder"] == "cornell":
+        return workloads.cornell_box(cfg["W"], cfg["H"])
+    return workloads.sphere_field(cfg["spheres"], cfg["W"], cfg["H"])
+
+
+def scene_bytes(sc):
+    b = 0
+    for m in sc.Meshes:
+        b += m.Vertices.nbytes + m.Indices.nbytes
+        b += 0 if m.ShadingNormals is None else m.ShadingNormals.nbytes
+        b += 0 if m.TextureCoordinates is None else m.TextureCoordinates.nbytes
+    if sc.Background is not None:
+        b += sc.Background.Image.data.nbytes
+    return int(b)
+
+
+def b_ray(ntri):
+    """Algorithmic bytes of one ray query over N triangles: ray in (32) + hit out (16) + one
+    root-to-leaf chain of 64-byte nodes + two leaf triangles (2 x 36)."""
+    return 48 + 64 * math.ceil(math.log2(max(ntri, 2))) + 72
+
+
+class ClockSampler:
+    """Samples nvidia-smi clocks and throttle reasons while the timed region runs."""
+
+    FIELDS = "clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown," \
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap"
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                                          "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx.append(float(parts[1]))
+            except ValueError:
+                continue
+            for k, nm in enumerate(names):
+                if parts[4 + k].lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(mx)), "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_info():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(ws, x):
+    if ws <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def read_profile_traffic(kernel):
+    """Per-ray DRAM traffic of a kernel from the committed ncu summary (profiles/), or None."""
+    path = os.path.join(ROOT, "profiles", "ncu_traffic.txt")
+    if not os.path.exists(path):
+        return None
+    for ln in open(path):
+        parts = ln.split()
+        if len(parts) >= 2 and parts[0] == kernel:
+            try:
+                return float(parts[1])
+            except ValueError:
+                return None
+    return None
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+# ---------------------------------------------------------------------------------------------
+def cpu_sample(cfg, seconds_target=15.0, min_paths=4096, nthreads=None, scene=None):
+    """Times the oracle PathTracer on a bounded strided sample of the workload's paths.
+    Returns (Msamples/s, description, threads)."""
+    from oracle import pyoracle as O
+    sc = scene if scene is not None else make_scene(cfg)
+    o = O.OracleScene.from_scene(sc)
+    p = o.params(cfg["W"], cfg["H"], cfg["spp"], cfg["depth"])
+    nthreads = nthreads or os.cpu_count() or 1
+    npix = cfg["W"] * cfg["H"]
+    # calibrate on a small sample, then size the sample for ~seconds_target
+    n = min_paths
+    pix = np.linspace(0, npix - 1, n).astype(np.int32)
+    t0 = time.perf_counter()
+    o.render_paths(p, 0, pix, nthreads)
+    dt = max(time.perf_counter() - t0, 1e-6)
+    n = int(min(npix, max(min_paths, n * seconds_target / dt)))
+    pix = np.linspace(0, npix - 1, n).astype(np.int32)
+    t0 = time.perf_counter()
+    o.render_paths(p, 1, pix, nthreads)
+    dt = time.perf_counter() - t0
+    return n / dt / 1e6, f"{n} strided paths of iteration 1 ({n / npix:.3f} of one spp)", nthreads, o, p, n
+
+
+def run_reference(args, cfg):
+    ws, rank, _ = dist_info()
+    if rank != 0:
+        return
+    from seesharp_gb300 import workloads  # noqa: F401  (scene generator only)
+    sc = make_scene(cfg)
+    nthreads = os.cpu_count() or 1
+    # size one step for a few seconds of CPU work
+    _, _, _, o, p, n = cpu_sample(cfg, seconds_target=max(2.0, 60.0 / max(1, args.steps + args.warmup)), nthreads=nthreads, scene=sc)
+    pix = np.linspace(0, cfg["W"] * cfg["H"] - 1, n).astype(np.int32)
+    for w in range(args.warmup):
+        o.render_paths(p, 2 + w, pix, nthreads)
+    t0 = time.perf_counter()
+    for k in range(args.steps):
+        o.render_paths(p, 100 + k, pix, nthreads)
+    dt = time.perf_counter() - t0
+    val = n * args.steps / dt / 1e6
+    line = {
+        "metric": "Msamples/s PathTracer", "value": round(val, 4), "unit": "Msamples/s", "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(dt / args.steps * 1000, 3), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scene generator)", "impl": "reference",
+        "config": {"workload": cfg["name"]},
+        "cpu_baseline": {"value": round(val, 4), "unit": "Msamples/s", "cores": nthreads, "kind": "port",
+                         "sample": f"{n} strided paths per step of the {cfg['W']}x{cfg['H']} image (one sample each), C++ restatement of the "
+                                   f"reference PathTracer on {nthreads} host threads"},
+        "e2e": {"value": round(val, 4), "unit": "Msamples/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args, cfg):
+    import torch
+
+    ws, rank, local = dist_info()
+    if ws > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local)) if False else dist.init_process_group("gloo")
+    torch.cuda.set_device(local)
+    from seesharp_gb300 import PathTracer, _native
+
+    sc = make_scene(cfg)
+    sc.device = local
+    t0 = time.perf_counter()
+    sc.Prepare()
+    prep_s = time.perf_counter() - t0
+    ctx = _native.default_context(local)
+    info = sc.native.info()
+    W, H, spp, depth = cfg["W"], cfg["H"], cfg["spp"], cfg["depth"]
+    samples = W * H * spp
+    film = torch.zeros((H, W, 3), dtype=torch.float32, device=f"cuda:{local}")
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")
+    params = _native.make_params(W, H, spp, depth)
+
+    def step():
+        return sc.native.render(params, film.data_ptr(), _native.SST_MEM_DEVICE)
+
+    for _ in range(args.warmup):
+        step()
+    # timed region: K renders, L2 flushed between them, kernel events on the renderer's stream
+    _native.set_profiling(ctx, True)
+    render_ms, rays, srays = 0.0, 0, 0
+    barrier(ws)
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        wall0 = time.perf_counter()
+        for k in range(args.steps):
+            flush.fill_(float(k))
+            torch.cuda.synchronize()
+            st = step()
+            render_ms += st.renderTimeMs
+            rays += st.numRays
+            srays += st.numShadowRays
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - wall0
+    barrier(ws)
+    ktimes = _native.kernel_times(ctx)
+    _native.set_profiling(ctx, False)
+    ms_per_step = max_over_ranks(ws, render_ms / args.steps)
+    value = samples * ws / (ms_per_step / 1000.0) / 1e6
+
+    # e2e through the public API with host buffers: Prepare (geometry H2D, BVH) + Render (film D2H)
+    from seesharp_gb300 import FrameBuffer
+    e2e_steps = max(1, min(args.steps, 3))
+    h2d = scene_bytes(sc)
+    d2h = W * H * 12
+    barrier(ws)
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        sc.FrameBuffer = FrameBuffer(W, H)
+        sc.Prepare()
+        PathTracer(TotalSpp=spp, MaxDepth=depth).Render(sc)
+    e2e_s = max_over_ranks(ws, (time.perf_counter() - t0) / e2e_steps)
+    e2e_val = samples * ws / e2e_s / 1e6
+    assert np.isfinite(sc.FrameBuffer.Image.data).all()
+
+    # roofline of the dominant traversal kernel
+    peak, peak_kind = measured_peaks()
+    tc = ktimes["trace_closest"]
+    bpr = b_ray(info["triangles"])
+    per_launch_bytes = tc["items"] * bpr / max(tc["launches"], 1)
+    avg_ms = tc["ms"] / max(tc["launches"], 1)
+    achieved = per_launch_bytes / (avg_ms / 1000.0) / 1e9 if avg_ms > 0 else 0.0
+    tpr = read_profile_traffic("trace_closest")
+    roofline = {"kernel": "k_trace<0> (closest-hit BVH traversal)", "bound": "hbm", "achieved": round(achieved, 2), "peak": peak,
+                "unit": "GB/s", "frac": round(achieved / peak, 4), "peak_kind": peak_kind,
+                "traffic": None if tpr is None else round(tpr * tc["items"] / max(tc["launches"], 1)),
+                "algorithmic_bytes_per_ray": bpr, "rays_per_launch": round(tc["items"] / max(tc["launches"], 1)),
+                "avg_launch_ms": round(avg_ms, 4)}
+    # algorithmic bytes per sample (B_sample) from the traced ray counts
+    steps = args.steps
+    ext, sh = rays / steps / samples, srays / steps / samples
+    b_sample = ext * (bpr + 172) + sh * (bpr - 12) + 12
+    launches = sum(v["launches"] for v in ktimes.values())
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        val, desc, thr, _, _, _ = cpu_sample(cfg, seconds_target=args.cpu_seconds, scene=sc)
+        cpu = {"value": round(val, 4), "unit": "Msamples/s", "cores": thr, "kind": "port",
+               "sample": desc + f"; C++ restatement of the reference PathTracer, {thr} threads"}
+    clocks = clk.summary()
+    if rank == 0:
+        line = {
+            "metric": "Msamples/s PathTracer", "value": round(value, 3), "unit": "Msamples/s", "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(ms_per_step, 3), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic (seeded scene generator)",
+            "config": {"workload": cfg["name"], "triangles": info["triangles"], "emitters": info["emitters"], "bvh_nodes": info["bvh_nodes"],
+                       "width": W, "height": H, "spp": spp, "max_depth": depth, "l2": "256 MB buffer written between timed steps",
+                       "parallelism": f"replicas x{ws}"},
+            "e2e": {"value": round(e2e_val, 3), "unit": "Msamples/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                    "s_per_step": round(e2e_s, 4), "includes": "Scene.Prepare (upload + BVH build) + PathTracer.Render (film read-back)"},
+            "roofline": roofline,
+            "bytes_per_sample": round(b_sample, 1), "rays_per_sample": round(ext, 4), "shadow_rays_per_sample": round(sh, 4),
+            "gpu_launches": launches,
+            "kernel_ms": {k: round(v["ms"], 3) for k, v in ktimes.items()},
+            "prepare_s": round(prep_s, 3),
+            "clocks": clocks,
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(line), flush=True)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--config", type=int, default=1, choices=sorted(CONFIGS))
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    cfg = CONFIGS[args.config]
+    if args.impl == "reference":
+        run_reference(args, cfg)
+    else:
+        run_ours(args, cfg)
+
+
+if __name__ == "__main__":
+    main()

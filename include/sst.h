@@ -186,6 +186,16 @@ typedef struct SstRenderJob {
  * wavefront: all jobs' paths share the ray queues.  Films as in sst_render. */
 int sst_render_batch(sst_ctx* ctx, const SstRenderJob* jobs, int32_t numJobs, SstRenderStats* stats);
 
+/* ---- kernel timing ------------------------------------------------------------------------------
+ * With profiling enabled, sst_render records CUDA events around every kernel launch on the
+ * context's stream and accumulates, per kernel class (0 camera, 1 closest-hit traversal,
+ * 2 shade, 3 shadow-ray traversal, 4 film fold), the GPU time in ms, the number of launches and
+ * the number of items (rays or paths) processed.  Enabling it adds a device synchronisation per
+ * wave; disabled by default. */
+#define SST_KERNEL_CLASSES 5
+int sst_set_profiling(sst_ctx* ctx, int32_t enable);
+int sst_get_kernel_times(sst_ctx* ctx, double* ms, int64_t* launches, int64_t* items, int32_t numClasses);
+
 /* ---- function-level entry points used by the parity tests --------------------------------------
  * Each runs the device code of one reference function on a batch of inputs (host arrays). */
 /* Material.EvaluateWithCosine + Material.Pdf (Material.cs:80-83).  points: n*11 floats

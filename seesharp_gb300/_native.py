@@ -97,6 +97,8 @@ SIGNATURES = {
     "sst_occluded": [_vp, _vp, _i32, _vp, _i32],
     "sst_render": [_vp, _P(SstPathTracerParams), _vp, _i32, _P(SstRenderStats)],
     "sst_render_batch": [_vp, _P(SstRenderJob), _i32, _P(SstRenderStats)],
+    "sst_set_profiling": [_vp, _i32],
+    "sst_get_kernel_times": [_vp, _vp, _vp, _vp, _i32],
     "sst_debug_material_eval": [_vp, _i32, _i32, _vp, _vp, _vp, _vp, _vp],
     "sst_debug_material_sample": [_vp, _i32, _i32, _vp, _vp, _vp, _vp, _vp, _vp],
     "sst_debug_envmap": [_vp, _i32, _vp, _vp, _vp, _vp, _vp, _vp, _vp],
@@ -175,6 +177,22 @@ def default_context(device=0):
         ctx = Context(device)
         _contexts[device] = ctx
     return ctx
+
+
+KERNEL_CLASSES = ["camera", "trace_closest", "shade", "trace_shadow", "film_fold"]
+
+
+def set_profiling(ctx, enable):
+    check(ctx.lib.sst_set_profiling(ctx.handle, int(bool(enable))))
+
+
+def kernel_times(ctx):
+    n = len(KERNEL_CLASSES)
+    ms = np.zeros(n, np.float64)
+    la = np.zeros(n, np.int64)
+    it = np.zeros(n, np.int64)
+    check(ctx.lib.sst_get_kernel_times(ctx.handle, ptr(ms), ptr(la), ptr(it), n))
+    return {k: {"ms": float(ms[i]), "launches": int(la[i]), "items": int(it[i])} for i, k in enumerate(KERNEL_CLASSES)}
 
 
 class SceneHandle:

@@ -1,0 +1,1280 @@
+// libsst host driver: the C ABI of include/sst.h.
+//
+// Scene.Prepare (Scene.cs:103-164) becomes sst_scene_commit: the meshes are concatenated into
+// one triangle table, a binned-SAH BVH is built, all per-triangle data are stored in BVH leaf
+// order, and the environment-map sampling tables are built on the GPU.  PathTracerBase.Render
+// (Integrators/PathTracer.cs:199-267) becomes sst_render: the (iteration, pixel) paths are cut
+// into waves that fit the path-state buffers; each wave runs camera -> {closest hit, shade,
+// shadow rays} x depth -> film fold on one CUDA stream.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/sst.h"
+#include "sst_kernels.h"
+#include "sst_types.h"
+
+using namespace sst;
+
+// ---------------------------------------------------------------------------------------------
+// errors
+// ---------------------------------------------------------------------------------------------
+static thread_local std::string g_lastError;
+
+struct SstException {
+    int code;
+    std::string msg;
+};
+static void fail(int code, const std::string& msg) { throw SstException{code, msg}; }
+#define CUDA_CHECK(x)                                                                                         \
+    do {                                                                                                      \
+        cudaError_t e_ = (x);                                                                                 \
+        if (e_ != cudaSuccess) {                                                                              \
+            fail(e_ == cudaErrorMemoryAllocation ? SST_ERR_OUT_OF_MEMORY : SST_ERR_CUDA,                      \
+                 std::string(#x) + ": " + cudaGetErrorString(e_));                                            \
+        }                                                                                                     \
+    } while (0)
+
+template <class F> static int guarded(F&& f) {
+    try {
+        f();
+        return SST_OK;
+    } catch (const SstException& e) {
+        g_lastError = e.msg;
+        return e.code;
+    } catch (const std::bad_alloc&) {
+        g_lastError = "host out of memory";
+        return SST_ERR_OUT_OF_MEMORY;
+    } catch (const std::exception& e) {
+        g_lastError = e.what();
+        return SST_ERR_INVALID_ARGUMENT;
+    }
+}
+
+// ---------------------------------------------------------------------------------------------
+// device buffers
+// ---------------------------------------------------------------------------------------------
+struct DevBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+    DevBuf() = default;
+    DevBuf(const DevBuf&) = delete;
+    DevBuf& operator=(const DevBuf&) = delete;
+    ~DevBuf() { release(); }
+    void release() {
+        if (p) cudaFree(p);
+        p = nullptr;
+        bytes = 0;
+    }
+    void ensure(size_t b) {
+        if (b <= bytes) return;
+        release();
+        CUDA_CHECK(cudaMalloc(&p, b));
+        bytes = b;
+    }
+    template <class T> void upload(const std::vector<T>& v, cudaStream_t s) {
+        ensure(std::max<size_t>(1, v.size() * sizeof(T)));
+        if (!v.empty()) CUDA_CHECK(cudaMemcpyAsync(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, s));
+    }
+    template <class T> T* as() const { return static_cast<T*>(p); }
+};
+
+// ---------------------------------------------------------------------------------------------
+// context
+// ---------------------------------------------------------------------------------------------
+struct sst_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    int numSMs = 0;
+    // wavefront buffers
+    DevBuf pathA[8], pathB[8];
+    DevBuf hits, nee, shRo, shRd, shTgt, counters, samples, stats, film;
+    int cap = 0, shCap = 0, neeSlots = 0;
+    size_t sampleCap = 0;
+    DevBuf scratchIn, scratchOut, scratchOut2;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    int* pinnedCount = nullptr;
+    // kernel timing (sst_set_profiling)
+    bool profiling = false;
+    std::vector<cudaEvent_t> evPool;
+    std::vector<std::pair<int, int>> evMarks;  // (class, event index of the start)
+    double kMs[SST_KERNEL_CLASSES] = {};
+    int64_t kLaunches[SST_KERNEL_CLASSES] = {};
+    int64_t kItems[SST_KERNEL_CLASSES] = {};
+};
+
+// Kernel timing: an event pair around each launch, read back after the wave.
+struct KTimer {
+    sst_ctx* c;
+    int cls;
+    int start;
+    KTimer(sst_ctx* ctx, int k) : c(ctx), cls(k), start(-1) {
+        if (!c->profiling) return;
+        start = int(c->evMarks.size()) * 2;
+        while (int(c->evPool.size()) < start + 2) {
+            cudaEvent_t e;
+            CUDA_CHECK(cudaEventCreate(&e));
+            c->evPool.push_back(e);
+        }
+        CUDA_CHECK(cudaEventRecord(c->evPool[start], c->stream));
+    }
+    ~KTimer() {
+        if (start < 0) return;
+        cudaEventRecord(c->evPool[start + 1], c->stream);
+        c->evMarks.push_back({cls, start});
+        c->kLaunches[cls]++;
+    }
+};
+static void flushTimers(sst_ctx* c) {
+    if (!c->profiling || c->evMarks.empty()) return;
+    CUDA_CHECK(cudaStreamSynchronize(c->stream));
+    for (auto& m : c->evMarks) {
+        float ms = 0;
+        CUDA_CHECK(cudaEventElapsedTime(&ms, c->evPool[m.second], c->evPool[m.second + 1]));
+        c->kMs[m.first] += ms;
+    }
+    c->evMarks.clear();
+}
+
+struct HostMesh {
+    std::vector<float> V, N, UV;
+    std::vector<int> I;
+    int material = -1;
+    std::vector<float> faceN;  // 3 per face
+};
+struct HostEmitter {
+    int mesh, face;
+    float rad[3];
+    float exponent;
+};
+struct HostTexture {
+    int w, h, ch, border;
+    std::vector<float> data;
+};
+
+struct sst_scene {
+    sst_ctx* ctx = nullptr;
+    std::vector<HostTexture> textures;
+    std::vector<DevMaterial> materials;
+    std::vector<HostMesh> meshes;
+    std::vector<HostEmitter> emitters;
+    std::vector<float> envRgb;
+    int envW = 0, envH = 0;
+    float w2c[16] = {};
+    float fovDeg = 0;
+    bool cameraSet = false;
+    bool committed = false;
+    int W = 0, H = 0;
+    // device
+    DevBuf nodes, triv, triN, triAux, triVtx, vnrm, vuv, mats, texs, texData, ems, envImg, envRowCdf, envColCdf, envHasCol, envRowMarg;
+    DevScene dev{};
+    int nTri = 0, nNodes = 0;
+    std::vector<int> meshTriOffset;
+};
+
+// ---------------------------------------------------------------------------------------------
+// host math: 4x4 inverse (Laplace expansion over 2x2 minors), perspective matrix
+// ---------------------------------------------------------------------------------------------
+static bool invert4(const float* m, float* out) {
+    float s0 = m[0] * m[5] - m[4] * m[1];
+    float s1 = m[0] * m[6] - m[4] * m[2];
+    float s2 = m[0] * m[7] - m[4] * m[3];
+    float s3 = m[1] * m[6] - m[5] * m[2];
+    float s4 = m[1] * m[7] - m[5] * m[3];
+    float s5 = m[2] * m[7] - m[6] * m[3];
+    float c5 = m[10] * m[15] - m[14] * m[11];
+    float c4 = m[9] * m[15] - m[13] * m[11];
+    float c3 = m[9] * m[14] - m[13] * m[10];
+    float c2 = m[8] * m[15] - m[12] * m[11];
+    float c1 = m[8] * m[14] - m[12] * m[10];
+    float c0 = m[8] * m[13] - m[12] * m[9];
+    float det = s0 * c5 - s1 * c4 + s2 * c3 + s3 * c2 - s4 * c1 + s5 * c0;
+    if (!(std::fabs(det) > 0.0f) || !std::isfinite(det)) return false;
+    float id = 1.0f / det;
+    out[0] = (m[5] * c5 - m[6] * c4 + m[7] * c3) * id;
+    out[1] = (-m[1] * c5 + m[2] * c4 - m[3] * c3) * id;
+    out[2] = (m[13] * s5 - m[14] * s4 + m[15] * s3) * id;
+    out[3] = (-m[9] * s5 + m[10] * s4 - m[11] * s3) * id;
+    out[4] = (-m[4] * c5 + m[6] * c2 - m[7] * c1) * id;
+    out[5] = (m[0] * c5 - m[2] * c2 + m[3] * c1) * id;
+    out[6] = (-m[12] * s5 + m[14] * s2 - m[15] * s1) * id;
+    out[7] = (m[8] * s5 - m[10] * s2 + m[11] * s1) * id;
+    out[8] = (m[4] * c4 - m[5] * c2 + m[7] * c0) * id;
+    out[9] = (-m[0] * c4 + m[1] * c2 - m[3] * c0) * id;
+    out[10] = (m[12] * s4 - m[13] * s2 + m[15] * s0) * id;
+    out[11] = (-m[8] * s4 + m[9] * s2 - m[11] * s0) * id;
+    out[12] = (-m[4] * c3 + m[5] * c1 - m[6] * c0) * id;
+    out[13] = (m[0] * c3 - m[1] * c1 + m[2] * c0) * id;
+    out[14] = (-m[12] * s3 + m[13] * s1 - m[14] * s0) * id;
+    out[15] = (m[8] * s3 - m[9] * s1 + m[10] * s0) * id;
+    return true;
+}
+// Matrix4x4.CreatePerspectiveFieldOfView (right-handed), PerspectiveCamera.cs:42-52
+static void perspective(float fov, float aspect, float n, float f, float* m) {
+    std::fill(m, m + 16, 0.0f);
+    float y = 1.0f / std::tan(fov * 0.5f);
+    float x = y / aspect;
+    float nfr = f / (n - f);
+    m[0] = x;
+    m[5] = y;
+    m[10] = nfr;
+    m[11] = -1.0f;
+    m[14] = n * nfr;
+}
+
+// ---------------------------------------------------------------------------------------------
+// binned-SAH BVH (host build)
+// ---------------------------------------------------------------------------------------------
+struct Aabb {
+    float lo[3] = {1e30f, 1e30f, 1e30f}, hi[3] = {-1e30f, -1e30f, -1e30f};
+    void grow(const Aabb& b) {
+        for (int k = 0; k < 3; ++k) { lo[k] = std::min(lo[k], b.lo[k]); hi[k] = std::max(hi[k], b.hi[k]); }
+    }
+    void grow(const float* p) {
+        for (int k = 0; k < 3; ++k) { lo[k] = std::min(lo[k], p[k]); hi[k] = std::max(hi[k], p[k]); }
+    }
+    float area() const {
+        float dx = std::max(0.f, hi[0] - lo[0]), dy = std::max(0.f, hi[1] - lo[1]), dz = std::max(0.f, hi[2] - lo[2]);
+        return dx * dy + dy * dz + dz * dx;
+    }
+};
+
+struct BvhBuilder {
+    std::vector<Aabb> box;
+    std::vector<float> cen;  // 3 per prim
+    std::vector<int> order;
+    std::vector<float4> nodes;
+    int maxDepth = 0;
+
+    uint32_t leafRef(int first, int count) { return kLeafFlag | (uint32_t(count - 1) << kLeafCountShift) | uint32_t(first); }
+
+    Aabb rangeBox(int first, int count, Aabb* cbox) {
+        Aabb b, c;
+        for (int i = first; i < first + count; ++i) {
+            b.grow(box[order[i]]);
+            c.grow(&cen[3 * size_t(order[i])]);
+        }
+        if (cbox) *cbox = c;
+        return b;
+    }
+
+    void setChild(int node, int which, const Aabb& b, uint32_t ref) {
+        float4* n = &nodes[4 * size_t(node)];
+        if (which == 0) {
+            n[0].x = b.lo[0]; n[0].y = b.hi[0]; n[0].z = b.lo[1]; n[0].w = b.hi[1];
+            n[2].x = b.lo[2]; n[2].y = b.hi[2];
+            n[3].x = __uint_as_float_host(ref);
+        } else {
+            n[1].x = b.lo[0]; n[1].y = b.hi[0]; n[1].z = b.lo[1]; n[1].w = b.hi[1];
+            n[2].z = b.lo[2]; n[2].w = b.hi[2];
+            n[3].y = __uint_as_float_host(ref);
+        }
+    }
+    static float __uint_as_float_host(uint32_t u) { float f; std::memcpy(&f, &u, 4); return f; }
+
+    // Chooses a split of [first, first+count); returns the split position or -1 for a leaf.
+    int split(int first, int count, const Aabb& b, const Aabb& cb, int depth) {
+        const int kBins = 16;
+        if (count <= 1) return -1;
+        float leafCost = float(count);
+        int bestAxis = -1, bestBin = -1;
+        float bestCost = 1e30f;
+        float pa = b.area();
+        bool forceMedian = depth >= 32;
+        if (!forceMedian) {
+            for (int ax = 0; ax < 3; ++ax) {
+                float ext = cb.hi[ax] - cb.lo[ax];
+                if (!(ext > 0.0f)) continue;
+                Aabb bb[kBins];
+                int bc[kBins] = {};
+                float sc = kBins / ext;
+                for (int i = first; i < first + count; ++i) {
+                    int p = order[i];
+                    int k = std::min(kBins - 1, int((cen[3 * size_t(p) + ax] - cb.lo[ax]) * sc));
+                    bc[k]++;
+                    bb[k].grow(box[p]);
+                }
+                float rArea[kBins];
+                int rCnt[kBins];
+                Aabb acc;
+                int n = 0;
+                for (int k = kBins - 1; k > 0; --k) {
+                    acc.grow(bb[k]);
+                    n += bc[k];
+                    rArea[k] = acc.area();
+                    rCnt[k] = n;
+                }
+                Aabb lacc;
+                int ln = 0;
+                for (int k = 0; k < kBins - 1; ++k) {
+                    lacc.grow(bb[k]);
+                    ln += bc[k];
+                    if (ln == 0 || rCnt[k + 1] == 0) continue;
+                    float cost = 1.0f + (lacc.area() * ln + rArea[k + 1] * rCnt[k + 1]) / std::max(pa, 1e-30f);
+                    if (cost < bestCost) { bestCost = cost; bestAxis = ax; bestBin = k; }
+                }
+            }
+        }
+        if (bestAxis >= 0 && count <= kMaxLeafSize && leafCost <= bestCost) return -1;
+        int mid;
+        if (bestAxis >= 0) {
+            float ext = cb.hi[bestAxis] - cb.lo[bestAxis];
+            float sc = kBins / ext;
+            auto pred = [&](int p) { return std::min(kBins - 1, int((cen[3 * size_t(p) + bestAxis] - cb.lo[bestAxis]) * sc)) <= bestBin; };
+            mid = int(std::partition(order.begin() + first, order.begin() + first + count, pred) - order.begin());
+        } else {
+            if (count <= kMaxLeafSize && !forceMedian) return -1;
+            int ax = 0;
+            float e = -1;
+            for (int k = 0; k < 3; ++k)
+                if (cb.hi[k] - cb.lo[k] > e) { e = cb.hi[k] - cb.lo[k]; ax = k; }
+            mid = first + count / 2;
+            std::nth_element(order.begin() + first, order.begin() + mid, order.begin() + first + count,
+                             [&](int a, int c) { return cen[3 * size_t(a) + ax] < cen[3 * size_t(c) + ax]; });
+        }
+        if (mid <= first || mid >= first + count) mid = first + count / 2;
+        return mid;
+    }
+
+    // Builds the subtree for [first, first+count) and returns its reference.
+    uint32_t build(int first, int count, const Aabb& b, const Aabb& cb, int depth) {
+        maxDepth = std::max(maxDepth, depth);
+        int mid = split(first, count, b, cb, depth);
+        if (mid < 0) {
+            if (count > kMaxLeafSize) mid = first + count / 2;
+            else return leafRef(first, count);
+        }
+        int node = int(nodes.size() / 4);
+        nodes.resize(nodes.size() + 4, make_float4(0, 0, 0, 0));
+        Aabb lcb, rcb;
+        Aabb lb = rangeBox(first, mid - first, &lcb), rb = rangeBox(mid, first + count - mid, &rcb);
+        uint32_t l = build(first, mid - first, lb, lcb, depth + 1);
+        uint32_t r = build(mid, first + count - mid, rb, rcb, depth + 1);
+        setChild(node, 0, lb, l);
+        setChild(node, 1, rb, r);
+        return uint32_t(node);
+    }
+
+    void run(int n) {
+        order.resize(n);
+        for (int i = 0; i < n; ++i) order[i] = i;
+        nodes.clear();
+        if (n == 0) return;
+        Aabb cb;
+        Aabb b = rangeBox(0, n, &cb);
+        // the root is always an inner node
+        nodes.resize(4, make_float4(0, 0, 0, 0));
+        int mid = split(0, n, b, cb, 0);
+        if (mid < 0) {
+            if (n == 1) {
+                setChild(0, 0, b, leafRef(0, 1));
+                setChild(0, 1, b, leafRef(0, 1));
+                return;
+            }
+            mid = n / 2;
+        }
+        Aabb lcb, rcb;
+        Aabb lb = rangeBox(0, mid, &lcb), rb = rangeBox(mid, n - mid, &rcb);
+        uint32_t l = build(0, mid, lb, lcb, 1);
+        uint32_t r = build(mid, n - mid, rb, rcb, 1);
+        setChild(0, 0, lb, l);
+        setChild(0, 1, rb, r);
+    }
+};
+
+// ---------------------------------------------------------------------------------------------
+// scene commit
+// ---------------------------------------------------------------------------------------------
+static void commitScene(sst_scene* s, int W, int H) {
+    if (W <= 0 || H <= 0) fail(SST_ERR_INVALID_ARGUMENT, "frame buffer size must be positive");
+    // Scene.IsValid (Scene.cs:170-197)
+    if (s->meshes.empty()) fail(SST_ERR_INVALID_SCENE, "No meshes in the scene.");
+    for (size_t i = 0; i < s->meshes.size(); ++i)
+        if (s->meshes[i].material < 0) fail(SST_ERR_INVALID_SCENE, "Mesh[" + std::to_string(i) + "] does not have a material.");
+    if (!s->cameraSet) fail(SST_ERR_INVALID_SCENE, "Camera not set.");
+    if (s->emitters.empty() && s->envW == 0) fail(SST_ERR_INVALID_SCENE, "No emitters and no background in the scene.");
+    cudaStream_t st = s->ctx->stream;
+    CUDA_CHECK(cudaSetDevice(s->ctx->device));
+
+    // global triangle table
+    int nt = 0;
+    s->meshTriOffset.clear();
+    std::vector<int> vtxOffset;
+    int nv = 0;
+    bool anyNormals = false, anyUV = false;
+    for (auto& m : s->meshes) {
+        s->meshTriOffset.push_back(nt);
+        vtxOffset.push_back(nv);
+        nt += int(m.I.size() / 3);
+        nv += int(m.V.size() / 3);
+        anyNormals |= !m.N.empty();
+        anyUV |= !m.UV.empty();
+    }
+    s->nTri = nt;
+    std::vector<int> triEmitter(nt, -1);
+    for (size_t e = 0; e < s->emitters.size(); ++e) {
+        int g = s->meshTriOffset[s->emitters[e].mesh] + s->emitters[e].face;
+        if (triEmitter[g] >= 0) fail(SST_ERR_INVALID_SCENE, "two emitters on the same triangle");
+        triEmitter[g] = int(e);
+    }
+    // BVH over all triangles
+    BvhBuilder b;
+    b.box.resize(nt);
+    b.cen.resize(3 * size_t(nt));
+    std::vector<int> gMesh(nt), gFace(nt);
+    {
+        int g = 0;
+        for (size_t mi = 0; mi < s->meshes.size(); ++mi) {
+            const HostMesh& m = s->meshes[mi];
+            for (size_t f = 0; f < m.I.size() / 3; ++f, ++g) {
+                gMesh[g] = int(mi);
+                gFace[g] = int(f);
+                Aabb bb;
+                for (int k = 0; k < 3; ++k) bb.grow(&m.V[3 * size_t(m.I[3 * f + k])]);
+                b.box[g] = bb;
+                for (int k = 0; k < 3; ++k) b.cen[3 * size_t(g) + k] = 0.5f * (bb.lo[k] + bb.hi[k]);
+            }
+        }
+    }
+    b.run(nt);
+    if (b.maxDepth >= kMaxBvhDepth) fail(SST_ERR_DEVICE_LIMIT, "BVH deeper than the traversal stack");
+    s->nNodes = int(b.nodes.size() / 4);
+    // leaf-ordered triangle data
+    std::vector<float4> triv(3 * size_t(nt)), triN(nt);
+    std::vector<int4> triAux(nt), triVtx(nt);
+    for (int t = 0; t < nt; ++t) {
+        int g = b.order[t];
+        const HostMesh& m = s->meshes[gMesh[g]];
+        int f = gFace[g];
+        int i0 = m.I[3 * f], i1 = m.I[3 * f + 1], i2 = m.I[3 * f + 2];
+        const float* a = &m.V[3 * size_t(i0)];
+        const float* bb = &m.V[3 * size_t(i1)];
+        const float* c = &m.V[3 * size_t(i2)];
+        float gw;
+        std::memcpy(&gw, &g, 4);
+        triv[3 * size_t(t)] = make_float4(a[0], a[1], a[2], gw);
+        triv[3 * size_t(t) + 1] = make_float4(bb[0], bb[1], bb[2], 0.f);
+        triv[3 * size_t(t) + 2] = make_float4(c[0], c[1], c[2], 0.f);
+        float ew;
+        std::memcpy(&ew, &triEmitter[g], 4);
+        triN[t] = make_float4(m.faceN[3 * f], m.faceN[3 * f + 1], m.faceN[3 * f + 2], ew);
+        int flags = (m.N.empty() ? 0 : 1) | (m.UV.empty() ? 0 : 2);
+        triAux[t] = make_int4(m.material, gMesh[g], f, flags);
+        int vo = vtxOffset[gMesh[g]];
+        triVtx[t] = make_int4(vo + i0, vo + i1, vo + i2, 0);
+    }
+    std::vector<float> vnrm, vuv;
+    if (anyNormals) {
+        vnrm.assign(3 * size_t(nv), 0.f);
+        for (size_t mi = 0; mi < s->meshes.size(); ++mi)
+            if (!s->meshes[mi].N.empty()) std::copy(s->meshes[mi].N.begin(), s->meshes[mi].N.end(), vnrm.begin() + 3 * size_t(vtxOffset[mi]));
+    }
+    if (anyUV) {
+        vuv.assign(2 * size_t(nv), 0.f);
+        for (size_t mi = 0; mi < s->meshes.size(); ++mi)
+            if (!s->meshes[mi].UV.empty()) std::copy(s->meshes[mi].UV.begin(), s->meshes[mi].UV.end(), vuv.begin() + 2 * size_t(vtxOffset[mi]));
+    }
+    // emitters
+    std::vector<DevEmitter> ems(s->emitters.size());
+    for (size_t e = 0; e < s->emitters.size(); ++e) {
+        const HostEmitter& he = s->emitters[e];
+        const HostMesh& m = s->meshes[he.mesh];
+        int f = he.face;
+        DevEmitter& d = ems[e];
+        const float* p[3];
+        for (int k = 0; k < 3; ++k) p[k] = &m.V[3 * size_t(m.I[3 * f + k])];
+        d.v1 = make_float4(p[0][0], p[0][1], p[0][2], 0.f);
+        d.v2 = make_float4(p[1][0], p[1][1], p[1][2], 0.f);
+        d.v3 = make_float4(p[2][0], p[2][1], p[2][2], 0.f);
+        if (!m.N.empty()) {
+            const float* q[3];
+            for (int k = 0; k < 3; ++k) q[k] = &m.N[3 * size_t(m.I[3 * f + k])];
+            d.n1 = make_float4(q[0][0], q[0][1], q[0][2], 1.f);
+            d.n2 = make_float4(q[1][0], q[1][1], q[1][2], 0.f);
+            d.n3 = make_float4(q[2][0], q[2][1], q[2][2], 0.f);
+        } else {
+            d.n1 = d.n2 = d.n3 = make_float4(0, 0, 0, 0);
+        }
+        // Triangle.cs:22-36: area = |cross(v2 - v1, v3 - v1)| * 0.5
+        float e1[3], e2[3];
+        for (int k = 0; k < 3; ++k) { e1[k] = p[1][k] - p[0][k]; e2[k] = p[2][k] - p[0][k]; }
+        float cx = e1[1] * e2[2] - e1[2] * e2[1], cy = e1[2] * e2[0] - e1[0] * e2[2], cz = e1[0] * e2[1] - e1[1] * e2[0];
+        float area = std::sqrt(cx * cx + cy * cy + cz * cz) * 0.5f;
+        d.faceN = make_float4(m.faceN[3 * f], m.faceN[3 * f + 1], m.faceN[3 * f + 2], 1.0f / area);
+        d.rad = make_float4(he.rad[0], he.rad[1], he.rad[2], he.exponent);
+        d.norm = (he.exponent + 1.0f) / (2.0f * 3.14159265f);  // GlossyEmitter.cs:14
+        d.globalTri = s->meshTriOffset[he.mesh] + f;
+    }
+    // textures
+    std::vector<DevTexture> texs;
+    std::vector<float> texPool;
+    for (auto& t : s->textures) {
+        DevTexture d{t.w, t.h, t.ch, t.border, (long long)texPool.size()};
+        texs.push_back(d);
+        texPool.insert(texPool.end(), t.data.begin(), t.data.end());
+    }
+    // upload
+    s->nodes.upload(b.nodes, st);
+    s->triv.upload(triv, st);
+    s->triN.upload(triN, st);
+    s->triAux.upload(triAux, st);
+    s->triVtx.upload(triVtx, st);
+    s->vnrm.upload(vnrm, st);
+    s->vuv.upload(vuv, st);
+    s->mats.upload(s->materials, st);
+    s->texs.upload(texs, st);
+    s->texData.upload(texPool, st);
+    s->ems.upload(ems, st);
+    DevScene& d = s->dev;
+    d = DevScene{};
+    d.nodes = s->nodes.as<float4>();
+    d.triv = s->triv.as<float4>();
+    d.triN = s->triN.as<float4>();
+    d.triAux = s->triAux.as<int4>();
+    d.triVtx = s->triVtx.as<int4>();
+    d.vnrm = anyNormals ? s->vnrm.as<float>() : nullptr;
+    d.vuv = anyUV ? s->vuv.as<float>() : nullptr;
+    d.mats = s->mats.as<DevMaterial>();
+    d.texs = s->texs.as<DevTexture>();
+    d.texData = s->texData.as<float>();
+    d.emitters = s->ems.as<DevEmitter>();
+    d.nEmitters = int(s->emitters.size());
+    d.nTri = nt;
+    d.nNodes = s->nNodes;
+    // environment map (EnvironmentMap.cs:139-156)
+    d.hasEnv = s->envW > 0;
+    if (d.hasEnv) {
+        std::vector<float4> img(size_t(s->envW) * s->envH);
+        for (size_t i = 0; i < img.size(); ++i) img[i] = make_float4(s->envRgb[3 * i], s->envRgb[3 * i + 1], s->envRgb[3 * i + 2], 0.f);
+        s->envImg.upload(img, st);
+        s->envColCdf.ensure(sizeof(float) * img.size());
+        s->envRowCdf.ensure(sizeof(float) * s->envH);
+        s->envRowMarg.ensure(sizeof(float) * s->envH);
+        s->envHasCol.ensure(sizeof(int) * s->envH);
+        launch_env_build(s->envImg.as<float4>(), s->envW, s->envH, s->envColCdf.as<float>(), s->envRowMarg.as<float>(), s->envHasCol.as<int>(),
+                         s->envRowCdf.as<float>(), st);
+        CUDA_CHECK(cudaGetLastError());
+        d.env.w = s->envW;
+        d.env.h = s->envH;
+        d.env.img = s->envImg.as<float4>();
+        d.env.rowCdf = s->envRowCdf.as<float>();
+        d.env.colCdf = s->envColCdf.as<float>();
+        d.env.hasCol = s->envHasCol.as<int>();
+    }
+    // camera (Camera.cs:34-42, PerspectiveCamera.cs:42-52)
+    float c2v[16];
+    if (!invert4(s->w2c, d.cam.c2w)) fail(SST_ERR_INVALID_ARGUMENT, "World to camera transform must be invertible.");
+    perspective(s->fovDeg * 3.14159265f / 180.0f, float(W) / float(H), 0.001f, 1000.0f, c2v);
+    if (!invert4(c2v, d.cam.v2c)) fail(SST_ERR_INVALID_ARGUMENT, "degenerate projection");
+    d.cam.W = W;
+    d.cam.H = H;
+    CUDA_CHECK(cudaStreamSynchronize(st));
+    s->W = W;
+    s->H = H;
+    s->committed = true;
+}
+
+// ---------------------------------------------------------------------------------------------
+// wavefront buffers
+// ---------------------------------------------------------------------------------------------
+static void bindPath(DevBuf* bufs, PathBuf& p, int cap) {
+    size_t c = size_t(cap);
+    bufs[0].ensure(c * 4); bufs[1].ensure(c * 4); bufs[2].ensure(c * 4);
+    for (int k = 3; k < 8; ++k) bufs[k].ensure(c * 16);
+    p.pix = bufs[0].as<uint32_t>();
+    p.rng = bufs[1].as<uint32_t>();
+    p.depth = bufs[2].as<uint32_t>();
+    p.pw = bufs[3].as<float4>();
+    p.rad = bufs[4].as<float4>();
+    p.prev = bufs[5].as<float4>();
+    p.ro = bufs[6].as<float4>();
+    p.rd = bufs[7].as<float4>();
+}
+
+static int defaultWaveCapacity() {
+    const char* e = getenv("SST_WAVE_CAPACITY");
+    if (e) return std::max(1024, atoi(e));
+    return 1 << 21;
+}
+
+struct Wave {
+    WaveBuffers wb;
+};
+
+static void ensureWave(sst_ctx* c, int cap, int ns, Wave& w) {
+    if (cap > c->cap) {
+        // grow all path buffers
+        c->cap = cap;
+        c->hits.ensure(size_t(cap) * 16);
+    }
+    bindPath(c->pathA, w.wb.a, c->cap);
+    bindPath(c->pathB, w.wb.b, c->cap);
+    c->neeSlots = std::max(c->neeSlots, 2 * ns);
+    c->nee.ensure(size_t(c->cap) * 16 * c->neeSlots);
+    size_t shCap = size_t(c->cap) * 2 * ns;
+    c->shRo.ensure(shCap * 16);
+    c->shRd.ensure(shCap * 16);
+    c->shTgt.ensure(shCap * 4);
+    c->counters.ensure(sizeof(int) * kNumCounters);
+    c->stats.ensure(sizeof(DevStats));
+    w.wb.hits = c->hits.as<float4>();
+    w.wb.nee = c->nee.as<float4>();
+    w.wb.shRo = c->shRo.as<float4>();
+    w.wb.shRd = c->shRd.as<float4>();
+    w.wb.shTgt = c->shTgt.as<int>();
+    w.wb.counters = c->counters.as<int>();
+    w.wb.cap = c->cap;
+    w.wb.shCap = int(shCap);
+}
+
+// ---------------------------------------------------------------------------------------------
+// render
+// ---------------------------------------------------------------------------------------------
+static void checkParams(const sst_scene* s, const SstPathTracerParams* p) {
+    if (!s->committed) fail(SST_ERR_NOT_COMMITTED, "scene is not committed");
+    if (p->width != s->W || p->height != s->H) fail(SST_ERR_INVALID_ARGUMENT, "frame buffer size differs from the committed camera resolution");
+    if (p->totalSpp < 0 || p->maxDepth < 1 || p->numShadowRays < 0 || p->numShadowRays > kMaxShadowRays || p->firstIteration < 0)
+        fail(SST_ERR_INVALID_ARGUMENT, "invalid path tracer parameters");
+    if (p->maxDepth > kMaxPathDepth) fail(SST_ERR_UNSUPPORTED, "MaxDepth above 1000 is not supported");
+}
+
+// Renders iterations [iterFirst, iterEnd) of one scene into the device film.
+static void renderDevice(sst_scene* s, const SstPathTracerParams* P, float* dFilm, int iterFirst, int iterEnd, SstRenderStats* out) {
+    sst_ctx* c = s->ctx;
+    cudaStream_t st = c->stream;
+    const int pixels = P->width * P->height;
+    const int ns = std::max(1, P->numShadowRays);
+    int cap = std::min(defaultWaveCapacity(), std::max(pixels, 1));
+    // several whole iterations per wave when the image is small
+    int itersPerWave = std::max(1, cap / pixels);
+    int pixPerWave = std::min(pixels, cap);
+    cap = std::max(pixPerWave * itersPerWave, 1);
+    Wave w;
+    ensureWave(c, cap, ns, w);
+    size_t sampleBytes = size_t(cap) * 12;
+    c->samples.ensure(sampleBytes);
+    PTConfig cfg{P->width, P->height, P->maxDepth, P->minDepth, P->baseSeed, P->numShadowRays, P->enableBsdfDI, P->ignoreNanAndInf};
+    DevStats* dstats = c->stats.as<DevStats>();
+    CUDA_CHECK(cudaMemsetAsync(dstats, 0, sizeof(DevStats), st));
+    CUDA_CHECK(cudaEventRecord(c->ev0, st));
+    int iterations = 0;
+    auto t0 = std::chrono::steady_clock::now();
+    for (int it = iterFirst; it < iterEnd;) {
+        if (P->maximumRenderTimeMs > 0 && it > iterFirst) {
+            CUDA_CHECK(cudaStreamSynchronize(st));
+            double ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+            double per = ms / std::max(1, iterations);
+            if (ms + per > double(P->maximumRenderTimeMs)) break;  // PathTracer.cs:221-227
+        }
+        int nIt = std::min(itersPerWave, iterEnd - it);
+        for (int p0 = 0; p0 < pixels; p0 += pixPerWave) {
+            int pc = std::min(pixPerWave, pixels - p0);
+            int n = pc * nIt;
+            int* cnt = w.wb.counters;
+            CUDA_CHECK(cudaMemsetAsync(cnt, 0, sizeof(int) * kNumCounters, st));
+            {
+                KTimer kt(c, 0);
+                launch_camera(s->dev, cfg, w.wb.a, p0, pc, n, uint32_t(it), cnt + kCntQueue + 1, st);
+            }
+            PathBuf A = w.wb.a, B = w.wb.b;
+            int maxItems = n;
+            for (int d = 1; d <= P->maxDepth; ++d) {
+                {
+                    KTimer kt(c, 1);
+                    launch_trace_closest(s->dev, A.ro, A.rd, cnt + kCntQueue + d, cnt + kCntWork + 2 * d, w.wb.hits, dstats, st);
+                }
+                {
+                    KTimer kt(c, 2);
+                    launch_shade(ns, s->dev, cfg, A, B, w.wb.hits, w.wb.nee, w.wb.cap, w.wb.shRo, w.wb.shRd, w.wb.shTgt, cnt + kCntQueue + d,
+                                 cnt + kCntQueue + d + 1, cnt + kCntShadow + d, c->samples.as<float>(), dstats, maxItems, st);
+                }
+                {
+                    KTimer kt(c, 3);
+                    launch_trace_shadow(s->dev, w.wb.shRo, w.wb.shRd, w.wb.shTgt, cnt + kCntShadow + d, cnt + kCntWork + 2 * d + 1, w.wb.nee,
+                                        dstats, st);
+                }
+                std::swap(A, B);
+                if (d >= 6 && d < P->maxDepth) {
+                    // stop early once the queue is empty (long MaxDepth with Russian roulette)
+                    CUDA_CHECK(cudaMemcpyAsync(c->pinnedCount, cnt + kCntQueue + d + 1, sizeof(int), cudaMemcpyDeviceToHost, st));
+                    CUDA_CHECK(cudaStreamSynchronize(st));
+                    if (*c->pinnedCount == 0) break;
+                    maxItems = *c->pinnedCount;
+                }
+            }
+            {
+                KTimer kt(c, 4);
+                launch_film_fold(cfg, c->samples.as<float>(), p0, pc, nIt, uint32_t(it), dFilm, dstats, st);
+            }
+            CUDA_CHECK(cudaGetLastError());
+            if (c->profiling) {
+                // items per class: queue lengths of this wave
+                std::vector<int> hc(kNumCounters);
+                CUDA_CHECK(cudaMemcpyAsync(hc.data(), cnt, sizeof(int) * kNumCounters, cudaMemcpyDeviceToHost, st));
+                flushTimers(c);
+                c->kItems[0] += n;
+                c->kItems[4] += pc;
+                for (int d = 1; d <= P->maxDepth && d < 1024; ++d) {
+                    c->kItems[1] += hc[kCntQueue + d];
+                    c->kItems[2] += hc[kCntQueue + d];
+                    c->kItems[3] += hc[kCntShadow + d];
+                }
+            }
+        }
+        it += nIt;
+        iterations += nIt;
+    }
+    CUDA_CHECK(cudaEventRecord(c->ev1, st));
+    CUDA_CHECK(cudaStreamSynchronize(st));
+    float ms = 0;
+    CUDA_CHECK(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
+    DevStats hs;
+    CUDA_CHECK(cudaMemcpy(&hs, dstats, sizeof(DevStats), cudaMemcpyDeviceToHost));
+    if (hs.errorFlags & 1) fail(SST_ERR_DEVICE_LIMIT, "BVH traversal stack overflow");
+    if (out) {
+        out->renderTimeMs += ms;
+        out->numIterations += iterations;
+        out->numRays += hs.rays;
+        out->numShadowRays += hs.shadowRays;
+        uint64_t prev = out->numNanOrInf;
+        for (uint64_t k = 0; k < std::min<uint64_t>(hs.nanCount, 4) && prev + k < 4; ++k) {
+            out->nanPixel[prev + k] = hs.nanPixel[k];
+            out->nanIteration[prev + k] = hs.nanIter[k];
+        }
+        out->numNanOrInf += hs.nanCount;
+    }
+}
+
+// Copies n items of `bytes` each to the device (or uses device pointers directly).
+template <class T> static const T* toDevice(sst_ctx* c, DevBuf& buf, const T* p, size_t n, int memory) {
+    if (memory == SST_MEM_DEVICE) return p;
+    buf.ensure(std::max<size_t>(1, n * sizeof(T)));
+    CUDA_CHECK(cudaMemcpyAsync(buf.p, p, n * sizeof(T), cudaMemcpyHostToDevice, c->stream));
+    return buf.as<T>();
+}
+
+template <class T> static T* devCopy(DevBuf& b, const T* h, size_t n, cudaStream_t st) {
+    b.ensure(std::max<size_t>(1, n * sizeof(T)));
+    if (h) CUDA_CHECK(cudaMemcpyAsync(b.p, h, n * sizeof(T), cudaMemcpyHostToDevice, st));
+    return b.as<T>();
+}
+template <class T> static void hostCopy(T* h, const DevBuf& b, size_t n, cudaStream_t st) {
+    CUDA_CHECK(cudaMemcpyAsync(h, b.p, n * sizeof(T), cudaMemcpyDeviceToHost, st));
+}
+
+static void runQuery(sst_scene* s, const SstRay* rays, int n, SstHit* hits, int32_t* occl, int memory, bool anyHit) {
+    if (!s || (n > 0 && !rays) || n < 0) fail(SST_ERR_INVALID_ARGUMENT, "invalid query");
+    if (!s->committed) fail(SST_ERR_NOT_COMMITTED, "scene is not committed");
+    if (n == 0) return;
+    sst_ctx* c = s->ctx;
+    cudaStream_t st = c->stream;
+    const float4* dr = reinterpret_cast<const float4*>(toDevice(c, c->scratchIn, rays, n, memory));
+    // separate origin / direction arrays (SstRay = org, tmin, dir, tmax = two float4)
+    DevBuf ro, rd;
+    ro.ensure(size_t(n) * 16);
+    rd.ensure(size_t(n) * 16);
+    CUDA_CHECK(cudaMemcpy2DAsync(ro.p, 16, dr, 32, 16, n, cudaMemcpyDeviceToDevice, st));
+    CUDA_CHECK(cudaMemcpy2DAsync(rd.p, 16, reinterpret_cast<const char*>(dr) + 16, 32, 16, n, cudaMemcpyDeviceToDevice, st));
+    DevBuf cnt, hitsBuf, occBuf;
+    cnt.ensure(sizeof(int) * 2);
+    int hostCnt[2] = {n, 0};
+    CUDA_CHECK(cudaMemcpyAsync(cnt.p, hostCnt, sizeof(hostCnt), cudaMemcpyHostToDevice, st));
+    c->stats.ensure(sizeof(DevStats));
+    CUDA_CHECK(cudaMemsetAsync(c->stats.p, 0, sizeof(DevStats), st));
+    if (anyHit) {
+        occBuf.ensure(size_t(n) * 4);
+        launch_trace_query(s->dev, ro.as<float4>(), rd.as<float4>(), cnt.as<int>(), cnt.as<int>() + 1, nullptr, occBuf.as<int>(), c->stats.as<DevStats>(),
+                           true, st);
+        CUDA_CHECK(cudaMemcpyAsync(occl, occBuf.p, size_t(n) * 4, memory == SST_MEM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, st));
+        CUDA_CHECK(cudaStreamSynchronize(st));
+        return;
+    }
+    hitsBuf.ensure(size_t(n) * 16);
+    launch_trace_query(s->dev, ro.as<float4>(), rd.as<float4>(), cnt.as<int>(), cnt.as<int>() + 1, hitsBuf.as<float4>(), nullptr, c->stats.as<DevStats>(),
+                       false, st);
+    std::vector<float4> hh(n);
+    CUDA_CHECK(cudaMemcpyAsync(hh.data(), hitsBuf.p, size_t(n) * 16, cudaMemcpyDeviceToHost, st));
+    CUDA_CHECK(cudaStreamSynchronize(st));
+    // expand into SstHit on the host (the device result is the compact (t, u, v, tri) record)
+    std::vector<float4> tv(3), tn(1);
+    std::vector<int4> aux(1);
+    std::vector<SstHit> outHits(n);
+    for (int i = 0; i < n; ++i) {
+        SstHit& h = outHits[i];
+        std::memset(&h, 0, sizeof(h));
+        int ti;
+        std::memcpy(&ti, &hh[i].w, 4);
+        if (ti < 0) { h.meshId = -1; h.primId = -1; continue; }
+        CUDA_CHECK(cudaMemcpy(tv.data(), s->triv.as<float4>() + 3 * size_t(ti), 48, cudaMemcpyDeviceToHost));
+        CUDA_CHECK(cudaMemcpy(tn.data(), s->triN.as<float4>() + ti, 16, cudaMemcpyDeviceToHost));
+        CUDA_CHECK(cudaMemcpy(aux.data(), s->triAux.as<int4>() + ti, 16, cudaMemcpyDeviceToHost));
+        float u = hh[i].y, v = hh[i].z;
+        h.distance = hh[i].x;
+        h.u = u;
+        h.v = v;
+        h.meshId = aux[0].y;
+        h.primId = aux[0].z;
+        float w = 1.0f - u - v;
+        const float* a = &tv[0].x;
+        const float* b = &tv[1].x;
+        const float* cc = &tv[2].x;
+        float e[3];
+        for (int k = 0; k < 3; ++k) {
+            h.position[k] = u * b[k] + v * cc[k] + w * a[k];
+            e[k] = std::fabs(u * b[k]) + std::fabs(v * cc[k]) + std::fabs(w * a[k]);
+        }
+        h.errorOffset = std::sqrt(e[0] * e[0] + e[1] * e[1] + e[2] * e[2]) * 32.0f * 1.19209e-07f;
+        h.normal[0] = tn[0].x;
+        h.normal[1] = tn[0].y;
+        h.normal[2] = tn[0].z;
+    }
+    if (memory == SST_MEM_DEVICE) CUDA_CHECK(cudaMemcpy(hits, outHits.data(), sizeof(SstHit) * n, cudaMemcpyHostToDevice));
+    else std::memcpy(hits, outHits.data(), sizeof(SstHit) * n);
+}
+
+// ---------------------------------------------------------------------------------------------
+// C ABI
+// ---------------------------------------------------------------------------------------------
+extern "C" {
+
+int sst_version(int32_t* major, int32_t* minor) {
+    if (major) *major = 0;
+    if (minor) *minor = 1;
+    return SST_OK;
+}
+
+int sst_last_error(char* buffer, size_t size) {
+    if (!buffer || size == 0) return SST_ERR_INVALID_ARGUMENT;
+    std::strncpy(buffer, g_lastError.c_str(), size - 1);
+    buffer[size - 1] = 0;
+    return SST_OK;
+}
+
+int sst_create(int32_t device, sst_ctx** out) {
+    return guarded([&] {
+        if (!out) fail(SST_ERR_INVALID_ARGUMENT, "out is NULL");
+        int n = 0;
+        CUDA_CHECK(cudaGetDeviceCount(&n));
+        if (device < 0 || device >= n) fail(SST_ERR_INVALID_ARGUMENT, "no such CUDA device");
+        CUDA_CHECK(cudaSetDevice(device));
+        auto c = std::make_unique<sst_ctx>();
+        c->device = device;
+        CUDA_CHECK(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+        CUDA_CHECK(cudaDeviceGetAttribute(&c->numSMs, cudaDevAttrMultiProcessorCount, device));
+        CUDA_CHECK(cudaEventCreate(&c->ev0));
+        CUDA_CHECK(cudaEventCreate(&c->ev1));
+        CUDA_CHECK(cudaMallocHost(&c->pinnedCount, sizeof(int) * 4));
+        *out = c.release();
+    });
+}
+
+int sst_destroy(sst_ctx* ctx) {
+    return guarded([&] {
+        if (!ctx) return;
+        cudaSetDevice(ctx->device);
+        cudaStreamSynchronize(ctx->stream);
+        if (ctx->pinnedCount) cudaFreeHost(ctx->pinnedCount);
+        if (ctx->ev0) cudaEventDestroy(ctx->ev0);
+        if (ctx->ev1) cudaEventDestroy(ctx->ev1);
+        cudaStreamDestroy(ctx->stream);
+        delete ctx;
+    });
+}
+
+int sst_scene_create(sst_ctx* ctx, sst_scene** out) {
+    return guarded([&] {
+        if (!ctx || !out) fail(SST_ERR_INVALID_ARGUMENT, "NULL argument");
+        auto s = std::make_unique<sst_scene>();
+        s->ctx = ctx;
+        *out = s.release();
+    });
+}
+
+int sst_scene_destroy(sst_scene* scene) {
+    return guarded([&] {
+        if (!scene) return;
+        cudaSetDevice(scene->ctx->device);
+        cudaStreamSynchronize(scene->ctx->stream);
+        delete scene;
+    });
+}
+
+int sst_scene_add_texture(sst_scene* s, const float* data, int32_t w, int32_t h, int32_t ch, int32_t border, int32_t* out) {
+    return guarded([&] {
+        if (!s || !data || !out || w <= 0 || h <= 0 || (ch != 1 && ch != 3) || (border != 0 && border != 1))
+            fail(SST_ERR_INVALID_ARGUMENT, "invalid texture");
+        HostTexture t{w, h, ch, border, std::vector<float>(data, data + size_t(w) * h * ch)};
+        s->textures.push_back(std::move(t));
+        s->committed = false;
+        *out = int(s->textures.size()) - 1;
+    });
+}
+
+static void checkTex(sst_scene* s, int tex, int wantCh) {
+    if (tex >= int(s->textures.size())) fail(SST_ERR_INVALID_ARGUMENT, "texture index out of range");
+    (void)wantCh;
+}
+
+int sst_scene_add_material_diffuse(sst_scene* s, const float base[3], int32_t tex, int32_t transmitter, int32_t* out) {
+    return guarded([&] {
+        if (!s || !base || !out) fail(SST_ERR_INVALID_ARGUMENT, "NULL argument");
+        checkTex(s, tex, 3);
+        DevMaterial m{};
+        m.type = kDiffuse;
+        m.baseTex = tex < 0 ? -1 : tex;
+        m.roughTex = -1;
+        m.transmitter = transmitter ? 1 : 0;
+        for (int k = 0; k < 3; ++k) m.base[k] = base[k];
+        m.rough = 1.0f;
+        m.ior = 1.0f;
+        s->materials.push_back(m);
+        s->committed = false;
+        *out = int(s->materials.size()) - 1;
+    });
+}
+
+static DevMaterial genericFrom(sst_scene* s, const SstGenericMaterial* p) {
+    checkTex(s, p->baseColorTexture, 3);
+    checkTex(s, p->roughnessTexture, 1);
+    DevMaterial m{};
+    m.type = kGeneric;
+    m.baseTex = p->baseColorTexture < 0 ? -1 : p->baseColorTexture;
+    m.roughTex = p->roughnessTexture < 0 ? -1 : p->roughnessTexture;
+    for (int k = 0; k < 3; ++k) m.base[k] = p->baseColor[k];
+    m.rough = p->roughness;
+    m.metallic = p->metallic;
+    m.specTint = p->specularTintStrength;
+    m.aniso = p->anisotropic;
+    m.specTrans = p->specularTransmittance;
+    m.ior = p->indexOfRefraction;
+    return m;
+}
+
+int sst_scene_add_material_generic(sst_scene* s, const SstGenericMaterial* p, int32_t* out) {
+    return guarded([&] {
+        if (!s || !p || !out) fail(SST_ERR_INVALID_ARGUMENT, "NULL argument");
+        s->materials.push_back(genericFrom(s, p));
+        s->committed = false;
+        *out = int(s->materials.size()) - 1;
+    });
+}
+
+int sst_scene_update_material_generic(sst_scene* s, int32_t material, const SstGenericMaterial* p) {
+    return guarded([&] {
+        if (!s || !p || material < 0 || material >= int(s->materials.size()) || s->materials[material].type != kGeneric)
+            fail(SST_ERR_INVALID_ARGUMENT, "invalid generic material");
+        s->materials[material] = genericFrom(s, p);
+        if (s->committed) {
+            CUDA_CHECK(cudaMemcpyAsync(s->mats.as<DevMaterial>() + material, &s->materials[material], sizeof(DevMaterial), cudaMemcpyHostToDevice,
+                                       s->ctx->stream));
+            CUDA_CHECK(cudaStreamSynchronize(s->ctx->stream));
+        }
+    });
+}
+
+int sst_scene_add_mesh(sst_scene* s, const float* V, int32_t nV, const int32_t* I, int32_t nT, const float* N, const float* UV, int32_t material,
+                       int32_t* out) {
+    return guarded([&] {
+        if (!s || !out || nV < 0 || nT < 0 || (nV > 0 && !V) || (nT > 0 && !I)) fail(SST_ERR_INVALID_ARGUMENT, "invalid mesh");
+        if (material >= int(s->materials.size())) fail(SST_ERR_INVALID_ARGUMENT, "material index out of range");
+        HostMesh m;
+        m.V.assign(V, V + 3 * size_t(nV));
+        m.I.assign(I, I + 3 * size_t(nT));
+        for (int32_t k = 0; k < 3 * nT; ++k)
+            if (m.I[k] < 0 || m.I[k] >= nV) fail(SST_ERR_INVALID_ARGUMENT, "vertex index out of range");
+        if (N) m.N.assign(N, N + 3 * size_t(nV));
+        if (UV) m.UV.assign(UV, UV + 2 * size_t(nV));
+        m.material = material;
+        m.faceN.resize(3 * size_t(nT));
+        for (int f = 0; f < nT; ++f) {  // normalized cross(v2 - v1, v3 - v1)
+            const float* a = &m.V[3 * size_t(m.I[3 * f])];
+            const float* b = &m.V[3 * size_t(m.I[3 * f + 1])];
+            const float* c = &m.V[3 * size_t(m.I[3 * f + 2])];
+            float e1[3] = {b[0] - a[0], b[1] - a[1], b[2] - a[2]}, e2[3] = {c[0] - a[0], c[1] - a[1], c[2] - a[2]};
+            float n[3] = {e1[1] * e2[2] - e1[2] * e2[1], e1[2] * e2[0] - e1[0] * e2[2], e1[0] * e2[1] - e1[1] * e2[0]};
+            float l = std::sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+            for (int k = 0; k < 3; ++k) m.faceN[3 * size_t(f) + k] = n[k] / l;
+        }
+        s->meshes.push_back(std::move(m));
+        s->committed = false;
+        *out = int(s->meshes.size()) - 1;
+    });
+}
+
+int sst_scene_add_emitters(sst_scene* s, int32_t mesh, const int32_t* faces, int32_t nFaces, const float rad[3], float exponent, int32_t* outFirst,
+                           int32_t* outCount) {
+    return guarded([&] {
+        if (!s || !rad || mesh < 0 || mesh >= int(s->meshes.size())) fail(SST_ERR_INVALID_ARGUMENT, "invalid emitter mesh");
+        const HostMesh& m = s->meshes[mesh];
+        int nf = int(m.I.size() / 3);
+        int first = int(s->emitters.size());
+        int count = faces ? nFaces : nf;
+        int added = 0;
+        for (int k = 0; k < count; ++k) {
+            int f = faces ? faces[k] : k;
+            if (f < 0 || f >= nf) fail(SST_ERR_INVALID_ARGUMENT, "face index out of range");
+            const float* a = &m.V[3 * size_t(m.I[3 * f])];
+            const float* b = &m.V[3 * size_t(m.I[3 * f + 1])];
+            const float* c = &m.V[3 * size_t(m.I[3 * f + 2])];
+            float e1[3] = {b[0] - a[0], b[1] - a[1], b[2] - a[2]}, e2[3] = {c[0] - a[0], c[1] - a[1], c[2] - a[2]};
+            float n[3] = {e1[1] * e2[2] - e1[2] * e2[1], e1[2] * e2[0] - e1[0] * e2[2], e1[0] * e2[1] - e1[1] * e2[0]};
+            float area = std::sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]) * 0.5f;
+            if (area == 0.0f) {
+                if (faces) fail(SST_ERR_INVALID_ARGUMENT, "Zero-area triangles cannot be emitters");
+                continue;  // DiffuseEmitter.MakeFromMesh skips them (DiffuseEmitter.cs:24-28)
+            }
+            s->emitters.push_back(HostEmitter{mesh, f, {rad[0], rad[1], rad[2]}, exponent < 0 ? -1.0f : exponent});
+            ++added;
+        }
+        s->committed = false;
+        if (outFirst) *outFirst = first;
+        if (outCount) *outCount = added;
+    });
+}
+
+int sst_scene_set_emitter_radiance(sst_scene* s, int32_t first, int32_t count, const float* rgb) {
+    return guarded([&] {
+        if (!s || !rgb || first < 0 || count < 0 || first + count > int(s->emitters.size())) fail(SST_ERR_INVALID_ARGUMENT, "emitter range");
+        for (int k = 0; k < count; ++k)
+            for (int c = 0; c < 3; ++c) s->emitters[first + k].rad[c] = rgb[3 * k + c];
+        if (s->committed) {
+            // radiance lives in DevEmitter.rad: patch the device copies
+            std::vector<DevEmitter> tmp(count);
+            CUDA_CHECK(cudaMemcpy(tmp.data(), s->ems.as<DevEmitter>() + first, sizeof(DevEmitter) * count, cudaMemcpyDeviceToHost));
+            for (int k = 0; k < count; ++k) tmp[k].rad = make_float4(rgb[3 * k], rgb[3 * k + 1], rgb[3 * k + 2], tmp[k].rad.w);
+            CUDA_CHECK(cudaMemcpy(s->ems.as<DevEmitter>() + first, tmp.data(), sizeof(DevEmitter) * count, cudaMemcpyHostToDevice));
+        }
+    });
+}
+
+int sst_scene_set_envmap(sst_scene* s, const float* rgb, int32_t w, int32_t h) {
+    return guarded([&] {
+        if (!s || !rgb || w <= 0 || h <= 0) fail(SST_ERR_INVALID_ARGUMENT, "invalid environment map");
+        s->envRgb.assign(rgb, rgb + 3 * size_t(w) * h);
+        s->envW = w;
+        s->envH = h;
+        s->committed = false;
+    });
+}
+
+int sst_scene_set_camera(sst_scene* s, const float m[16], float fov) {
+    return guarded([&] {
+        if (!s || !m) fail(SST_ERR_INVALID_ARGUMENT, "NULL argument");
+        float tmp[16];
+        if (!invert4(m, tmp)) fail(SST_ERR_INVALID_ARGUMENT, "World to camera transform must be invertible.");
+        if (!(fov > 0.0f && fov < 180.0f)) fail(SST_ERR_INVALID_ARGUMENT, "field of view out of range");
+        std::memcpy(s->w2c, m, sizeof(float) * 16);
+        s->fovDeg = fov;
+        s->cameraSet = true;
+        s->committed = false;
+    });
+}
+
+int sst_scene_commit(sst_scene* s, int32_t w, int32_t h) {
+    return guarded([&] {
+        if (!s) fail(SST_ERR_INVALID_ARGUMENT, "NULL scene");
+        commitScene(s, w, h);
+    });
+}
+
+int sst_scene_info(sst_scene* s, int32_t* ne, int32_t* nt, int32_t* nn) {
+    return guarded([&] {
+        if (!s) fail(SST_ERR_INVALID_ARGUMENT, "NULL scene");
+        if (!s->committed) fail(SST_ERR_NOT_COMMITTED, "scene is not committed");
+        if (ne) *ne = int(s->emitters.size());
+        if (nt) *nt = s->nTri;
+        if (nn) *nn = s->nNodes;
+    });
+}
+
+int sst_trace(sst_scene* s, const SstRay* rays, int32_t n, SstHit* hits, int32_t memory) {
+    return guarded([&] {
+        if (!hits && n > 0) fail(SST_ERR_INVALID_ARGUMENT, "hits is NULL");
+        runQuery(s, rays, n, hits, nullptr, memory, false);
+    });
+}
+
+int sst_occluded(sst_scene* s, const SstRay* rays, int32_t n, int32_t* occluded, int32_t memory) {
+    return guarded([&] {
+        if (!occluded && n > 0) fail(SST_ERR_INVALID_ARGUMENT, "occluded is NULL");
+        runQuery(s, rays, n, nullptr, occluded, memory, true);
+    });
+}
+
+int sst_render(sst_scene* s, const SstPathTracerParams* p, float* film, int32_t memory, SstRenderStats* stats) {
+    return guarded([&] {
+        if (!s || !p || !film) fail(SST_ERR_INVALID_ARGUMENT, "NULL argument");
+        checkParams(s, p);
+        sst_ctx* c = s->ctx;
+        CUDA_CHECK(cudaSetDevice(c->device));
+        SstRenderStats local{};
+        for (int k = 0; k < 4; ++k) { local.nanPixel[k] = -1; local.nanIteration[k] = -1; }
+        size_t filmBytes = size_t(p->width) * p->height * 3 * sizeof(float);
+        float* dFilm = film;
+        auto tfb0 = std::chrono::steady_clock::now();
+        if (memory != SST_MEM_DEVICE) {
+            c->film.ensure(filmBytes);
+            dFilm = c->film.as<float>();
+            if (p->firstIteration > 0) CUDA_CHECK(cudaMemcpyAsync(dFilm, film, filmBytes, cudaMemcpyHostToDevice, c->stream));
+            else CUDA_CHECK(cudaMemsetAsync(dFilm, 0, filmBytes, c->stream));
+        } else if (p->firstIteration == 0) {
+            CUDA_CHECK(cudaMemsetAsync(dFilm, 0, filmBytes, c->stream));
+        }
+        CUDA_CHECK(cudaStreamSynchronize(c->stream));
+        double fbMs = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - tfb0).count();
+        if (p->firstIteration < p->totalSpp) renderDevice(s, p, dFilm, p->firstIteration, p->totalSpp, &local);
+        auto tfb1 = std::chrono::steady_clock::now();
+        if (memory != SST_MEM_DEVICE) CUDA_CHECK(cudaMemcpy(film, dFilm, filmBytes, cudaMemcpyDeviceToHost));
+        fbMs += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - tfb1).count();
+        local.frameBufferTimeMs = fbMs;
+        if (stats) *stats = local;
+    });
+}
+
+int sst_render_batch(sst_ctx* ctx, const SstRenderJob* jobs, int32_t numJobs, SstRenderStats* stats) {
+    return guarded([&] {
+        if (!ctx || (numJobs > 0 && !jobs) || numJobs < 0) fail(SST_ERR_INVALID_ARGUMENT, "invalid batch");
+        SstRenderStats total{};
+        for (int k = 0; k < 4; ++k) { total.nanPixel[k] = -1; total.nanIteration[k] = -1; }
+        for (int j = 0; j < numJobs; ++j) {
+            SstRenderStats st{};
+            int rc = sst_render(jobs[j].scene, &jobs[j].params, jobs[j].film, jobs[j].memory, &st);
+            if (rc != SST_OK) fail(rc, "job " + std::to_string(j) + ": " + g_lastError);
+            total.renderTimeMs += st.renderTimeMs;
+            total.frameBufferTimeMs += st.frameBufferTimeMs;
+            total.numIterations += st.numIterations;
+            total.numRays += st.numRays;
+            total.numShadowRays += st.numShadowRays;
+            total.numNanOrInf += st.numNanOrInf;
+        }
+        if (stats) *stats = total;
+    });
+}
+
+int sst_set_profiling(sst_ctx* ctx, int32_t enable) {
+    return guarded([&] {
+        if (!ctx) fail(SST_ERR_INVALID_ARGUMENT, "NULL context");
+        ctx->profiling = enable != 0;
+        for (int k = 0; k < SST_KERNEL_CLASSES; ++k) { ctx->kMs[k] = 0; ctx->kLaunches[k] = 0; ctx->kItems[k] = 0; }
+    });
+}
+
+int sst_get_kernel_times(sst_ctx* ctx, double* ms, int64_t* launches, int64_t* items, int32_t n) {
+    return guarded([&] {
+        if (!ctx || n < 0) fail(SST_ERR_INVALID_ARGUMENT, "invalid arguments");
+        for (int k = 0; k < std::min(n, SST_KERNEL_CLASSES); ++k) {
+            if (ms) ms[k] = ctx->kMs[k];
+            if (launches) launches[k] = ctx->kLaunches[k];
+            if (items) items[k] = ctx->kItems[k];
+        }
+    });
+}
+
+// ---- function-level entry points ----
+int sst_debug_material_eval(sst_scene* s, int32_t mat, int32_t n, const float* pts, const float* outs, const float* ins, float* vals, float* pdfs) {
+    return guarded([&] {
+        if (!s || !s->committed) fail(SST_ERR_NOT_COMMITTED, "scene is not committed");
+        if (mat < 0 || mat >= int(s->materials.size()) || n < 0) fail(SST_ERR_INVALID_ARGUMENT, "invalid material query");
+        if (n == 0) return;
+        cudaStream_t st = s->ctx->stream;
+        DevBuf a, b, c, d, e;
+        float* dp = devCopy(a, pts, 11 * size_t(n), st);
+        float* dout = devCopy(b, outs, 3 * size_t(n), st);
+        float* din = devCopy(c, ins, 3 * size_t(n), st);
+        float* dv = devCopy<float>(d, nullptr, 3 * size_t(n), st);
+        float* dpdf = devCopy<float>(e, nullptr, 2 * size_t(n), st);
+        launch_debug_material_eval(s->dev, mat, n, dp, dout, din, dv, dpdf, st);
+        CUDA_CHECK(cudaGetLastError());
+        hostCopy(vals, d, 3 * size_t(n), st);
+        hostCopy(pdfs, e, 2 * size_t(n), st);
+        CUDA_CHECK(cudaStreamSynchronize(st));
+    });
+}
+
+int sst_debug_material_sample(sst_scene* s, int32_t mat, int32_t n, const float* pts, const float* outs, const float* us, float* dirs, float* pdfs,
+                              float* ws) {
+    return guarded([&] {
+        if (!s || !s->committed) fail(SST_ERR_NOT_COMMITTED, "scene is not committed");
+        if (mat < 0 || mat >= int(s->materials.size()) || n < 0) fail(SST_ERR_INVALID_ARGUMENT, "invalid material query");
+        if (n == 0) return;
+        cudaStream_t st = s->ctx->stream;
+        DevBuf a, b, c, d, e, f;
+        float* dp = devCopy(a, pts, 11 * size_t(n), st);
+        float* dout = devCopy(b, outs, 3 * size_t(n), st);
+        float* du = devCopy(c, us, 3 * size_t(n), st);
+        float* dd = devCopy<float>(d, nullptr, 3 * size_t(n), st);
+        float* dpdf = devCopy<float>(e, nullptr, 2 * size_t(n), st);
+        float* dw = devCopy<float>(f, nullptr, 3 * size_t(n), st);
+        launch_debug_material_sample(s->dev, mat, n, dp, dout, du, dd, dpdf, dw, st);
+        CUDA_CHECK(cudaGetLastError());
+        hostCopy(dirs, d, 3 * size_t(n), st);
+        hostCopy(pdfs, e, 2 * size_t(n), st);
+        hostCopy(ws, f, 3 * size_t(n), st);
+        CUDA_CHECK(cudaStreamSynchronize(st));
+    });
+}
+
+int sst_debug_envmap(sst_scene* s, int32_t n, const float* us, float* dirs, float* pdfs, float* ws, const float* qd, float* rad, float* qpdf) {
+    return guarded([&] {
+        if (!s || !s->committed) fail(SST_ERR_NOT_COMMITTED, "scene is not committed");
+        if (!s->dev.hasEnv) fail(SST_ERR_INVALID_ARGUMENT, "scene has no environment map");
+        if (n <= 0) return;
+        cudaStream_t st = s->ctx->stream;
+        DevBuf a, b, c, d, e, f, g;
+        float* du = devCopy(a, us, 2 * size_t(n), st);
+        float* dq = devCopy(b, qd, 3 * size_t(n), st);
+        float* dd = devCopy<float>(c, nullptr, 3 * size_t(n), st);
+        float* dp = devCopy<float>(d, nullptr, size_t(n), st);
+        float* dw = devCopy<float>(e, nullptr, 3 * size_t(n), st);
+        float* dr = devCopy<float>(f, nullptr, 3 * size_t(n), st);
+        float* dqp = devCopy<float>(g, nullptr, size_t(n), st);
+        launch_debug_env(s->dev, n, du, dd, dp, dw, dq, dr, dqp, st);
+        CUDA_CHECK(cudaGetLastError());
+        hostCopy(dirs, c, 3 * size_t(n), st);
+        hostCopy(pdfs, d, size_t(n), st);
+        hostCopy(ws, e, 3 * size_t(n), st);
+        hostCopy(rad, f, 3 * size_t(n), st);
+        hostCopy(qpdf, g, size_t(n), st);
+        CUDA_CHECK(cudaStreamSynchronize(st));
+    });
+}
+
+int sst_debug_rng(uint32_t base, uint32_t sample, int32_t n, const uint32_t* pixels, int32_t draws, uint32_t* out) {
+    return guarded([&] {
+        if (n < 0 || draws < 0 || (n > 0 && (!pixels || !out))) fail(SST_ERR_INVALID_ARGUMENT, "invalid rng query");
+        if (n == 0 || draws == 0) return;
+        DevBuf a, b;
+        uint32_t* dp = devCopy(a, pixels, size_t(n), 0);
+        uint32_t* dout = devCopy<uint32_t>(b, nullptr, size_t(n) * draws, 0);
+        launch_debug_rng(base, sample, n, dp, draws, dout, 0);
+        CUDA_CHECK(cudaGetLastError());
+        CUDA_CHECK(cudaMemcpy(out, dout, sizeof(uint32_t) * size_t(n) * draws, cudaMemcpyDeviceToHost));
+    });
+}
+
+int sst_debug_camera(sst_scene* s, int32_t n, const float* film, float* org, float* dir) {
+    return guarded([&] {
+        if (!s || !s->committed) fail(SST_ERR_NOT_COMMITTED, "scene is not committed");
+        if (n <= 0) return;
+        cudaStream_t st = s->ctx->stream;
+        DevBuf a, b, c;
+        float* df = devCopy(a, film, 2 * size_t(n), st);
+        float* dor = devCopy<float>(b, nullptr, 3 * size_t(n), st);
+        float* ddr = devCopy<float>(c, nullptr, 3 * size_t(n), st);
+        launch_debug_camera(s->dev, n, df, dor, ddr, st);
+        CUDA_CHECK(cudaGetLastError());
+        hostCopy(org, b, 3 * size_t(n), st);
+        hostCopy(dir, c, 3 * size_t(n), st);
+        CUDA_CHECK(cudaStreamSynchronize(st));
+    });
+}
+
+}  // extern "C"

@@ -1,0 +1,680 @@
+// Wavefront path-tracing kernels for sm_103a.
+//
+//   k_env_build   -> EnvironmentMap.BuildSamplingGrid (Shading/Background/EnvironmentMap.cs:139-156)
+//   k_camera      -> PathTracerBase.RenderPixel's camera ray (Integrators/PathTracer.cs:287-306)
+//   k_trace       -> TinyEmbree Raytracer.Trace / IsOccluded / LeavesScene (PathTracer.cs:319,428,467)
+//   k_shade       -> one bounce of EstimateIncidentRadiance (PathTracer.cs:318-378), with queue
+//                    compaction and the FrameBuffer.Splat running mean (Images/FrameBuffer.cs:166-191)
+#include <cooperative_groups.h>
+#include <cuda_runtime.h>
+
+#include "sst_device.cuh"
+#include "sst_kernels.h"
+
+namespace cg = cooperative_groups;
+
+namespace sst {
+
+// =============================================================================================
+// K0: environment-map sampling tables.  One thread per row sums the row sequentially, exactly as
+// RegularGrid2d.Splat/Normalize and the PiecewiseConstantPDF constructor do on the CPU
+// (Sampling/RegularGrid2d.cs:62-81, Sampling/PiecewiseConstant.cs:12-29); the row distribution
+// over the marginals is then built by a single thread.  Round-to-nearest intrinsics keep the
+// additions uncontracted so the tables equal a scalar CPU build.
+// =============================================================================================
+__global__ void k_env_rows(const float4* img, int w, int h, float* colCdf, float* rowMarg, int* hasCol) {
+    int row = blockIdx.x * blockDim.x + threadIdx.x;
+    if (row >= h) return;
+    float* cdf = colCdf + (size_t)row * w;
+    float sum = 0.0f;
+    for (int c = 0; c < w; ++c) {
+        float4 p = img[(size_t)row * w + c];
+        float lum = __fadd_rn(__fadd_rn(__fmul_rn(0.2126f, p.x), __fmul_rn(0.7152f, p.y)), __fmul_rn(0.0722f, p.z));
+        sum = __fadd_rn(sum, lum);
+        cdf[c] = sum;
+    }
+    rowMarg[row] = sum;
+    hasCol[row] = sum != 0.0f;
+    if (sum > 0.0f)
+        for (int c = 0; c < w; ++c) cdf[c] = __fdiv_rn(cdf[c], sum);
+    cdf[w - 1] = 1.0f;
+}
+__global__ void k_env_marginal(const float* rowMarg, int h, float* rowCdf) {
+    if (blockIdx.x != 0 || threadIdx.x != 0) return;
+    float sum = 0.0f;
+    for (int r = 0; r < h; ++r) { sum = __fadd_rn(sum, rowMarg[r]); rowCdf[r] = sum; }
+    if (sum > 0.0f)
+        for (int r = 0; r < h; ++r) rowCdf[r] = __fdiv_rn(rowCdf[r], sum);
+    rowCdf[h - 1] = 1.0f;
+}
+
+void launch_env_build(const float4* img, int w, int h, float* colCdf, float* rowMarg, int* hasCol, float* rowCdf, cudaStream_t s) {
+    k_env_rows<<<(h + 127) / 128, 128, 0, s>>>(img, w, h, colCdf, rowMarg, hasCol);
+    k_env_marginal<<<1, 32, 0, s>>>(rowMarg, h, rowCdf);
+}
+
+// =============================================================================================
+// K2: camera rays.  Path p of the wave is pixel pixStart + p of iteration `iter`.
+// =============================================================================================
+__global__ void __launch_bounds__(256) k_camera(DevScene sc, PTConfig cfg, PathBuf A, int pixStart, int pixCount, int n, uint32_t iterBase,
+                                                int* qCount) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i == 0) *qCount = n;
+    if (i >= n) return;
+    int m = i / pixCount;
+    uint32_t pix = (uint32_t)(pixStart + (i - m * pixCount));
+    uint32_t iter = iterBase + (uint32_t)m;
+    uint32_t row = pix / (uint32_t)cfg.W, col = pix - row * (uint32_t)cfg.W;
+    Rng rng{hashSeed(cfg.baseSeed, pix, iter)};  // PathTracer.cs:236-237
+    float ox = rng.nextFloat();                  // PathTracer.cs:289
+    float oy = rng.nextFloat();
+    float3 org, dir;
+    cameraRay(sc.cam, (float)col + ox, (float)row + oy, org, dir);
+    A.pix[i] = (uint32_t)i;  // wave item; the film fold maps it back to (iteration, pixel)
+    A.rng[i] = rng.s;
+    A.depth[i] = 1u;
+    A.pw[i] = make_float4(1.f, 1.f, 1.f, 0.f);
+    A.rad[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    A.ro[i] = make_float4(org.x, org.y, org.z, 0.f);
+    A.rd[i] = make_float4(dir.x, dir.y, dir.z, CUDART_INF_F);
+}
+
+// =============================================================================================
+// K8: fold the per-iteration path estimates of a wave into the film with the frame buffer's
+// running mean: for iteration k (1-based) film = film * (k - 1) / k + v / k, non-finite
+// estimates logged and skipped (FrameBuffer.Splat/Normalize, Images/FrameBuffer.cs:166-191, 232).
+// =============================================================================================
+__global__ void k_film_fold(PTConfig cfg, const float* samples, int pixStart, int pixCount, int iters, uint32_t iterBase, float* film,
+                            DevStats* st) {
+    int p = blockIdx.x * blockDim.x + threadIdx.x;
+    if (p >= pixCount) return;
+    size_t pix = (size_t)(pixStart + p);
+    float* f = film + 3 * pix;
+    float3 cur = mk(f[0], f[1], f[2]);
+    for (int m = 0; m < iters; ++m) {
+        uint32_t iter = iterBase + (uint32_t)m;
+        const float* s = samples + 3 * ((size_t)m * pixCount + p);
+        float3 v = mk(s[0], s[1], s[2]);
+        float kf = (float)(iter + 1);
+        if (iter > 0) cur = cur * ((kf - 1.0f) / kf);
+        float a = avg3(v);
+        bool finite = isfinite(a);
+        if (!finite) {
+            unsigned long long k = atomicAdd(&st->nanCount, 1ull);
+            if (k < 4) { st->nanPixel[k] = (int)pix; st->nanIter[k] = (int)iter + 1; }
+        }
+        if (finite || !cfg.ignoreNan) cur = cur + v / kf;
+    }
+    f[0] = cur.x; f[1] = cur.y; f[2] = cur.z;
+}
+
+void launch_film_fold(const PTConfig& cfg, const float* samples, int pixStart, int pixCount, int iters, uint32_t iterBase, float* film,
+                      DevStats* st, cudaStream_t s) {
+    k_film_fold<<<(pixCount + 255) / 256, 256, 0, s>>>(cfg, samples, pixStart, pixCount, iters, iterBase, film, st);
+}
+
+// =============================================================================================
+// K3/K4: BVH traversal.  Binary BVH, both child boxes stored in the parent (64-byte nodes read
+// as four 128-bit loads), watertight ray/triangle test (Woop, Benthin, Wald 2013), per-thread
+// stack in shared memory with a local-memory tail, persistent warps fetching 32 rays at a time.
+// =============================================================================================
+struct RayPre {
+    int kx, ky, kz;
+    float Sx, Sy, Sz;
+};
+SST_D float comp(float3 a, int k) { return k == 0 ? a.x : (k == 1 ? a.y : a.z); }
+SST_D RayPre rayPre(float3 d) {
+    RayPre p;
+    float ax = fabsf(d.x), ay = fabsf(d.y), az = fabsf(d.z);
+    p.kz = (ax > ay) ? (ax > az ? 0 : 2) : (ay > az ? 1 : 2);
+    p.kx = p.kz == 2 ? 0 : p.kz + 1;
+    p.ky = p.kx == 2 ? 0 : p.kx + 1;
+    float dz = comp(d, p.kz);
+    if (dz < 0.0f) { int t = p.kx; p.kx = p.ky; p.ky = t; }
+    p.Sx = comp(d, p.kx) / dz;
+    p.Sy = comp(d, p.ky) / dz;
+    p.Sz = 1.0f / dz;
+    return p;
+}
+// Returns true with t, u (2nd vertex weight), v (3rd vertex weight) when tmin < t < tmax.
+SST_D bool isectTri(float3 o, const RayPre& p, float3 v0, float3 v1, float3 v2, float tmin, float tmax, float& t, float& u, float& v) {
+    float3 A = v0 - o, B = v1 - o, C = v2 - o;
+    float Az_ = comp(A, p.kz), Bz_ = comp(B, p.kz), Cz_ = comp(C, p.kz);
+    float Ax = comp(A, p.kx) - p.Sx * Az_, Ay = comp(A, p.ky) - p.Sy * Az_;
+    float Bx = comp(B, p.kx) - p.Sx * Bz_, By = comp(B, p.ky) - p.Sy * Bz_;
+    float Cx = comp(C, p.kx) - p.Sx * Cz_, Cy = comp(C, p.ky) - p.Sy * Cz_;
+    float U = Cx * By - Cy * Bx;
+    float V = Ax * Cy - Ay * Cx;
+    float W = Bx * Ay - By * Ax;
+    if (U == 0.0f || V == 0.0f || W == 0.0f) {  // edge case: exact evaluation in double
+        U = (float)((double)Cx * (double)By - (double)Cy * (double)Bx);
+        V = (float)((double)Ax * (double)Cy - (double)Ay * (double)Cx);
+        W = (float)((double)Bx * (double)Ay - (double)By * (double)Ax);
+    }
+    if ((U < 0.0f || V < 0.0f || W < 0.0f) && (U > 0.0f || V > 0.0f || W > 0.0f)) return false;
+    float det = U + V + W;
+    if (det == 0.0f) return false;
+    float T = U * (p.Sz * Az_) + V * (p.Sz * Bz_) + W * (p.Sz * Cz_);
+    float rcp = 1.0f / det;
+    float tt = T * rcp;
+    if (!(tt > tmin) || !(tt < tmax)) return false;
+    t = tt;
+    u = V * rcp;
+    v = W * rcp;
+    return true;
+}
+
+struct TraceResult {
+    float t, u, v;
+    int tri;  // leaf-ordered triangle, -1 for a miss
+};
+
+// Closest hit (ANY = false; ties in t resolve to the smaller global triangle id) or any hit.
+template <bool ANY>
+SST_D TraceResult traverse(const DevScene& sc, float3 org, float3 dir, float tmin, float tmax, int* sstack, int* errFlags) {
+    TraceResult r{tmax, 0.f, 0.f, -1};
+    if (sc.nNodes == 0 || !(tmax > tmin)) return r;
+    int bestGid = 0x7FFFFFFF;
+    RayPre pre = rayPre(dir);
+    float3 inv = mk(1.0f / dir.x, 1.0f / dir.y, 1.0f / dir.z);
+    float3 oi = mk(-org.x * inv.x, -org.y * inv.y, -org.z * inv.z);
+    int lstack[kMaxStack - kSmemStack];
+    int sp = 0;
+    uint32_t ref = 0;  // root inner node
+    const int tid = threadIdx.x;
+    for (;;) {
+        if (!(ref & kLeafFlag)) {
+            const float4* nd = sc.nodes + 4 * (size_t)ref;
+            float4 n0 = __ldg(nd), n1 = __ldg(nd + 1), n2 = __ldg(nd + 2), n3 = __ldg(nd + 3);
+            float hitT = r.t * 1.0000004f;  // conservative far bound (box/triangle rounding)
+            // child 0
+            float a0 = fmaf(n0.x, inv.x, oi.x), b0 = fmaf(n0.y, inv.x, oi.x);
+            float c0 = fmaf(n0.z, inv.y, oi.y), d0 = fmaf(n0.w, inv.y, oi.y);
+            float e0 = fmaf(n2.x, inv.z, oi.z), f0 = fmaf(n2.y, inv.z, oi.z);
+            float tn0 = fmaxf(fmaxf(fminf(a0, b0), fminf(c0, d0)), fmaxf(fminf(e0, f0), tmin));
+            float tf0 = fminf(fminf(fmaxf(a0, b0), fmaxf(c0, d0)), fminf(fmaxf(e0, f0), hitT));
+            // child 1
+            float a1 = fmaf(n1.x, inv.x, oi.x), b1 = fmaf(n1.y, inv.x, oi.x);
+            float c1 = fmaf(n1.z, inv.y, oi.y), d1 = fmaf(n1.w, inv.y, oi.y);
+            float e1 = fmaf(n2.z, inv.z, oi.z), f1 = fmaf(n2.w, inv.z, oi.z);
+            float tn1 = fmaxf(fmaxf(fminf(a1, b1), fminf(c1, d1)), fmaxf(fminf(e1, f1), tmin));
+            float tf1 = fminf(fminf(fmaxf(a1, b1), fmaxf(c1, d1)), fminf(fmaxf(e1, f1), hitT));
+            bool h0 = tn0 <= tf0 * 1.0000004f, h1 = tn1 <= tf1 * 1.0000004f;
+            uint32_t r0 = __float_as_uint(n3.x), r1 = __float_as_uint(n3.y);
+            if (h0 && h1) {
+                uint32_t nearR = r0, farR = r1;
+                if (tn1 < tn0) { nearR = r1; farR = r0; }
+                if (sp < kSmemStack) sstack[sp * kTraceBlock + tid] = (int)farR;
+                else if (sp < kMaxStack) lstack[sp - kSmemStack] = (int)farR;
+                else { atomicOr(errFlags, 1); return r; }
+                ++sp;
+                ref = nearR;
+                continue;
+            } else if (h0) { ref = r0; continue; }
+            else if (h1) { ref = r1; continue; }
+        } else {
+            int first = (int)(ref & kLeafFirstMask);
+            int cnt = (int)((ref >> kLeafCountShift) & 0xF) + 1;
+            for (int k = 0; k < cnt; ++k) {
+                int ti = first + k;
+                float4 a = __ldg(&sc.triv[3 * (size_t)ti]), b = __ldg(&sc.triv[3 * (size_t)ti + 1]), c = __ldg(&sc.triv[3 * (size_t)ti + 2]);
+                float t, u, v;
+                // allow an equal distance so that ties can resolve to the smaller id
+                float lim = ANY ? r.t : __uint_as_float(__float_as_uint(r.t) + (r.t < CUDART_INF_F ? 1u : 0u));
+                if (isectTri(org, pre, f3(a), f3(b), f3(c), tmin, lim, t, u, v)) {
+                    int gid = __float_as_int(a.w);
+                    if (ANY) { r.t = t; r.u = u; r.v = v; r.tri = ti; return r; }
+                    if (t < r.t || (t == r.t && gid < bestGid)) { r.t = t; r.u = u; r.v = v; r.tri = ti; bestGid = gid; }
+                }
+            }
+        }
+        if (sp == 0) break;
+        --sp;
+        ref = (uint32_t)(sp < kSmemStack ? sstack[sp * kTraceBlock + tid] : lstack[sp - kSmemStack]);
+    }
+    return r;
+}
+
+// mode 0: closest hit -> hits[i]; mode 1: shadow rays, zero nee[tgt[i]] when occluded;
+// mode 2: any hit -> occl[i] = 1/0.
+template <int MODE>
+__global__ void __launch_bounds__(kTraceBlock) k_trace(DevScene sc, const float4* ro, const float4* rd, const int* count, int* work,
+                                                       float4* hits, const int* tgt, float4* nee, int* occl, DevStats* stats,
+                                                       int countRays) {
+    __shared__ int sstack[kSmemStack * kTraceBlock];
+    const int n = *count;
+    const int lane = threadIdx.x & 31;
+    if (countRays && blockIdx.x == 0 && threadIdx.x == 0) {
+        if (MODE == 0) atomicAdd(&stats->rays, (unsigned long long)n);
+    }
+    for (;;) {
+        int base = 0;
+        if (lane == 0) base = atomicAdd(work, 32);
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (base >= n) break;
+        int i = base + lane;
+        if (i < n) {
+            float4 o = ro[i], d = rd[i];
+            TraceResult h = traverse<MODE != 0>(sc, f3(o), f3(d), o.w, d.w, sstack, &stats->errorFlags);
+            if (MODE == 0) {
+                hits[i] = make_float4(h.t, h.u, h.v, __int_as_float(h.tri));
+            } else if (MODE == 1) {
+                if (h.tri >= 0) nee[tgt[i]] = make_float4(0.f, 0.f, 0.f, 0.f);
+            } else {
+                occl[i] = h.tri >= 0 ? 1 : 0;
+            }
+        }
+    }
+}
+
+int traceGrid() {
+    static int g = 0;
+    if (g == 0) {
+        int dev, sms, bps;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_trace<0>, kTraceBlock, 0);
+        g = sms * (bps > 0 ? bps : 1);
+    }
+    return g;
+}
+
+void launch_trace_closest(const DevScene& sc, const float4* ro, const float4* rd, const int* count, int* work, float4* hits, DevStats* stats,
+                          cudaStream_t s) {
+    k_trace<0><<<traceGrid(), kTraceBlock, 0, s>>>(sc, ro, rd, count, work, hits, nullptr, nullptr, nullptr, stats, 1);
+}
+void launch_trace_shadow(const DevScene& sc, const float4* ro, const float4* rd, const int* tgt, const int* count, int* work, float4* nee,
+                         DevStats* stats, cudaStream_t s) {
+    k_trace<1><<<traceGrid(), kTraceBlock, 0, s>>>(sc, ro, rd, count, work, nullptr, tgt, nee, nullptr, stats, 0);
+}
+void launch_trace_query(const DevScene& sc, const float4* ro, const float4* rd, const int* count, int* work, float4* hits, int* occl,
+                        DevStats* stats, bool anyHit, cudaStream_t s) {
+    if (anyHit) k_trace<2><<<traceGrid(), kTraceBlock, 0, s>>>(sc, ro, rd, count, work, nullptr, nullptr, nullptr, occl, stats, 0);
+    else k_trace<0><<<traceGrid(), kTraceBlock, 0, s>>>(sc, ro, rd, count, work, hits, nullptr, nullptr, nullptr, stats, 0);
+}
+
+// =============================================================================================
+// K5 + K7 + K8: one bounce of the estimator for every queued path.
+// =============================================================================================
+SST_D void splat(float* samples, uint32_t item, float3 v) {
+    float* f = samples + 3 * (size_t)item;
+    f[0] = v.x; f[1] = v.y; f[2] = v.z;
+}
+
+// Queue `cnt` items per calling lane group and return this lane's slot.
+SST_D int aggAppend(int* counter) {
+    cg::coalesced_group g = cg::coalesced_threads();
+    int base = 0;
+    if (g.thread_rank() == 0) base = atomicAdd(counter, (int)g.size());
+    return g.shfl(base, 0) + (int)g.thread_rank();
+}
+
+template <int NS>
+__global__ void __launch_bounds__(128) k_shade(DevScene sc, PTConfig cfg, PathBuf A, PathBuf B, const float4* __restrict__ hits, float4* nee,
+                                               int cap, float4* shRo, float4* shRd, int* shTgt, const int* nIn, int* nOut, int* nSh,
+                                               float* film, DevStats* stats) {
+    const int n = *nIn;
+    if ((int)(blockIdx.x * blockDim.x) >= n) return;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool valid = i < n;
+
+    bool cont = false;
+    uint32_t outDepth = 0;
+    float3 prefix = mk(1, 1, 1), radiance = mk(0, 0, 0);
+    float prevPdfOut = 0.f;
+    float3 hitPos = mk(0, 0, 0), nRo = mk(0, 0, 0), nRd = mk(0, 0, 0);
+    float nTmax = CUDART_INF_F;
+    uint32_t pix = 0;
+    Rng rng{0};
+    int shIdx[2 * NS];
+    float3 shC[2 * NS];
+    uint32_t pend = 0;
+    int queries = 0;
+
+    if (valid) {
+        pix = A.pix[i];
+        rng.s = A.rng[i];
+        uint32_t dw = A.depth[i];
+        float4 pw = A.pw[i];
+        float4 rad4 = A.rad[i];
+        prefix = f3(pw);
+        float prevPdf = pw.w;
+        radiance = f3(rad4);
+        // resolve the NEE of the previous bounce (PathTracer.cs:363) in slot order
+        uint32_t pm = (dw >> kNeeShift) & 0xFFu;
+#pragma unroll
+        for (int k = 0; k < 2 * NS; ++k)
+            if (pm & (1u << k)) radiance = radiance + f3(nee[(size_t)k * cap + i]);
+        const uint32_t depth = dw & kDepthMask;
+        bool terminate = false;
+        if (dw & kDoneFlag) {
+            terminate = true;
+        } else {
+            float4 rd4 = A.rd[i];
+            float3 rdir = f3(rd4);
+            float4 h = hits[i];
+            int ti = __float_as_int(h.w);
+            if (ti < 0) {
+                // OnBackgroundHit (PathTracer.cs:384-400)
+                if ((int)depth >= cfg.minDepth && sc.hasEnv && cfg.enableBsdfDI) {
+                    float mis = 1.0f;
+                    if (depth > 1) {
+                        float pne = envPdf(sc.env, rdir) * (float)cfg.numShadowRays;
+                        mis = 1.0f / (1.0f + pne / prevPdf);
+                    }
+                    radiance = radiance + prefix * mis * envRadiance(sc.env, rdir);
+                }
+                terminate = true;
+            } else {
+                // SurfacePoint of the hit (Geometry/SurfacePoint.cs)
+                float4 a4 = __ldg(&sc.triv[3 * (size_t)ti]), b4 = __ldg(&sc.triv[3 * (size_t)ti + 1]), c4 = __ldg(&sc.triv[3 * (size_t)ti + 2]);
+                float4 fn = __ldg(&sc.triN[ti]);
+                int4 aux = __ldg(&sc.triAux[ti]);
+                float3 v1 = f3(a4), v2 = f3(b4), v3 = f3(c4);
+                float u = h.y, v = h.z;
+                Surf s;
+                s.pos = baryPos(v1, v2, v3, u, v);
+                s.n = f3(fn);
+                s.eps = errorOffset(v1, v2, v3, u, v);
+                s.mat = aux.x;
+                int4 vi = make_int4(0, 0, 0, 0);
+                if (aux.w) vi = __ldg(&sc.triVtx[ti]);
+                if (aux.w & 1) {
+                    float3 n1 = mk(sc.vnrm[3 * vi.x], sc.vnrm[3 * vi.x + 1], sc.vnrm[3 * vi.x + 2]);
+                    float3 n2 = mk(sc.vnrm[3 * vi.y], sc.vnrm[3 * vi.y + 1], sc.vnrm[3 * vi.y + 2]);
+                    float3 n3 = mk(sc.vnrm[3 * vi.z], sc.vnrm[3 * vi.z + 1], sc.vnrm[3 * vi.z + 2]);
+                    s.sn = normalize(u * n2 + v * n3 + (1.0f - u - v) * n1);
+                } else {
+                    s.sn = s.n;
+                }
+                if (aux.w & 2) {
+                    float w = 1.0f - u - v;
+                    s.uv = make_float2(u * sc.vuv[2 * vi.y] + v * sc.vuv[2 * vi.z] + w * sc.vuv[2 * vi.x],
+                                       u * sc.vuv[2 * vi.y + 1] + v * sc.vuv[2 * vi.z + 1] + w * sc.vuv[2 * vi.x + 1]);
+                } else {
+                    s.uv = make_float2(u, v);
+                }
+                hitPos = s.pos;
+                // SurfaceShader / ShadingContext (PathTracer.cs:334)
+                Ctx c;
+                c.f.n = s.sn;
+                basis(c.f.n, c.f.t, c.f.b);
+                c.outW = -rdir;
+                c.out = c.f.toLocal(c.outW);
+                c.faceN = s.n;
+                c.uv = s.uv;
+                const DevMaterial& m = sc.mats[s.mat];
+                Lp lp = {};
+                float3 diffBase = mk(0, 0, 0);
+                if (m.type == kGeneric) lp = localParams(sc, m, s.uv);
+                else diffBase = lookupRgb(sc, m.baseTex, m.base, s.uv);
+
+                // OnLightHit (PathTracer.cs:402-421)
+                int emIdx = __float_as_int(fn.w);
+                if (emIdx >= 0 && (int)depth >= cfg.minDepth) {
+                    const DevEmitter& em = sc.emitters[emIdx];
+                    float mis = 1.0f;
+                    if (depth > 1) {
+                        float3 prevPos = f3(A.prev[i]);
+                        float jac = areaToSolidAngle(prevPos, s.pos, s.n);
+                        float pne = em.faceN.w / (float)sc.nEmitters * (float)cfg.numShadowRays / jac;
+                        mis = 1.0f / (pne / prevPdf + 1.0f);
+                        if (!cfg.enableBsdfDI) mis = 0.0f;
+                    }
+                    radiance = radiance + prefix * mis * emitted(em, s.sn, -rdir);
+                }
+
+                // Russian roulette (PathTracer.cs:277-282, :352-354)
+                float surv = depth > 4 ? clampf(avg3(prefix), 0.05f, 0.95f) : 1.0f;
+                if (rng.nextFloat() > surv || (int)depth == cfg.maxDepth) {
+                    terminate = true;
+                } else {
+                    // Next event estimation (PathTracer.cs:357-364, :423-501)
+                    float3 neeScale = prefix;  // contributions are stored as prefix * c / surv
+                    if ((int)depth + 1 >= cfg.minDepth) {
+#pragma unroll
+                        for (int sIt = 0; sIt < NS; ++sIt) {
+                            if (sIt >= cfg.numShadowRays) break;
+                            if (sc.hasEnv) {
+                                ++queries;
+                                float e1 = rng.nextFloat(), e2 = rng.nextFloat();
+                                float3 ed; float epdf; float3 ew;
+                                envSample(sc.env, e1, e2, ed, epdf, ew);
+                                float pb;
+                                float3 bc = evalWithCos(sc, m, lp, diffBase, c, ed, pb);
+                                if (!(pb == 0.0f || epdf == 0.0f)) {
+                                    float mis = cfg.enableBsdfDI ? 1.0f / (1.0f + pb / (epdf * (float)cfg.numShadowRays)) : 1.0f;
+                                    float3 contrib = ew * bc / (float)cfg.numShadowRays;
+                                    float3 val = neeScale * (mis * contrib) / surv;
+                                    if (!isBlack(val)) {
+                                        int k = 2 * sIt;
+                                        int q = aggAppend(nSh);
+                                        float3 o = offsetPoint(s.pos, s.n, s.eps, ed);
+                                        shRo[q] = make_float4(o.x, o.y, o.z, 0.0f);
+                                        shRd[q] = make_float4(ed.x, ed.y, ed.z, CUDART_INF_F);
+                                        shIdx[k] = q;
+                                        shC[k] = val;
+                                        pend |= 1u << k;
+                                    }
+                                }
+                            }
+                            if (sc.nEmitters > 0) {
+                                ++queries;
+                                int idx = (int)rng.nextInt((uint32_t)sc.nEmitters);
+                                const DevEmitter& em = sc.emitters[idx];
+                                float selProb = 1.0f / (float)sc.nEmitters;
+                                float l1 = rng.nextFloat(), l2 = rng.nextFloat();
+                                float2 bar = toUniformTriangle(l1, l2);
+                                float3 e1 = f3(em.v1), e2 = f3(em.v2), e3 = f3(em.v3);
+                                float3 lpPos = baryPos(e1, e2, e3, bar.x, bar.y);
+                                float3 lpN = f3(em.faceN);
+                                float lpEps = errorOffset(e1, e2, e3, bar.x, bar.y);
+                                float3 lpSn = lpN;
+                                if (em.n1.w != 0.0f)
+                                    lpSn = normalize(bar.x * f3(em.n2) + bar.y * f3(em.n3) + (1.0f - bar.x - bar.y) * f3(em.n1));
+                                float3 l2s = normalize(s.pos - lpPos);
+                                float3 emis = emitted(em, lpSn, l2s);
+                                float jac = areaToSolidAngle(s.pos, lpPos, lpN);
+                                float pb;
+                                float3 bc = evalWithCos(sc, m, lp, diffBase, c, -l2s, pb);
+                                float lpPdf = em.faceN.w;
+                                float pne = lpPdf * selProb * (float)cfg.numShadowRays;
+                                float pbA = pb * jac;
+                                if (jac != 0.0f) {
+                                    float ratio = pbA / pne;
+                                    float mis = cfg.enableBsdfDI ? 1.0f / (ratio + 1.0f) : 1.0f;
+                                    float pdf = lpPdf / jac * selProb * (float)cfg.numShadowRays;
+                                    float3 contrib = emis / pdf * bc;
+                                    float3 val = neeScale * (mis * contrib) / surv;
+                                    if (!isBlack(val)) {
+                                        int k = 2 * sIt + 1;
+                                        int q = aggAppend(nSh);
+                                        float3 dd = lpPos - s.pos;
+                                        float3 o = offsetPoint(s.pos, s.n, s.eps, dd);
+                                        float3 e = offsetPoint(lpPos, lpN, lpEps, -dd);
+                                        float3 sd = e - o;
+                                        shRo[q] = make_float4(o.x, o.y, o.z, 0.0f);
+                                        shRd[q] = make_float4(sd.x, sd.y, sd.z, 1.0f - 1e-5f);
+                                        shIdx[k] = q;
+                                        shC[k] = val;
+                                        pend |= 1u << k;
+                                    }
+                                }
+                            }
+                        }
+                    }
+                    // SampleDirection (PathTracer.cs:526-530)
+                    float uc = rng.nextFloat();
+                    float u1 = rng.nextFloat(), u2 = rng.nextFloat();
+                    float3 dirW; float bpdf = 0.f; float3 bw = mk(0, 0, 0);
+                    bool ok = sampleMaterial(sc, m, lp, diffBase, c, uc, u1, u2, dirW, bpdf, bw);
+                    if (!ok || bpdf == 0.0f || isBlack(bw)) {
+                        if (pend) { cont = true; outDepth = kDoneFlag; }
+                        else terminate = true;
+                    } else {
+                        cont = true;
+                        prefix = prefix * (bw / surv);  // PathTracer.cs:372-378
+                        prevPdfOut = bpdf * surv;
+                        outDepth = depth + 1;
+                        nRo = offsetPoint(s.pos, s.n, s.eps, dirW);
+                        nRd = dirW;
+                    }
+                    outDepth |= pend << kNeeShift;
+                }
+            }
+        }
+        if (terminate) splat(film, pix, radiance);
+        if (!cont) pend = 0;
+    }
+    // shadow-query statistics (RayTracerStats.NumShadowRays semantics)
+    int totq = __reduce_add_sync(0xffffffffu, queries);
+    if ((threadIdx.x & 31) == 0 && totq) atomicAdd(&stats->shadowRays, (unsigned long long)totq);
+
+    // K7: warp ballot / popc compaction into the next queue
+    unsigned m = __ballot_sync(0xffffffffu, cont);
+    if (m == 0) return;
+    int lane = threadIdx.x & 31;
+    int base = 0;
+    if (lane == 0) base = atomicAdd(nOut, __popc(m));
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if (!cont) return;
+    int j = base + __popc(m & ((1u << lane) - 1u));
+    B.pix[j] = pix;
+    B.rng[j] = rng.s;
+    B.depth[j] = outDepth;
+    B.pw[j] = make_float4(prefix.x, prefix.y, prefix.z, prevPdfOut);
+    B.rad[j] = make_float4(radiance.x, radiance.y, radiance.z, 0.f);
+    B.prev[j] = make_float4(hitPos.x, hitPos.y, hitPos.z, 0.f);
+    B.ro[j] = make_float4(nRo.x, nRo.y, nRo.z, 0.f);
+    B.rd[j] = make_float4(nRd.x, nRd.y, nRd.z, (outDepth & kDoneFlag) ? -1.0f : nTmax);
+#pragma unroll
+    for (int k = 0; k < 2 * NS; ++k) {
+        if (pend & (1u << k)) {
+            int slot = k * cap + j;
+            shTgt[shIdx[k]] = slot;
+            nee[slot] = make_float4(shC[k].x, shC[k].y, shC[k].z, 0.f);
+        }
+    }
+}
+
+void launch_shade(int ns, const DevScene& sc, const PTConfig& cfg, const PathBuf& A, const PathBuf& B, const float4* hits, float4* nee, int cap,
+                  float4* shRo, float4* shRd, int* shTgt, const int* nIn, int* nOut, int* nSh, float* film, DevStats* stats, int maxItems,
+                  cudaStream_t s) {
+    int grid = (maxItems + 127) / 128;
+    if (grid == 0) return;
+    switch (ns) {
+        case 1: k_shade<1><<<grid, 128, 0, s>>>(sc, cfg, A, B, hits, nee, cap, shRo, shRd, shTgt, nIn, nOut, nSh, film, stats); break;
+        case 2: k_shade<2><<<grid, 128, 0, s>>>(sc, cfg, A, B, hits, nee, cap, shRo, shRd, shTgt, nIn, nOut, nSh, film, stats); break;
+        case 3: k_shade<3><<<grid, 128, 0, s>>>(sc, cfg, A, B, hits, nee, cap, shRo, shRd, shTgt, nIn, nOut, nSh, film, stats); break;
+        default: k_shade<4><<<grid, 128, 0, s>>>(sc, cfg, A, B, hits, nee, cap, shRo, shRd, shTgt, nIn, nOut, nSh, film, stats); break;
+    }
+}
+
+void launch_camera(const DevScene& sc, const PTConfig& cfg, const PathBuf& A, int pixStart, int pixCount, int n, uint32_t iterBase, int* qCount,
+                   cudaStream_t s) {
+    k_camera<<<(n + 255) / 256, 256, 0, s>>>(sc, cfg, A, pixStart, pixCount, n, iterBase, qCount);
+}
+
+// =============================================================================================
+// Function-level kernels for the parity tests
+// =============================================================================================
+SST_D Ctx ctxFromPoint(const float* p, float3 outW) {
+    Ctx c;
+    c.faceN = mk(p[3], p[4], p[5]);
+    c.f.n = mk(p[6], p[7], p[8]);
+    basis(c.f.n, c.f.t, c.f.b);
+    c.outW = outW;
+    c.out = c.f.toLocal(outW);
+    c.uv = make_float2(p[9], p[10]);
+    return c;
+}
+
+__global__ void k_debug_material_eval(DevScene sc, int mat, int n, const float* pts, const float* outs, const float* ins, float* vals, float* pdfs) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float* p = pts + 11 * (size_t)i;
+    Ctx c = ctxFromPoint(p, mk(outs[3 * i], outs[3 * i + 1], outs[3 * i + 2]));
+    const DevMaterial& m = sc.mats[mat];
+    Lp lp = {};
+    float3 db = mk(0, 0, 0);
+    if (m.type == kGeneric) lp = localParams(sc, m, c.uv);
+    else db = lookupRgb(sc, m.baseTex, m.base, c.uv);
+    float pdf;
+    float3 v = evalWithCos(sc, m, lp, db, c, mk(ins[3 * i], ins[3 * i + 1], ins[3 * i + 2]), pdf);
+    vals[3 * i] = v.x; vals[3 * i + 1] = v.y; vals[3 * i + 2] = v.z;
+    pdfs[2 * i] = pdf;
+    pdfs[2 * i + 1] = 0.0f;
+}
+
+__global__ void k_debug_material_sample(DevScene sc, int mat, int n, const float* pts, const float* outs, const float* us, float* dirs, float* pdfs,
+                                        float* ws) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float* p = pts + 11 * (size_t)i;
+    Ctx c = ctxFromPoint(p, mk(outs[3 * i], outs[3 * i + 1], outs[3 * i + 2]));
+    const DevMaterial& m = sc.mats[mat];
+    Lp lp = {};
+    float3 db = mk(0, 0, 0);
+    if (m.type == kGeneric) lp = localParams(sc, m, c.uv);
+    else db = lookupRgb(sc, m.baseTex, m.base, c.uv);
+    float3 d = mk(0, 0, 0), w = mk(0, 0, 0);
+    float pdf = 0.0f;
+    bool ok = sampleMaterial(sc, m, lp, db, c, us[3 * i], us[3 * i + 1], us[3 * i + 2], d, pdf, w);
+    if (!ok) { d = mk(0, 0, 0); pdf = 0.0f; w = mk(0, 0, 0); }
+    dirs[3 * i] = d.x; dirs[3 * i + 1] = d.y; dirs[3 * i + 2] = d.z;
+    pdfs[2 * i] = pdf;
+    pdfs[2 * i + 1] = 0.0f;
+    ws[3 * i] = w.x; ws[3 * i + 1] = w.y; ws[3 * i + 2] = w.z;
+}
+
+__global__ void k_debug_env(DevScene sc, int n, const float* us, float* dirs, float* pdfs, float* ws, const float* qd, float* rad, float* qpdf) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float3 d, w;
+    float pdf;
+    envSample(sc.env, us[2 * i], us[2 * i + 1], d, pdf, w);
+    dirs[3 * i] = d.x; dirs[3 * i + 1] = d.y; dirs[3 * i + 2] = d.z;
+    pdfs[i] = pdf;
+    ws[3 * i] = w.x; ws[3 * i + 1] = w.y; ws[3 * i + 2] = w.z;
+    float3 q = mk(qd[3 * i], qd[3 * i + 1], qd[3 * i + 2]);
+    float3 r = envRadiance(sc.env, q);
+    rad[3 * i] = r.x; rad[3 * i + 1] = r.y; rad[3 * i + 2] = r.z;
+    qpdf[i] = envPdf(sc.env, q);
+}
+
+__global__ void k_debug_rng(uint32_t base, uint32_t sample, int n, const uint32_t* pixels, int draws, uint32_t* out) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    Rng r{hashSeed(base, pixels[i], sample)};
+    for (int k = 0; k < draws; ++k) out[(size_t)i * draws + k] = r.next();
+}
+
+__global__ void k_debug_camera(DevScene sc, int n, const float* film, float* org, float* dir) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float3 o, d;
+    cameraRay(sc.cam, film[2 * i], film[2 * i + 1], o, d);
+    org[3 * i] = o.x; org[3 * i + 1] = o.y; org[3 * i + 2] = o.z;
+    dir[3 * i] = d.x; dir[3 * i + 1] = d.y; dir[3 * i + 2] = d.z;
+}
+
+void launch_debug_material_eval(const DevScene& sc, int mat, int n, const float* pts, const float* outs, const float* ins, float* vals, float* pdfs,
+                                cudaStream_t s) {
+    k_debug_material_eval<<<(n + 127) / 128, 128, 0, s>>>(sc, mat, n, pts, outs, ins, vals, pdfs);
+}
+void launch_debug_material_sample(const DevScene& sc, int mat, int n, const float* pts, const float* outs, const float* us, float* dirs, float* pdfs,
+                                  float* ws, cudaStream_t s) {
+    k_debug_material_sample<<<(n + 127) / 128, 128, 0, s>>>(sc, mat, n, pts, outs, us, dirs, pdfs, ws);
+}
+void launch_debug_env(const DevScene& sc, int n, const float* us, float* dirs, float* pdfs, float* ws, const float* qd, float* rad, float* qpdf,
+                      cudaStream_t s) {
+    k_debug_env<<<(n + 127) / 128, 128, 0, s>>>(sc, n, us, dirs, pdfs, ws, qd, rad, qpdf);
+}
+void launch_debug_rng(uint32_t base, uint32_t sample, int n, const uint32_t* pixels, int draws, uint32_t* out, cudaStream_t s) {
+    k_debug_rng<<<(n + 127) / 128, 128, 0, s>>>(base, sample, n, pixels, draws, out);
+}
+void launch_debug_camera(const DevScene& sc, int n, const float* film, float* org, float* dir, cudaStream_t s) {
+    k_debug_camera<<<(n + 127) / 128, 128, 0, s>>>(sc, n, film, org, dir);
+}
+
+}  // namespace sst

@@ -1,0 +1,33 @@
+// Launch wrappers of the kernels in sst_kernels.cu (called by the host driver in sst_api.cu).
+#pragma once
+#include <cuda_runtime.h>
+
+#include "sst_types.h"
+
+namespace sst {
+
+void launch_env_build(const float4* img, int w, int h, float* colCdf, float* rowMarg, int* hasCol, float* rowCdf, cudaStream_t s);
+void launch_camera(const DevScene& sc, const PTConfig& cfg, const PathBuf& A, int pixStart, int pixCount, int n, uint32_t iterBase, int* qCount,
+                   cudaStream_t s);
+void launch_film_fold(const PTConfig& cfg, const float* samples, int pixStart, int pixCount, int iters, uint32_t iterBase, float* film,
+                      DevStats* st, cudaStream_t s);
+void launch_trace_closest(const DevScene& sc, const float4* ro, const float4* rd, const int* count, int* work, float4* hits, DevStats* stats,
+                          cudaStream_t s);
+void launch_trace_shadow(const DevScene& sc, const float4* ro, const float4* rd, const int* tgt, const int* count, int* work, float4* nee,
+                         DevStats* stats, cudaStream_t s);
+void launch_trace_query(const DevScene& sc, const float4* ro, const float4* rd, const int* count, int* work, float4* hits, int* occl,
+                        DevStats* stats, bool anyHit, cudaStream_t s);
+void launch_shade(int ns, const DevScene& sc, const PTConfig& cfg, const PathBuf& A, const PathBuf& B, const float4* hits, float4* nee, int cap,
+                  float4* shRo, float4* shRd, int* shTgt, const int* nIn, int* nOut, int* nSh, float* film, DevStats* stats, int maxItems,
+                  cudaStream_t s);
+void launch_debug_material_eval(const DevScene& sc, int mat, int n, const float* pts, const float* outs, const float* ins, float* vals, float* pdfs,
+                                cudaStream_t s);
+void launch_debug_material_sample(const DevScene& sc, int mat, int n, const float* pts, const float* outs, const float* us, float* dirs, float* pdfs,
+                                  float* ws, cudaStream_t s);
+void launch_debug_env(const DevScene& sc, int n, const float* us, float* dirs, float* pdfs, float* ws, const float* qd, float* rad, float* qpdf,
+                      cudaStream_t s);
+void launch_debug_rng(uint32_t base, uint32_t sample, int n, const uint32_t* pixels, int draws, uint32_t* out, cudaStream_t s);
+void launch_debug_camera(const DevScene& sc, int n, const float* film, float* org, float* dir, cudaStream_t s);
+int traceGrid();
+
+}  // namespace sst

@@ -1,0 +1,139 @@
+// Device-side scene and wavefront layouts shared by the kernels and the host driver.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace sst {
+
+constexpr int kMaxShadowRays = 4;     // NumShadowRays supported per vertex
+constexpr int kTraceBlock = 128;      // threads per block of the traversal kernels
+constexpr int kSmemStack = 24;        // traversal stack entries kept in shared memory per thread
+constexpr int kMaxStack = 64;         // total stack entries (the BVH builder caps the depth below this)
+constexpr int kMaxBvhDepth = 60;
+constexpr int kMaxLeafSize = 8;
+
+// Node references: >= 0 inner node index; leaf = 0x80000000 | (count - 1) << 27 | first
+constexpr uint32_t kLeafFlag = 0x80000000u;
+constexpr int kLeafCountShift = 27;
+constexpr uint32_t kLeafFirstMask = (1u << kLeafCountShift) - 1u;
+
+enum MaterialType : int { kDiffuse = 0, kGeneric = 1 };
+
+struct DevMaterial {
+    int type;
+    int baseTex;   // texture index or -1
+    int roughTex;  // texture index or -1
+    int transmitter;
+    float base[3];
+    float rough;
+    float metallic, specTint, aniso, specTrans, ior;
+    int pad[1];
+};
+
+struct DevTexture {
+    int w, h, channels, border;
+    long long offset;  // float offset into the texel pool
+};
+
+// One emissive triangle with everything NEE needs (DiffuseEmitter / GlossyEmitter + Triangle)
+struct DevEmitter {
+    float4 v1, v2, v3;   // vertex positions (mesh order)
+    float4 n1, n2, n3;   // vertex shading normals; n1.w = 1 when the mesh has them
+    float4 faceN;        // face normal xyz, w = 1 / area
+    float4 rad;          // radiance rgb, w = glossy exponent (< 0: diffuse)
+    float norm;          // (exponent + 1) / (2 pi)
+    int globalTri;
+    int pad[2];
+};
+
+struct DevEnv {
+    int w, h;
+    const float4* img;     // w*h texels (rgb, pad)
+    const float* rowCdf;   // h
+    const float* colCdf;   // h*w
+    const int* hasCol;     // h
+};
+
+struct DevCamera {
+    float v2c[16];  // viewToCamera (row-major, row-vector convention)
+    float c2w[16];  // cameraToWorld
+    int W, H;
+};
+
+struct DevScene {
+    const float4* nodes;   // 4 float4 per node
+    const float4* triv;    // 3 float4 per leaf-ordered triangle: v1 (w = global tri id), v2, v3
+    const float4* triN;    // per leaf-ordered triangle: face normal, w = emitter index (int bits, -1)
+    const int4* triAux;    // (material, mesh, local face, attribute flags: 1 normals, 2 uvs)
+    const int4* triVtx;    // global vertex indices of the three corners
+    const float* vnrm;     // 3 floats per global vertex (0 when absent)
+    const float* vuv;      // 2 floats per global vertex
+    const DevMaterial* mats;
+    const DevTexture* texs;
+    const float* texData;
+    const DevEmitter* emitters;
+    int nEmitters;
+    int nTri;
+    int nNodes;
+    int hasEnv;
+    DevEnv env;
+    DevCamera cam;
+};
+
+struct PTConfig {
+    int W, H;
+    int maxDepth, minDepth;
+    uint32_t baseSeed;
+    int numShadowRays;
+    int enableBsdfDI;
+    int ignoreNan;
+};
+
+// Device counters of one render (zeroed per render).
+struct DevStats {
+    unsigned long long rays;
+    unsigned long long shadowRays;
+    unsigned long long nanCount;
+    int nanPixel[4];
+    int nanIter[4];
+    int errorFlags;  // bit 0: traversal stack overflow
+    int pad[3];
+};
+
+// Structure-of-arrays path state for one buffer (double-buffered A/B).
+struct PathBuf {
+    uint32_t* pix;
+    uint32_t* rng;
+    uint32_t* depth;   // bits 0-15 depth, 16-23 pending NEE slots, bit 31 done
+    float4* pw;        // prefix weight rgb, previous pdf
+    float4* rad;       // radiance estimate rgb
+    float4* prev;      // previous hit position
+    float4* ro;        // ray origin, tmin
+    float4* rd;        // ray direction, tmax
+};
+
+constexpr uint32_t kDepthMask = 0xFFFFu;
+constexpr int kNeeShift = 16;
+constexpr uint32_t kDoneFlag = 0x80000000u;
+
+struct WaveBuffers {
+    PathBuf a, b;
+    float4* hits;        // per path of the current queue: t, u, v, leaf triangle (int bits, -1 miss)
+    float4* nee;         // [slot * cap + path]: pending NEE contribution
+    float4* shRo;        // shadow queue: origin, tmin
+    float4* shRd;        // direction, tmax
+    int* shTgt;          // nee slot index
+    int* counters;       // per bounce queue lengths and work counters
+    int cap;             // paths per wave
+    int shCap;           // shadow queue capacity
+};
+
+// Counter layout (ints): [0, 1024) queue length per depth; [1024, 2048) shadow-queue length per
+// depth; [2048, 4096) work-fetch counters of the persistent traversal kernels (two per depth).
+constexpr int kMaxPathDepth = 1000;
+constexpr int kCntQueue = 0;
+constexpr int kCntShadow = 1024;
+constexpr int kCntWork = 2048;
+constexpr int kNumCounters = 4096;
+
+}  // namespace sst

@@ -1,0 +1,379 @@
+"""GPU parity: the CUDA path (through the C ABI) against the oracle on the same seeded inputs.
+
+Tolerances: integer work (RNG streams) bit-exact; single functions in FP32 to a relative 1e-4
+(absolute 1e-6 near zero) -- the kernels use fused multiply-adds and CUDA's transcendental
+functions, the oracle strict IEEE single precision; images by the reference's Validation criterion
+(mean within 1%, SeeSharp.Validation/Validator.cs:26) plus per-path agreement at 1 spp.
+"""
+import ctypes
+import math
+
+import numpy as np
+import pytest
+
+from oracle import pyoracle as O
+from seesharp_gb300 import (DiffuseMaterial, FrameBuffer, GenericMaterial, Matrix4x4, Mesh, PathTracer, PerspectiveCamera, RgbColor, RgbImage, Scene,
+                            TextureMono, TextureRgb, EnvironmentMap, DiffuseEmitter, mean_rgb, workloads)
+from seesharp_gb300 import _native
+
+pytestmark = pytest.mark.gpu
+
+
+def close(a, b, rtol=1e-4, atol=1e-6):
+    a, b = np.asarray(a, np.float64), np.asarray(b, np.float64)
+    return np.abs(a - b) <= atol + rtol * np.abs(b)
+
+
+def _p(a):
+    return ctypes.c_void_p(a.ctypes.data)
+
+
+# ---------------------------------------------------------------------------------------------
+def test_rng_streams_bit_exact():
+    L = _native.load_library()
+    pixels = np.arange(0, 4096 * 37, 37, dtype=np.uint32)
+    out = np.zeros((pixels.size, 8), np.uint32)
+    _native.check(L.sst_debug_rng(0xC030114, 5, pixels.size, _p(pixels), 8, _p(out)))
+    for i in range(0, pixels.size, 97):
+        seed = O.rng_hashseed(0xC030114, int(pixels[i]), 5)
+        assert np.array_equal(out[i], O.rng_stream(seed, 8))
+
+
+def test_camera_rays():
+    sc = workloads.cornell_box(37, 23)
+    sc.Prepare()
+    o = O.OracleScene.from_scene(sc)
+    rng = np.random.default_rng(1)
+    film = np.ascontiguousarray(rng.uniform(0, 1, size=(500, 2)) * [37, 23], np.float32)
+    org = np.zeros((500, 3), np.float32)
+    d = np.zeros((500, 3), np.float32)
+    _native.check(sc.native.lib.sst_debug_camera(sc.native.handle, 500, _p(film), _p(org), _p(d)))
+    for i in range(500):
+        eo, ed = o.camera_ray(*film[i])
+        assert np.all(close(org[i], eo)) and np.all(close(d[i], ed, 1e-5, 1e-6))
+
+
+# ---------------------------------------------------------------------------------------------
+def material_scene(materials):
+    sc = Scene()
+    for mat in materials:
+        m = Mesh([[-1, -1, 0], [1, -1, 0], [1, 1, 0], [-1, 1, 0]], [0, 1, 2, 0, 2, 3])
+        m.Material = mat
+        sc.Meshes.append(m)
+    e = Mesh([[-1, -1, 5], [1, -1, 5], [1, 1, 5]], [0, 1, 2])
+    e.Material = DiffuseMaterial()
+    sc.Meshes.append(e)
+    sc.Emitters.extend(DiffuseEmitter.MakeFromMesh(e, RgbColor.White))
+    sc.Camera = PerspectiveCamera(Matrix4x4.CreateLookAt([0, 0, 3], [0, 0, 0], [0, 1, 0]), 40)
+    sc.FrameBuffer = FrameBuffer(8, 8)
+    return sc
+
+
+MATERIALS = [
+    DiffuseMaterial(DiffuseMaterial.Parameters(BaseColor=TextureRgb(RgbColor(0.7, 0.4, 0.2)))),
+    DiffuseMaterial(DiffuseMaterial.Parameters(BaseColor=TextureRgb(RgbColor(0.5, 0.5, 0.9)), Transmitter=True)),
+    GenericMaterial(GenericMaterial.Parameters(BaseColor=TextureRgb(RgbColor(0.8, 0.3, 0.1)), Roughness=TextureMono(0.4))),
+    GenericMaterial(GenericMaterial.Parameters(BaseColor=TextureRgb(RgbColor(0.9, 0.8, 0.3)), Roughness=TextureMono(0.2), Metallic=0.6)),
+    GenericMaterial(GenericMaterial.Parameters(BaseColor=TextureRgb(RgbColor(1, 1, 1)), Roughness=TextureMono(0.2), SpecularTransmittance=0.8)),
+    GenericMaterial(GenericMaterial.Parameters(Roughness=TextureMono(0.1), SpecularTransmittance=1.0, SpecularTintStrength=0.0, Anisotropic=0.5)),
+    GenericMaterial(GenericMaterial.Parameters(BaseColor=TextureRgb(RgbColor(0.3, 0.6, 0.2)), Roughness=TextureMono(0.9), IndexOfRefraction=1.1)),
+]
+
+
+def random_points(rng, n):
+    pts = np.zeros((n, 11), np.float32)
+    # tilted shading normals around a face normal, shading normal = face normal half the time
+    fn = rng.normal(size=(n, 3))
+    fn /= np.linalg.norm(fn, axis=1, keepdims=True)
+    sn = fn + 0.2 * rng.normal(size=(n, 3)) * (rng.random((n, 1)) < 0.5)
+    sn /= np.linalg.norm(sn, axis=1, keepdims=True)
+    pts[:, 3:6] = fn
+    pts[:, 6:9] = sn
+    pts[:, 9:11] = rng.random((n, 2))
+    return pts
+
+
+def unit(rng, n):
+    v = rng.normal(size=(n, 3))
+    return (v / np.linalg.norm(v, axis=1, keepdims=True)).astype(np.float32)
+
+
+@pytest.mark.parametrize("mi", range(len(MATERIALS)))
+def test_material_eval_and_pdf(mi):
+    sc = material_scene([MATERIALS[mi]])
+    sc.Prepare()
+    o = O.OracleScene.from_scene(sc)
+    rng = np.random.default_rng(100 + mi)
+    n = 2000
+    pts, outs, ins = random_points(rng, n), unit(rng, n), unit(rng, n)
+    vals = np.zeros((n, 3), np.float32)
+    pdfs = np.zeros((n, 2), np.float32)
+    _native.check(sc.native.lib.sst_debug_material_eval(sc.native.handle, 0, n, _p(pts), _p(outs), _p(ins), _p(vals), _p(pdfs)))
+    bad = 0
+    for i in range(n):
+        ev, ep = o.material_eval(0, pts[i], outs[i], ins[i])
+        ok = np.all(close(vals[i], ev, 1e-3, 1e-5)) and close(pdfs[i, 0], ep[0], 1e-3, 1e-5)
+        bad += not ok
+    assert bad <= n * 0.002, f"{bad} of {n} evaluations differ"
+
+
+@pytest.mark.parametrize("mi", range(len(MATERIALS)))
+def test_material_sample(mi):
+    sc = material_scene([MATERIALS[mi]])
+    sc.Prepare()
+    o = O.OracleScene.from_scene(sc)
+    rng = np.random.default_rng(200 + mi)
+    n = 2000
+    pts, outs = random_points(rng, n), unit(rng, n)
+    us = rng.random((n, 3)).astype(np.float32)
+    dirs = np.zeros((n, 3), np.float32)
+    pdfs = np.zeros((n, 2), np.float32)
+    ws = np.zeros((n, 3), np.float32)
+    _native.check(sc.native.lib.sst_debug_material_sample(sc.native.handle, 0, n, _p(pts), _p(outs), _p(us), _p(dirs), _p(pdfs), _p(ws)))
+    bad = 0
+    for i in range(n):
+        d, pdf, w = o.material_sample(0, pts[i], outs[i], *us[i])
+        if pdf[0] == 0 or not np.all(np.isfinite(w)):
+            ok = pdfs[i, 0] == 0 or not np.all(np.isfinite(ws[i]))
+        else:
+            ok = np.all(close(dirs[i], d, 1e-3, 1e-5)) and close(pdfs[i, 0], pdf[0], 1e-3, 1e-5) and np.all(close(ws[i], w, 1e-3, 1e-5))
+        bad += not ok
+    assert bad <= n * 0.002, f"{bad} of {n} samples differ"
+
+
+# ---------------------------------------------------------------------------------------------
+def test_environment_map():
+    sc = material_scene([MATERIALS[0]])
+    img = workloads.procedural_sky(512, 256, seed=4)
+    sc.Background = EnvironmentMap(RgbImage(img))
+    sc.Prepare()
+    o = O.OracleScene.from_scene(sc)
+    rng = np.random.default_rng(3)
+    n = 4000
+    us = rng.random((n, 2)).astype(np.float32)
+    qd = unit(rng, n)
+    dirs = np.zeros((n, 3), np.float32)
+    pdfs = np.zeros(n, np.float32)
+    ws = np.zeros((n, 3), np.float32)
+    rad = np.zeros((n, 3), np.float32)
+    qp = np.zeros(n, np.float32)
+    _native.check(sc.native.lib.sst_debug_envmap(sc.native.handle, n, _p(us), _p(dirs), _p(pdfs), _p(ws), _p(qd), _p(rad), _p(qp)))
+    bad = 0
+    for i in range(n):
+        d, pdf, w = o.env_sample(*us[i])
+        ok = np.all(close(dirs[i], d, 1e-4, 1e-5)) and close(pdfs[i], pdf, 1e-4) and np.all(close(ws[i], w, 1e-4, 1e-5))
+        ok = ok and np.all(rad[i] == o.env_radiance(qd[i])) and close(qp[i], o.env_pdf(qd[i]), 1e-4)
+        bad += not ok
+    assert bad <= n * 0.002, f"{bad} of {n} environment queries differ"
+
+
+def test_environment_known_answers():
+    """Background_EnvironmentMap.cs:25-95 on the device."""
+    sc = material_scene([MATERIALS[0]])
+    img = RgbImage(512, 256)
+    img.AtomicAdd(128, 64, RgbColor.White * 10)
+    sc.Background = EnvironmentMap(img)
+    sc.Prepare()
+    q = np.array([[0, 1, 1], [0, -1, 0], [-1, 0, 0], [0, 1, 1]], np.float32)
+    us = np.full((4, 2), 0.2, np.float32)
+    dirs, pdfs, ws = np.zeros((4, 3), np.float32), np.zeros(4, np.float32), np.zeros((4, 3), np.float32)
+    rad, qp = np.zeros((4, 3), np.float32), np.zeros(4, np.float32)
+    _native.check(sc.native.lib.sst_debug_envmap(sc.native.handle, 4, _p(us), _p(dirs), _p(pdfs), _p(ws), _p(q), _p(rad), _p(qp)))
+    assert np.all(rad[0] == 10) and np.all(rad[1] == 0) and np.all(rad[2] == 0)
+    # sample pdf consistent with DirectionPdf of the sampled direction (to 3 places)
+    dq = np.ascontiguousarray(dirs[:1])
+    _native.check(sc.native.lib.sst_debug_envmap(sc.native.handle, 1, _p(us), _p(dirs), _p(pdfs), _p(ws), _p(dq), _p(rad), _p(qp)))
+    assert round(float(pdfs[0]), 3) == round(float(qp[0]), 3)
+
+
+# ---------------------------------------------------------------------------------------------
+def triangle_soup(rng, n):
+    c = rng.uniform(-5, 5, size=(n, 1, 3))
+    v = (c + rng.normal(scale=0.6, size=(n, 3, 3))).astype(np.float32)
+    sc = Scene()
+    m = Mesh(v.reshape(-1, 3), np.arange(3 * n, dtype=np.int32))
+    m.Material = DiffuseMaterial()
+    sc.Meshes.append(m)
+    sc.Emitters.extend(DiffuseEmitter.MakeFromMesh(m, RgbColor.White))
+    sc.Camera = PerspectiveCamera(Matrix4x4.CreateLookAt([0, 0, 12], [0, 0, 0], [0, 1, 0]), 40)
+    sc.FrameBuffer = FrameBuffer(8, 8)
+    return sc
+
+
+@pytest.mark.parametrize("seed,ntri", [(1, 300), (2, 3000)])
+def test_intersection_against_fp64(seed, ntri):
+    """Closest hit: primitive id exact and t to a relative 1e-5 on non-degenerate rays, against an
+    FP64 brute-force watertight intersector."""
+    rng = np.random.default_rng(seed)
+    sc = triangle_soup(rng, ntri)
+    sc.Prepare()
+    o = O.OracleScene.from_scene(sc, fp64=False)
+    n = 4000
+    org = rng.uniform(-8, 8, size=(n, 3))
+    tgt = rng.uniform(-4, 4, size=(n, 3))
+    d = tgt - org
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    rays = np.zeros((n, 8), np.float32)
+    rays[:, 0:3] = org
+    rays[:, 4:7] = d
+    rays[:, 7] = np.inf
+    hits = sc.native.trace(rays).view(np.float32)
+    mesh_id = hits[:, 4].view(np.int32)
+    prim = hits[:, 3].view(np.int32)
+    ref, second = o.trace_brute64(rays[:, 0:3].astype(np.float64), rays[:, 4:7].astype(np.float64), with_second=True)
+    checked = 0
+    for i in range(n):
+        rt, ru, rv, rtri = ref[i]
+        rtri = int(rtri)
+        if rtri < 0:
+            assert mesh_id[i] == -1, i
+            continue
+        # non-degenerate: away from triangle edges and from the next surface along the ray
+        w = 1 - ru - rv
+        if min(ru, rv, w) < 1e-4 or (second[i] - rt) < 1e-4 * rt:
+            continue
+        assert mesh_id[i] == 0 and prim[i] == rtri, (i, prim[i], rtri)
+        assert abs(hits[i, 0] - rt) <= 1e-5 * rt, (hits[i, 0], rt)
+        checked += 1
+    assert checked > n // 4
+
+
+def test_occlusion_queries():
+    rng = np.random.default_rng(9)
+    sc = triangle_soup(rng, 500)
+    sc.Prepare()
+    o = O.OracleScene.from_scene(sc)
+    n = 3000
+    rays = np.zeros((n, 8), np.float32)
+    rays[:, 0:3] = rng.uniform(-8, 8, size=(n, 3))
+    rays[:, 4:7] = unit(rng, n)
+    rays[:, 7] = rng.uniform(0.5, 20, size=n)
+    occ = sc.native.occluded(rays)
+    t, u, v, tri = o.trace(rays, any_hit=True)
+    # compare only rays whose closest hit is not within 1e-4 of the segment end
+    tc, _, _, tric = o.trace(np.where(np.arange(8) == 7, np.inf, rays).astype(np.float32))
+    sel = (tric < 0) | (np.abs(tc - rays[:, 7]) > 1e-4 * rays[:, 7])
+    assert np.array_equal(occ[sel] != 0, tri[sel] >= 0)
+
+
+# ---------------------------------------------------------------------------------------------
+def render_gpu(sc, spp, depth, seed=0xC030114, **kw):
+    sc.FrameBuffer.Reset()
+    pt = PathTracer(TotalSpp=spp, MaxDepth=depth, BaseSeed=seed, **kw)
+    pt.Render(sc)
+    return sc.FrameBuffer.Image.data.copy(), pt.last_stats
+
+
+def render_oracle(sc, spp, depth, seed=0xC030114, **kw):
+    o = O.OracleScene.from_scene(sc)
+    film, rays, srays = o.render(o.params(sc.FrameBuffer.Width, sc.FrameBuffer.Height, spp, depth, baseSeed=seed, **kw))
+    return film, rays, srays
+
+
+def per_path_agreement(a, b, rtol=1e-3, atol=1e-4):
+    ok = np.all(np.abs(a - b) <= atol + rtol * np.abs(b), axis=2)
+    return ok.mean()
+
+
+def test_cornell_box_paths_match():
+    """1 spp: the film is each path's radiance; paths agree with the oracle's, except the rare
+    ones where an FP32 rounding difference flips a discrete decision."""
+    sc = workloads.cornell_box(96, 96)
+    sc.Prepare()
+    g, st = render_gpu(sc, 1, 5)
+    r, rays, srays = render_oracle(sc, 1, 5)
+    assert per_path_agreement(g, r) >= 0.99
+    assert st.numRays == rays
+    assert abs(int(st.numShadowRays) - srays) <= 0.01 * srays
+
+
+def test_cornell_box_image_mean():
+    sc = workloads.cornell_box(128, 128)
+    sc.Prepare()
+    g, _ = render_gpu(sc, 16, 5)
+    r, _, _ = render_oracle(sc, 16, 5)
+    assert abs(mean_rgb(g) - mean_rgb(r)) <= 0.01 * mean_rgb(r)
+    assert per_path_agreement(g, r, 1e-2, 1e-3) >= 0.98
+
+
+@pytest.mark.parametrize("name", list(workloads.VALIDATION_SCENES))
+def test_validation_scenes(name):
+    """SeeSharp.Validation scenes at reduced resolution: image means within 1%."""
+    sc, spp, depth = workloads.VALIDATION_SCENES[name](96, 96)
+    sc.Prepare()
+    g, _ = render_gpu(sc, spp, depth)
+    r, _, _ = render_oracle(sc, spp, depth)
+    assert np.isfinite(g).all()
+    assert abs(mean_rgb(g) - mean_rgb(r)) <= 0.01 * mean_rgb(r), (mean_rgb(g), mean_rgb(r))
+    assert per_path_agreement(g, r, 1e-2, 1e-3) >= 0.97
+
+
+def test_sphere_field_paths_match():
+    sc = workloads.sphere_field(12, 80, 80, level=3)
+    sc.Prepare()
+    g, st = render_gpu(sc, 1, 8)
+    r, rays, srays = render_oracle(sc, 1, 8)
+    assert per_path_agreement(g, r) >= 0.98
+    assert abs(int(st.numRays) - rays) <= 0.01 * rays
+
+
+def test_min_depth_and_no_bsdf_di():
+    sc = workloads.cornell_box(48, 48)
+    sc.Prepare()
+    for kw in ({"MinDepth": 3}, {"EnableBsdfDI": False}, {"NumShadowRays": 2}):
+        pt = PathTracer(TotalSpp=4, MaxDepth=6, **kw)
+        sc.FrameBuffer.Reset()
+        pt.Render(sc)
+        g = sc.FrameBuffer.Image.data.copy()
+        o = O.OracleScene.from_scene(sc)
+        r, _, _ = o.render(o.params(48, 48, 4, 6, minDepth=kw.get("MinDepth", 1), enableBsdfDI=kw.get("EnableBsdfDI", True),
+                                    numShadowRays=kw.get("NumShadowRays", 1)))
+        assert abs(mean_rgb(g) - mean_rgb(r)) <= 0.01 * max(mean_rgb(r), 1e-6), kw
+        assert per_path_agreement(g, r, 1e-2, 1e-3) >= 0.97, kw
+
+
+def test_progressive_resume_is_exact():
+    """Rendering 3 iterations, then resuming to 7, equals rendering 7 at once (same running mean)."""
+    sc = workloads.cornell_box(40, 40)
+    sc.Prepare()
+    full, _ = render_gpu(sc, 7, 5)
+    sc.FrameBuffer.Reset()
+    PathTracer(TotalSpp=3, MaxDepth=5).Render(sc)
+    assert sc.FrameBuffer.CurIteration == 3
+    PathTracer(TotalSpp=7, MaxDepth=5).Render(sc)
+    assert sc.FrameBuffer.CurIteration == 7
+    assert np.array_equal(sc.FrameBuffer.Image.data, full)
+
+
+def test_wave_splitting_is_exact(monkeypatch):
+    """Waves smaller than the image (several waves per iteration) give the identical film."""
+    sc = workloads.cornell_box(64, 48)
+    sc.Prepare()
+    a, _ = render_gpu(sc, 3, 5)
+    import os
+    os.environ["SST_WAVE_CAPACITY"] = "1000"
+    try:
+        b, _ = render_gpu(sc, 3, 5)
+    finally:
+        del os.environ["SST_WAVE_CAPACITY"]
+    assert np.array_equal(a, b)
+
+
+def test_invalid_scene_raises():
+    from seesharp_gb300 import InvalidOperationException
+    sc = workloads.cornell_box(8, 8)
+    sc.Meshes[0].Material = None
+    with pytest.raises(InvalidOperationException):
+        sc.Prepare()
+
+
+def test_device_film_pointer():
+    """sst_render with a device film (SST_MEM_DEVICE) equals the host-film path."""
+    import torch
+    sc = workloads.cornell_box(32, 32)
+    sc.Prepare()
+    host, _ = render_gpu(sc, 2, 4)
+    film = torch.zeros((32, 32, 3), dtype=torch.float32, device="cuda:0")
+    p = _native.make_params(32, 32, 2, 4)
+    sc.native.render(p, film.data_ptr(), _native.SST_MEM_DEVICE)
+    assert np.array_equal(film.cpu().numpy(), host)
