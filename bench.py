@@ -262,7 +262,7 @@ def run_ours(args, cfg):
 
     # e2e through the public API with host buffers: Prepare (geometry H2D, BVH) + Render (film D2H)
     from seesharp_gb300 import FrameBuffer
-    e2e_steps = max(1, min(args.steps, 3))
+    e2e_steps = 0 if args.no_e2e else max(1, min(args.steps, 3))
     h2d = scene_bytes(sc)
     d2h = W * H * 12
     barrier(ws)
@@ -271,9 +271,10 @@ def run_ours(args, cfg):
         sc.FrameBuffer = FrameBuffer(W, H)
         sc.Prepare()
         PathTracer(TotalSpp=spp, MaxDepth=depth).Render(sc)
-    e2e_s = max_over_ranks(ws, (time.perf_counter() - t0) / e2e_steps)
-    e2e_val = samples * ws / e2e_s / 1e6
-    assert np.isfinite(sc.FrameBuffer.Image.data).all()
+    e2e_s = max_over_ranks(ws, (time.perf_counter() - t0) / max(e2e_steps, 1))
+    e2e_val = samples * ws / e2e_s / 1e6 if e2e_steps else None
+    if e2e_steps:
+        assert np.isfinite(sc.FrameBuffer.Image.data).all()
 
     # roofline of the dominant traversal kernel
     peak, peak_kind = measured_peaks()
@@ -308,13 +309,13 @@ def run_ours(args, cfg):
             "config": {"workload": cfg["name"], "triangles": info["triangles"], "emitters": info["emitters"], "bvh_nodes": info["bvh_nodes"],
                        "width": W, "height": H, "spp": spp, "max_depth": depth, "l2": "256 MB buffer written between timed steps",
                        "parallelism": f"replicas x{ws}"},
-            "e2e": {"value": round(e2e_val, 3), "unit": "Msamples/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+            "e2e": {"value": None if e2e_val is None else round(e2e_val, 3), "unit": "Msamples/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                     "s_per_step": round(e2e_s, 4), "includes": "Scene.Prepare (upload + BVH build) + PathTracer.Render (film read-back)"},
             "roofline": roofline,
             "bytes_per_sample": round(b_sample, 1), "rays_per_sample": round(ext, 4), "shadow_rays_per_sample": round(sh, 4),
             "gpu_launches": launches,
             "kernel_ms": {k: round(v["ms"], 3) for k, v in ktimes.items()},
-            "prepare_s": round(prep_s, 3),
+            "prepare_s": round(prep_s, 3), "bvh": os.environ.get("SST_BVH", "lbvh"),
             "clocks": clocks,
             "cpu_baseline": cpu,
         }
@@ -333,8 +334,17 @@ def main():
     ap.add_argument("--config", type=int, default=1, choices=sorted(CONFIGS))
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--width", type=int, default=None, help="override (profiling cases)")
+    ap.add_argument("--height", type=int, default=None)
+    ap.add_argument("--spp", type=int, default=None)
     args = ap.parse_args()
-    cfg = CONFIGS[args.config]
+    cfg = dict(CONFIGS[args.config])
+    for k, a in (("W", args.width), ("H", args.height), ("spp", args.spp)):
+        if a is not None:
+            cfg[k] = a
+            cfg["name"] = cfg["name"] + f"_{k}{a}"
+    os.environ.setdefault("SST_BVH", "lbvh")
     if args.impl == "reference":
         run_reference(args, cfg)
     else:

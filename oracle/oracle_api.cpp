@@ -139,6 +139,38 @@ template <class T> void renderRows(Handle* h, const PTParams& P, uint32_t sample
     for (auto& t : th) t.join();
     if (stats) { stats[0] += rays.load(); stats[1] += srays.load(); }
 }
+template <class T> static void matEval(const Scene<T>& sc, int mat, const float* pt, const float* outDir, const float* inDir, float* value, float* pdf2,
+                                       float* comp) {
+    SurfacePoint<T> sp = PointFrom<T>(pt);
+    ShadingContext<T> ctx(sp, V3<T>(outDir[0], outDir[1], outDir[2]));
+    MaterialEval<T> me{sc, sc.materials[mat]};
+    V3<T> in(inDir[0], inDir[1], inDir[2]);
+    Rgb<T> v = me.EvaluateWithCosine(ctx, in);
+    ComponentWeights<T> cw;
+    T p0, p1;
+    me.Pdf(ctx, in, p0, p1, &cw);
+    pdf2[0] = float(p0); pdf2[1] = float(p1);
+    value[0] = float(v.r); value[1] = float(v.g); value[2] = float(v.b);
+    if (comp) {
+        comp[0] = float(cw.n);
+        for (int k = 0; k < 3; ++k) { comp[1 + k] = float(cw.pdfs[k]); comp[4 + k] = float(cw.weights[k]); comp[7 + k] = float(cw.pdfsRev[k]); comp[10 + k] = float(cw.weightsRev[k]); }
+    }
+}
+template <class T> static void matSample(const Scene<T>& sc, int mat, const float* pt, const float* outDir, float u, float u1, float u2, float* dir,
+                                         float* pdf2, float* weight, float* comp) {
+    SurfacePoint<T> sp = PointFrom<T>(pt);
+    ShadingContext<T> ctx(sp, V3<T>(outDir[0], outDir[1], outDir[2]));
+    MaterialEval<T> me{sc, sc.materials[mat]};
+    ComponentWeights<T> cw;
+    BsdfSample<T> s = me.Sample(ctx, T(u), V2<T>(T(u1), T(u2)), &cw);
+    dir[0] = float(s.Direction.x); dir[1] = float(s.Direction.y); dir[2] = float(s.Direction.z);
+    pdf2[0] = float(s.Pdf); pdf2[1] = float(s.PdfReverse);
+    weight[0] = float(s.Weight.r); weight[1] = float(s.Weight.g); weight[2] = float(s.Weight.b);
+    if (comp) {
+        comp[0] = float(cw.n);
+        for (int k = 0; k < 3; ++k) { comp[1 + k] = float(cw.pdfs[k]); comp[4 + k] = float(cw.weights[k]); comp[7 + k] = float(cw.pdfsRev[k]); comp[10 + k] = float(cw.weightsRev[k]); }
+    }
+}
 }  // namespace
 
 extern "C" {
@@ -304,38 +336,17 @@ int ora_camera_ray(void* p, float fx, float fy, float* org, float* dir) {
 
 // Material queries at an explicit surface point pt = (position 3, face normal 3, shading normal 3,
 // uv 2).  comp (optional, 13 floats): n, pdfs[3], weights[3], pdfsRev[3], weightsRev[3].
+// Runs in the scene's precision (FP64 scenes evaluate in double and round the outputs).
 int ora_material_eval(void* p, int mat, const float* pt, const float* outDir, const float* inDir, float* value, float* pdf2, float* comp) {
     Handle* H = static_cast<Handle*>(p);
-    const Scene<float>& sc = H->s32;
-    SurfacePoint<float> sp = PointFrom<float>(pt);
-    ShadingContext<float> ctx(sp, V3<float>(outDir[0], outDir[1], outDir[2]));
-    MaterialEval<float> me{sc, sc.materials[mat]};
-    V3<float> in(inDir[0], inDir[1], inDir[2]);
-    Rgb<float> v = me.EvaluateWithCosine(ctx, in);
-    ComponentWeights<float> cw;
-    me.Pdf(ctx, in, pdf2[0], pdf2[1], &cw);
-    value[0] = v.r; value[1] = v.g; value[2] = v.b;
-    if (comp) {
-        comp[0] = float(cw.n);
-        for (int k = 0; k < 3; ++k) { comp[1 + k] = cw.pdfs[k]; comp[4 + k] = cw.weights[k]; comp[7 + k] = cw.pdfsRev[k]; comp[10 + k] = cw.weightsRev[k]; }
-    }
+    if (H->fp64) matEval(H->s64, mat, pt, outDir, inDir, value, pdf2, comp);
+    else matEval(H->s32, mat, pt, outDir, inDir, value, pdf2, comp);
     return 0;
 }
 int ora_material_sample(void* p, int mat, const float* pt, const float* outDir, float u, float u1, float u2, float* dir, float* pdf2, float* weight, float* comp) {
     Handle* H = static_cast<Handle*>(p);
-    const Scene<float>& sc = H->s32;
-    SurfacePoint<float> sp = PointFrom<float>(pt);
-    ShadingContext<float> ctx(sp, V3<float>(outDir[0], outDir[1], outDir[2]));
-    MaterialEval<float> me{sc, sc.materials[mat]};
-    ComponentWeights<float> cw;
-    BsdfSample<float> s = me.Sample(ctx, u, V2<float>(u1, u2), &cw);
-    dir[0] = s.Direction.x; dir[1] = s.Direction.y; dir[2] = s.Direction.z;
-    pdf2[0] = s.Pdf; pdf2[1] = s.PdfReverse;
-    weight[0] = s.Weight.r; weight[1] = s.Weight.g; weight[2] = s.Weight.b;
-    if (comp) {
-        comp[0] = float(cw.n);
-        for (int k = 0; k < 3; ++k) { comp[1 + k] = cw.pdfs[k]; comp[4 + k] = cw.weights[k]; comp[7 + k] = cw.pdfsRev[k]; comp[10 + k] = cw.weightsRev[k]; }
-    }
+    if (H->fp64) matSample(H->s64, mat, pt, outDir, u, u1, u2, dir, pdf2, weight, comp);
+    else matSample(H->s32, mat, pt, outDir, u, u1, u2, dir, pdf2, weight, comp);
     return 0;
 }
 

@@ -19,6 +19,7 @@
 #include <vector>
 
 #include "../../include/sst.h"
+#include "sst_bvh.h"
 #include "sst_kernels.h"
 #include "sst_types.h"
 
@@ -176,7 +177,7 @@ struct sst_scene {
     // device
     DevBuf nodes, triv, triN, triAux, triVtx, vnrm, vuv, mats, texs, texData, ems, envImg, envRowCdf, envColCdf, envHasCol, envRowMarg;
     DevScene dev{};
-    int nTri = 0, nNodes = 0;
+    int nTri = 0, nNodes = 0, bvhDepth = 0;
     std::vector<int> meshTriOffset;
 };
 
@@ -425,51 +426,92 @@ static void commitScene(sst_scene* s, int W, int H) {
         if (triEmitter[g] >= 0) fail(SST_ERR_INVALID_SCENE, "two emitters on the same triangle");
         triEmitter[g] = int(e);
     }
-    // BVH over all triangles
-    BvhBuilder b;
-    b.box.resize(nt);
-    b.cen.resize(3 * size_t(nt));
-    std::vector<int> gMesh(nt), gFace(nt);
+    // per-triangle records in global order
+    std::vector<float4> trivG(3 * size_t(nt)), triNG(nt);
+    std::vector<int4> auxG(nt), vtxG(nt);
     {
         int g = 0;
         for (size_t mi = 0; mi < s->meshes.size(); ++mi) {
             const HostMesh& m = s->meshes[mi];
+            int vo = vtxOffset[mi];
+            int flags = (m.N.empty() ? 0 : 1) | (m.UV.empty() ? 0 : 2);
             for (size_t f = 0; f < m.I.size() / 3; ++f, ++g) {
-                gMesh[g] = int(mi);
-                gFace[g] = int(f);
-                Aabb bb;
-                for (int k = 0; k < 3; ++k) bb.grow(&m.V[3 * size_t(m.I[3 * f + k])]);
-                b.box[g] = bb;
-                for (int k = 0; k < 3; ++k) b.cen[3 * size_t(g) + k] = 0.5f * (bb.lo[k] + bb.hi[k]);
+                int i0 = m.I[3 * f], i1 = m.I[3 * f + 1], i2 = m.I[3 * f + 2];
+                const float* a = &m.V[3 * size_t(i0)];
+                const float* bb = &m.V[3 * size_t(i1)];
+                const float* c = &m.V[3 * size_t(i2)];
+                float gw;
+                std::memcpy(&gw, &g, 4);
+                trivG[3 * size_t(g)] = make_float4(a[0], a[1], a[2], gw);
+                trivG[3 * size_t(g) + 1] = make_float4(bb[0], bb[1], bb[2], 0.f);
+                trivG[3 * size_t(g) + 2] = make_float4(c[0], c[1], c[2], 0.f);
+                float ew;
+                std::memcpy(&ew, &triEmitter[g], 4);
+                triNG[g] = make_float4(m.faceN[3 * f], m.faceN[3 * f + 1], m.faceN[3 * f + 2], ew);
+                auxG[g] = make_int4(m.material, int(mi), int(f), flags);
+                vtxG[g] = make_int4(vo + i0, vo + i1, vo + i2, 0);
             }
         }
     }
-    b.run(nt);
-    if (b.maxDepth >= kMaxBvhDepth) fail(SST_ERR_DEVICE_LIMIT, "BVH deeper than the traversal stack");
-    s->nNodes = int(b.nodes.size() / 4);
-    // leaf-ordered triangle data
-    std::vector<float4> triv(3 * size_t(nt)), triN(nt);
-    std::vector<int4> triAux(nt), triVtx(nt);
-    for (int t = 0; t < nt; ++t) {
-        int g = b.order[t];
-        const HostMesh& m = s->meshes[gMesh[g]];
-        int f = gFace[g];
-        int i0 = m.I[3 * f], i1 = m.I[3 * f + 1], i2 = m.I[3 * f + 2];
-        const float* a = &m.V[3 * size_t(i0)];
-        const float* bb = &m.V[3 * size_t(i1)];
-        const float* c = &m.V[3 * size_t(i2)];
-        float gw;
-        std::memcpy(&gw, &g, 4);
-        triv[3 * size_t(t)] = make_float4(a[0], a[1], a[2], gw);
-        triv[3 * size_t(t) + 1] = make_float4(bb[0], bb[1], bb[2], 0.f);
-        triv[3 * size_t(t) + 2] = make_float4(c[0], c[1], c[2], 0.f);
-        float ew;
-        std::memcpy(&ew, &triEmitter[g], 4);
-        triN[t] = make_float4(m.faceN[3 * f], m.faceN[3 * f + 1], m.faceN[3 * f + 2], ew);
-        int flags = (m.N.empty() ? 0 : 1) | (m.UV.empty() ? 0 : 2);
-        triAux[t] = make_int4(m.material, gMesh[g], f, flags);
-        int vo = vtxOffset[gMesh[g]];
-        triVtx[t] = make_int4(vo + i0, vo + i1, vo + i2, 0);
+    const char* bvhEnv = getenv("SST_BVH");
+    bool hostBuild = bvhEnv && std::string(bvhEnv) == "sah";
+    s->triv.ensure(std::max<size_t>(1, sizeof(float4) * 3 * size_t(nt)));
+    s->triN.ensure(std::max<size_t>(1, sizeof(float4) * size_t(nt)));
+    s->triAux.ensure(std::max<size_t>(1, sizeof(int4) * size_t(nt)));
+    s->triVtx.ensure(std::max<size_t>(1, sizeof(int4) * size_t(nt)));
+    if (!hostBuild && nt > 0) {
+        // GPU linear BVH (sst_bvh.cu) and a leaf-order gather on the device
+        DevBuf gTriv, gTriN, gAux, gVtx, order, scratch;
+        gTriv.upload(trivG, st);
+        gTriN.upload(triNG, st);
+        gAux.upload(auxG, st);
+        gVtx.upload(vtxG, st);
+        s->nodes.ensure(sizeof(float4) * 4 * size_t(std::max(1, nt - 1)));
+        order.ensure(sizeof(int) * size_t(nt));
+        size_t sb = lbvhScratchBytes(nt);
+        scratch.ensure(sb);
+        int nodeCount = 0, maxDepth = 0;
+        int rc = buildLbvh(gTriv.as<float4>(), nt, s->nodes.as<float4>(), order.as<int>(), scratch.p, sb, &nodeCount, &maxDepth, st);
+        if (rc != 0) fail(SST_ERR_CUDA, "GPU BVH build failed: " + std::string(cudaGetErrorString(cudaGetLastError())));
+        if (maxDepth + 2 >= kMaxStack) {
+            hostBuild = true;  // deeper than the traversal stack: use the host SAH build instead
+        } else {
+            launch_leaf_gather(order.as<int>(), nt, gTriv.as<float4>(), gTriN.as<float4>(), gAux.as<int4>(), gVtx.as<int4>(), s->triv.as<float4>(),
+                               s->triN.as<float4>(), s->triAux.as<int4>(), s->triVtx.as<int4>(), st);
+            CUDA_CHECK(cudaGetLastError());
+            CUDA_CHECK(cudaStreamSynchronize(st));
+            s->nNodes = nodeCount;
+            s->bvhDepth = maxDepth;
+        }
+    }
+    if (hostBuild || nt == 0) {
+        BvhBuilder b;
+        b.box.resize(nt);
+        b.cen.resize(3 * size_t(nt));
+        for (int g = 0; g < nt; ++g) {
+            Aabb bb;
+            for (int k = 0; k < 3; ++k) bb.grow(&trivG[3 * size_t(g) + k].x);
+            b.box[g] = bb;
+            for (int k = 0; k < 3; ++k) b.cen[3 * size_t(g) + k] = 0.5f * (bb.lo[k] + bb.hi[k]);
+        }
+        b.run(nt);
+        if (b.maxDepth >= kMaxBvhDepth) fail(SST_ERR_DEVICE_LIMIT, "BVH deeper than the traversal stack");
+        s->nNodes = int(b.nodes.size() / 4);
+        s->bvhDepth = b.maxDepth;
+        std::vector<float4> triv(3 * size_t(nt)), triN(nt);
+        std::vector<int4> triAux(nt), triVtx(nt);
+        for (int t = 0; t < nt; ++t) {
+            int g = b.order[t];
+            for (int k = 0; k < 3; ++k) triv[3 * size_t(t) + k] = trivG[3 * size_t(g) + k];
+            triN[t] = triNG[g];
+            triAux[t] = auxG[g];
+            triVtx[t] = vtxG[g];
+        }
+        s->nodes.upload(b.nodes, st);
+        s->triv.upload(triv, st);
+        s->triN.upload(triN, st);
+        s->triAux.upload(triAux, st);
+        s->triVtx.upload(triVtx, st);
     }
     std::vector<float> vnrm, vuv;
     if (anyNormals) {
@@ -522,11 +564,6 @@ static void commitScene(sst_scene* s, int W, int H) {
         texPool.insert(texPool.end(), t.data.begin(), t.data.end());
     }
     // upload
-    s->nodes.upload(b.nodes, st);
-    s->triv.upload(triv, st);
-    s->triN.upload(triN, st);
-    s->triAux.upload(triAux, st);
-    s->triVtx.upload(triVtx, st);
     s->vnrm.upload(vnrm, st);
     s->vuv.upload(vuv, st);
     s->mats.upload(s->materials, st);

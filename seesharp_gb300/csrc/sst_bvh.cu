@@ -1,0 +1,350 @@
+// GPU BVH construction (replaces the Embree build behind Raytracer.CommitScene, Scene.cs:108-113).
+//
+// Linear BVH after Karras, "Maximizing Parallelism in the Construction of BVHs, Octrees, and k-d
+// Trees" (HPG 2012):
+//   1. centroid bounds (atomic min/max on order-preserving integer images of the floats)
+//   2. 63-bit Morton keys of the triangle centroids, radix-sorted with CUB
+//   3. one thread per internal node finds its key range and split (longest common prefix, ties
+//      broken by the sorted index)
+//   4. bottom-up refit: the second child to arrive computes the parent's box, leaf count and the
+//      surface-area cost C(n) = min(Ci N A(n) [N <= kMaxLeafSize], Ct A(n) + C(l) + C(r)), which
+//      decides where subtrees collapse into multi-triangle leaves
+//   5. kept inner nodes are numbered by a prefix sum and written in the traversal layout (both
+//      child boxes in the parent, 64-byte nodes); a collapsed subtree becomes one leaf reference
+//      to its contiguous range of sorted triangles.
+#include <cub/cub.cuh>
+#include <cuda_runtime.h>
+
+#include "sst_bvh.h"
+#include "sst_types.h"
+
+namespace sst {
+
+namespace {
+
+constexpr float kCt = 1.0f;  // traversal cost relative to one triangle test
+constexpr float kCi = 1.0f;
+
+__device__ __forceinline__ int floatOrd(float f) {
+    int i = __float_as_int(f);
+    return i >= 0 ? i : i ^ 0x7FFFFFFF;
+}
+__device__ __forceinline__ float ordFloat(int i) { return __int_as_float(i >= 0 ? i : i ^ 0x7FFFFFFF); }
+
+__global__ void k_centroid_bounds(const float4* tri, int n, int* bounds /* 6: min xyz, max xyz (ordered ints) */) {
+    __shared__ int smin[3], smax[3];
+    if (threadIdx.x < 3) { smin[threadIdx.x] = 0x7FFFFFFF; smax[threadIdx.x] = (int)0x80000000; }
+    __syncthreads();
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        float4 a = tri[3 * (size_t)i], b = tri[3 * (size_t)i + 1], c = tri[3 * (size_t)i + 2];
+        float cx = 0.5f * (fminf(a.x, fminf(b.x, c.x)) + fmaxf(a.x, fmaxf(b.x, c.x)));
+        float cy = 0.5f * (fminf(a.y, fminf(b.y, c.y)) + fmaxf(a.y, fmaxf(b.y, c.y)));
+        float cz = 0.5f * (fminf(a.z, fminf(b.z, c.z)) + fmaxf(a.z, fmaxf(b.z, c.z)));
+        atomicMin(&smin[0], floatOrd(cx)); atomicMin(&smin[1], floatOrd(cy)); atomicMin(&smin[2], floatOrd(cz));
+        atomicMax(&smax[0], floatOrd(cx)); atomicMax(&smax[1], floatOrd(cy)); atomicMax(&smax[2], floatOrd(cz));
+    }
+    __syncthreads();
+    if (threadIdx.x < 3) {
+        atomicMin(&bounds[threadIdx.x], smin[threadIdx.x]);
+        atomicMax(&bounds[3 + threadIdx.x], smax[threadIdx.x]);
+    }
+}
+
+__device__ __forceinline__ unsigned long long spread21(unsigned int v) {
+    unsigned long long x = v & 0x1FFFFFu;
+    x = (x | x << 32) & 0x1F00000000FFFFull;
+    x = (x | x << 16) & 0x1F0000FF0000FFull;
+    x = (x | x << 8) & 0x100F00F00F00F00Full;
+    x = (x | x << 4) & 0x10C30C30C30C30C3ull;
+    x = (x | x << 2) & 0x1249249249249249ull;
+    return x;
+}
+
+__global__ void k_morton(const float4* tri, int n, const int* bounds, unsigned long long* keys, int* vals) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    float lo[3] = {ordFloat(bounds[0]), ordFloat(bounds[1]), ordFloat(bounds[2])};
+    float hi[3] = {ordFloat(bounds[3]), ordFloat(bounds[4]), ordFloat(bounds[5])};
+    float4 a = tri[3 * (size_t)i], b = tri[3 * (size_t)i + 1], c = tri[3 * (size_t)i + 2];
+    float cc[3] = {0.5f * (fminf(a.x, fminf(b.x, c.x)) + fmaxf(a.x, fmaxf(b.x, c.x))),
+                   0.5f * (fminf(a.y, fminf(b.y, c.y)) + fmaxf(a.y, fmaxf(b.y, c.y))),
+                   0.5f * (fminf(a.z, fminf(b.z, c.z)) + fmaxf(a.z, fmaxf(b.z, c.z)))};
+    unsigned int q[3];
+    for (int k = 0; k < 3; ++k) {
+        float ext = hi[k] - lo[k];
+        float t = ext > 0.0f ? (cc[k] - lo[k]) / ext : 0.5f;
+        q[k] = (unsigned int)fminf(fmaxf(t * 2097152.0f, 0.0f), 2097151.0f);
+    }
+    keys[i] = (spread21(q[0]) << 2) | (spread21(q[1]) << 1) | spread21(q[2]);
+    vals[i] = i;
+}
+
+// Longest common prefix of sorted keys i and j (-1 outside [0, n)); equal keys compare indices.
+__device__ __forceinline__ int delta(const unsigned long long* k, int n, int i, int j) {
+    if (j < 0 || j >= n) return -1;
+    unsigned long long a = k[i], b = k[j];
+    if (a == b) return 64 + __clz((unsigned)(i ^ j));
+    return __clzll(a ^ b);
+}
+
+// Internal node i covers sorted leaves [first, last]; children encoded >= 0 internal, < 0 leaf ~idx.
+__global__ void k_karras(const unsigned long long* k, int n, int2* range, int2* child, int* parentInner, int* parentLeaf) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n - 1) return;
+    int d = (delta(k, n, i, i + 1) - delta(k, n, i, i - 1)) >= 0 ? 1 : -1;
+    int dmin = delta(k, n, i, i - d);
+    int lmax = 2;
+    while (delta(k, n, i, i + lmax * d) > dmin) lmax <<= 1;
+    int l = 0;
+    for (int t = lmax >> 1; t >= 1; t >>= 1)
+        if (delta(k, n, i, i + (l + t) * d) > dmin) l += t;
+    int j = i + l * d;
+    int dnode = delta(k, n, i, j);
+    int s = 0;
+    int div = 2;
+    for (int t = (l + 1) / 2; ; t = (l + div - 1) / div) {
+        if (delta(k, n, i, i + (s + t) * d) > dnode) s += t;
+        if (t == 1) break;
+        div <<= 1;
+    }
+    int gamma = i + s * d + min(d, 0);
+    int first = min(i, j), last = max(i, j);
+    int left = (first == gamma) ? ~gamma : gamma;
+    int right = (last == gamma + 1) ? ~(gamma + 1) : gamma + 1;
+    range[i] = make_int2(first, last);
+    child[i] = make_int2(left, right);
+    if (left < 0) parentLeaf[~left] = i; else parentInner[left] = i;
+    if (right < 0) parentLeaf[~right] = i; else parentInner[right] = i;
+}
+
+struct NodeFit {
+    float lo[3], hi[3];
+};
+
+__device__ __forceinline__ float areaOf(const float* lo, const float* hi) {
+    float dx = fmaxf(0.0f, hi[0] - lo[0]), dy = fmaxf(0.0f, hi[1] - lo[1]), dz = fmaxf(0.0f, hi[2] - lo[2]);
+    return dx * dy + dy * dz + dz * dx;
+}
+
+// Bottom-up refit from every leaf.  boxes: 6 floats per inner node; cost: per inner node;
+// collapse[i] = 1 when the subtree is cheaper as one leaf.
+__global__ void k_refit(const float4* tri, const int* order, int n, const int2* range, const int2* child, const int* parentInner,
+                        const int* parentLeaf, int* visits, float* boxes, float* cost, int* collapse) {
+    int li = blockIdx.x * blockDim.x + threadIdx.x;
+    if (li >= n) return;
+    int node = parentLeaf[li];
+    while (node >= 0) {
+        __threadfence();
+        if (atomicAdd(&visits[node], 1) == 0) return;  // the other child is not done yet
+        __threadfence();
+        int2 c = child[node];
+        float lo[3] = {1e30f, 1e30f, 1e30f}, hi[3] = {-1e30f, -1e30f, -1e30f};
+        float cs = 0.0f;
+        for (int s = 0; s < 2; ++s) {
+            int ch = s == 0 ? c.x : c.y;
+            float clo[3], chi[3], ccost;
+            if (ch < 0) {
+                int t = order[~ch];
+                float4 a = tri[3 * (size_t)t], b = tri[3 * (size_t)t + 1], d = tri[3 * (size_t)t + 2];
+                clo[0] = fminf(a.x, fminf(b.x, d.x)); chi[0] = fmaxf(a.x, fmaxf(b.x, d.x));
+                clo[1] = fminf(a.y, fminf(b.y, d.y)); chi[1] = fmaxf(a.y, fmaxf(b.y, d.y));
+                clo[2] = fminf(a.z, fminf(b.z, d.z)); chi[2] = fmaxf(a.z, fmaxf(b.z, d.z));
+                ccost = kCi * areaOf(clo, chi);
+            } else {
+                const volatile float* bx = boxes + 6 * (size_t)ch;
+                for (int k = 0; k < 3; ++k) { clo[k] = bx[k]; chi[k] = bx[3 + k]; }
+                ccost = ((const volatile float*)cost)[ch];
+            }
+            for (int k = 0; k < 3; ++k) { lo[k] = fminf(lo[k], clo[k]); hi[k] = fmaxf(hi[k], chi[k]); }
+            cs += ccost;
+        }
+        float A = areaOf(lo, hi);
+        int2 r = range[node];
+        int cnt = r.y - r.x + 1;
+        float split = kCt * A + cs;
+        float leaf = kCi * cnt * A;
+        bool col = cnt <= kMaxLeafSize && leaf <= split;
+        float* bo = boxes + 6 * (size_t)node;
+        for (int k = 0; k < 3; ++k) { bo[k] = lo[k]; bo[3 + k] = hi[k]; }
+        cost[node] = col ? leaf : split;
+        collapse[node] = col ? 1 : 0;
+        node = parentInner[node];
+    }
+}
+
+// kept[i] = 1 when inner node i is not inside a collapsed subtree (and is not collapsed itself);
+// depth[i] = number of kept ancestors.  Walks to the root (depth bounded by the key length).
+__global__ void k_kept(const int* parentInner, const int* collapse, int n, int* kept, int* maxDepth) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n - 1) return;
+    int k = (i == 0 || !collapse[i]) ? 1 : 0;
+    int depth = 0;
+    int p = parentInner[i];
+    for (int guard = 0; p >= 0 && guard < 4096; ++guard) {
+        if (collapse[p] && p != 0) k = 0;
+        ++depth;
+        p = parentInner[p];
+    }
+    kept[i] = k;
+    if (k) atomicMax(maxDepth, depth);
+}
+
+__device__ __forceinline__ uint32_t leafRef(int first, int count) {
+    return kLeafFlag | ((uint32_t)(count - 1) << kLeafCountShift) | (uint32_t)first;
+}
+
+__global__ void k_emit(const float4* tri, const int* order, int n, const int2* range, const int2* child, const int* collapse, const int* kept,
+                       const int* newIdx, const float* boxes, float4* nodes) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n - 1 || !kept[i]) return;
+    int2 c = child[i];
+    float4* out = nodes + 4 * (size_t)newIdx[i];
+    float4 o0, o1, o2, o3;
+    uint32_t refs[2];
+    float b[2][6];
+    for (int s = 0; s < 2; ++s) {
+        int ch = s == 0 ? c.x : c.y;
+        if (ch < 0) {
+            int t = order[~ch];
+            float4 a = tri[3 * (size_t)t], bb = tri[3 * (size_t)t + 1], d = tri[3 * (size_t)t + 2];
+            b[s][0] = fminf(a.x, fminf(bb.x, d.x)); b[s][3] = fmaxf(a.x, fmaxf(bb.x, d.x));
+            b[s][1] = fminf(a.y, fminf(bb.y, d.y)); b[s][4] = fmaxf(a.y, fmaxf(bb.y, d.y));
+            b[s][2] = fminf(a.z, fminf(bb.z, d.z)); b[s][5] = fmaxf(a.z, fmaxf(bb.z, d.z));
+            refs[s] = leafRef(~ch, 1);
+        } else {
+            for (int k = 0; k < 6; ++k) b[s][k] = boxes[6 * (size_t)ch + k];
+            if (collapse[ch]) {
+                int2 r = range[ch];
+                refs[s] = leafRef(r.x, r.y - r.x + 1);
+            } else {
+                refs[s] = (uint32_t)newIdx[ch];
+            }
+        }
+    }
+    o0 = make_float4(b[0][0], b[0][3], b[0][1], b[0][4]);
+    o1 = make_float4(b[1][0], b[1][3], b[1][1], b[1][4]);
+    o2 = make_float4(b[0][2], b[0][5], b[1][2], b[1][5]);
+    o3 = make_float4(__uint_as_float(refs[0]), __uint_as_float(refs[1]), 0.0f, 0.0f);
+    out[0] = o0; out[1] = o1; out[2] = o2; out[3] = o3;
+}
+
+// Single-triangle scene: root with the same one-triangle leaf in both slots.
+__global__ void k_emit_single(const float4* tri, float4* nodes) {
+    float4 a = tri[0], b = tri[1], c = tri[2];
+    float lo[3] = {fminf(a.x, fminf(b.x, c.x)), fminf(a.y, fminf(b.y, c.y)), fminf(a.z, fminf(b.z, c.z))};
+    float hi[3] = {fmaxf(a.x, fmaxf(b.x, c.x)), fmaxf(a.y, fmaxf(b.y, c.y)), fmaxf(a.z, fmaxf(b.z, c.z))};
+    uint32_t r = leafRef(0, 1);
+    nodes[0] = make_float4(lo[0], hi[0], lo[1], hi[1]);
+    nodes[1] = make_float4(lo[0], hi[0], lo[1], hi[1]);
+    nodes[2] = make_float4(lo[2], hi[2], lo[2], hi[2]);
+    nodes[3] = make_float4(__uint_as_float(r), __uint_as_float(r), 0.0f, 0.0f);
+}
+
+template <class T> T* carve(char*& p, size_t n) {
+    size_t off = (reinterpret_cast<size_t>(p) + 255) & ~size_t(255);
+    T* r = reinterpret_cast<T*>(off);
+    p = reinterpret_cast<char*>(off + n * sizeof(T));
+    return r;
+}
+
+}  // namespace
+
+size_t lbvhScratchBytes(int n) {
+    size_t tmp = 0;
+    cub::DeviceRadixSort::SortPairs(nullptr, tmp, (unsigned long long*)nullptr, (unsigned long long*)nullptr, (int*)nullptr, (int*)nullptr, n);
+    size_t s = 0;
+    s += 2 * sizeof(unsigned long long) * n + 2 * sizeof(int) * n;  // keys, values (double buffer)
+    s += sizeof(int2) * n * 2;                                       // range, child
+    s += sizeof(int) * n * 2;                                        // parents
+    s += sizeof(int) * n * 4;                                        // visits, collapse, kept, newIdx
+    s += sizeof(float) * n * 7;                                      // boxes, cost
+    s += tmp + 64 * 256 + 64;
+    return s;
+}
+
+int buildLbvh(const float4* tri, int n, float4* nodesOut, int* orderOut, void* scratch, size_t scratchBytes, int* hostNodeCount, int* hostMaxDepth,
+              cudaStream_t st) {
+    if (n <= 0) { *hostNodeCount = 0; *hostMaxDepth = 0; return 0; }
+    if (n == 1) {
+        k_emit_single<<<1, 1, 0, st>>>(tri, nodesOut);
+        int zero = 0;
+        cudaMemcpyAsync(orderOut, &zero, sizeof(int), cudaMemcpyHostToDevice, st);
+        *hostNodeCount = 1;
+        *hostMaxDepth = 0;
+        return cudaStreamSynchronize(st) == cudaSuccess ? 0 : -1;
+    }
+    char* p = static_cast<char*>(scratch);
+    unsigned long long* keysA = carve<unsigned long long>(p, n);
+    unsigned long long* keysB = carve<unsigned long long>(p, n);
+    int* valsA = carve<int>(p, n);
+    int* valsB = carve<int>(p, n);
+    int2* range = carve<int2>(p, n);
+    int2* child = carve<int2>(p, n);
+    int* parentInner = carve<int>(p, n);
+    int* parentLeaf = carve<int>(p, n);
+    int* visits = carve<int>(p, n);
+    int* collapse = carve<int>(p, n);
+    int* kept = carve<int>(p, n);
+    int* newIdx = carve<int>(p, n);
+    float* boxes = carve<float>(p, 6 * size_t(n));
+    float* cost = carve<float>(p, n);
+    int* small = carve<int>(p, 16);  // 0..5 centroid bounds, 6 max depth, 7 kept total
+    size_t tmpBytes = 0;
+    cub::DeviceRadixSort::SortPairs(nullptr, tmpBytes, keysA, keysB, valsA, valsB, n, 0, 63, st);
+    void* tmp = carve<char>(p, tmpBytes);
+    if (size_t(p - static_cast<char*>(scratch)) > scratchBytes) return -2;
+
+    int init[8] = {0x7FFFFFFF, 0x7FFFFFFF, 0x7FFFFFFF, (int)0x80000000, (int)0x80000000, (int)0x80000000, 0, 0};
+    cudaMemcpyAsync(small, init, sizeof(init), cudaMemcpyHostToDevice, st);
+    int grid = (n + 255) / 256;
+    k_centroid_bounds<<<std::min(grid, 1024), 256, 0, st>>>(tri, n, small);
+    k_morton<<<grid, 256, 0, st>>>(tri, n, small, keysA, valsA);
+    cub::DeviceRadixSort::SortPairs(tmp, tmpBytes, keysA, keysB, valsA, valsB, n, 0, 63, st);
+    cudaMemsetAsync(parentInner, 0xFF, sizeof(int) * n, st);
+    cudaMemsetAsync(visits, 0, sizeof(int) * n, st);
+    k_karras<<<grid, 256, 0, st>>>(keysB, n, range, child, parentInner, parentLeaf);
+    k_refit<<<grid, 256, 0, st>>>(tri, valsB, n, range, child, parentInner, parentLeaf, visits, boxes, cost, collapse);
+    k_kept<<<grid, 256, 0, st>>>(parentInner, collapse, n, kept, small + 6);
+    size_t scanBytes = 0;
+    cub::DeviceScan::ExclusiveSum(nullptr, scanBytes, kept, newIdx, n - 1, st);
+    if (scanBytes > tmpBytes) return -2;
+    cub::DeviceScan::ExclusiveSum(tmp, scanBytes, kept, newIdx, n - 1, st);
+    int hs[2];
+    cudaMemcpyAsync(&hs[0], newIdx + (n - 2), sizeof(int), cudaMemcpyDeviceToHost, st);
+    cudaMemcpyAsync(&hs[1], kept + (n - 2), sizeof(int), cudaMemcpyDeviceToHost, st);
+    int md = 0;
+    cudaMemcpyAsync(&md, small + 6, sizeof(int), cudaMemcpyDeviceToHost, st);
+    if (cudaStreamSynchronize(st) != cudaSuccess) return -1;
+    *hostNodeCount = hs[0] + hs[1];
+    *hostMaxDepth = md;
+    k_emit<<<grid, 256, 0, st>>>(tri, valsB, n, range, child, collapse, kept, newIdx, boxes, nodesOut);
+    cudaMemcpyAsync(orderOut, valsB, sizeof(int) * n, cudaMemcpyDeviceToDevice, st);
+    return cudaStreamSynchronize(st) == cudaSuccess ? 0 : -1;
+}
+
+}  // namespace sst
+
+namespace sst {
+namespace {
+__global__ void k_leaf_gather(const int* order, int n, const float4* trivG, const float4* triNG, const int4* auxG, const int4* vtxG, float4* triv,
+                              float4* triN, int4* aux, int4* vtx) {
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    int g = order[t];
+    float4 a = trivG[3 * (size_t)g];
+    a.w = __int_as_float(g);
+    triv[3 * (size_t)t] = a;
+    triv[3 * (size_t)t + 1] = trivG[3 * (size_t)g + 1];
+    triv[3 * (size_t)t + 2] = trivG[3 * (size_t)g + 2];
+    triN[t] = triNG[g];
+    aux[t] = auxG[g];
+    vtx[t] = vtxG[g];
+}
+}  // namespace
+
+void launch_leaf_gather(const int* order, int n, const float4* trivG, const float4* triNG, const int4* auxG, const int4* vtxG, float4* triv,
+                        float4* triN, int4* aux, int4* vtx, cudaStream_t st) {
+    if (n <= 0) return;
+    k_leaf_gather<<<(n + 255) / 256, 256, 0, st>>>(order, n, trivG, triNG, auxG, vtxG, triv, triN, aux, vtx);
+}
+}  // namespace sst

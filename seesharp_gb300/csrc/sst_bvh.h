@@ -1,0 +1,24 @@
+// GPU linear-BVH builder (sst_bvh.cu).
+#pragma once
+#include <cuda_runtime.h>
+
+#include "sst_types.h"
+
+namespace sst {
+
+// Scratch bytes buildLbvh needs for n triangles.
+size_t lbvhScratchBytes(int n);
+
+// Builds the traversal BVH over n triangles (3 float4 per triangle, global order).  Writes at most
+// n - 1 nodes (4 float4 each) to nodesOut and the leaf order (sorted position -> global triangle)
+// to orderOut.  Returns 0 on success; the node count and the maximum inner-node depth are
+// returned through the host pointers.
+int buildLbvh(const float4* tri, int n, float4* nodesOut, int* orderOut, void* scratch, size_t scratchBytes, int* hostNodeCount, int* hostMaxDepth,
+              cudaStream_t st);
+
+// Gathers per-triangle records into leaf order: out[t] = in[order[t]] (triv also stamps the
+// global id into v0.w).
+void launch_leaf_gather(const int* order, int n, const float4* trivG, const float4* triNG, const int4* auxG, const int4* vtxG, float4* triv,
+                        float4* triN, int4* aux, int4* vtx, cudaStream_t st);
+
+}  // namespace sst
