@@ -472,7 +472,7 @@ static void commitScene(sst_scene* s, int W, int H) {
         scratch.ensure(sb);
         int nodeCount = 0, maxDepth = 0;
         int rc = buildLbvh(gTriv.as<float4>(), nt, s->nodes.as<float4>(), order.as<int>(), scratch.p, sb, &nodeCount, &maxDepth, st);
-        if (rc != 0) fail(SST_ERR_CUDA, "GPU BVH build failed: " + std::string(cudaGetErrorString(cudaGetLastError())));
+        if (rc != 0) fail(SST_ERR_CUDA, "GPU BVH build failed (" + std::to_string(rc) + "): " + cudaGetErrorString(cudaGetLastError()));
         if (maxDepth + 2 >= kMaxStack) {
             hostBuild = true;  // deeper than the traversal stack: use the host SAH build instead
         } else {

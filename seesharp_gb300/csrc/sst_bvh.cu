@@ -249,9 +249,17 @@ template <class T> T* carve(char*& p, size_t n) {
 
 }  // namespace
 
+// CUB temporary storage shared by the radix sort and the prefix sum.
+static size_t cubTempBytes(int n) {
+    size_t sortBytes = 0, scanBytes = 0;
+    cub::DeviceRadixSort::SortPairs(nullptr, sortBytes, (unsigned long long*)nullptr, (unsigned long long*)nullptr, (int*)nullptr, (int*)nullptr, n,
+                                    0, 63);
+    cub::DeviceScan::ExclusiveSum(nullptr, scanBytes, (int*)nullptr, (int*)nullptr, n > 1 ? n - 1 : 1);
+    return std::max(sortBytes, scanBytes);
+}
+
 size_t lbvhScratchBytes(int n) {
-    size_t tmp = 0;
-    cub::DeviceRadixSort::SortPairs(nullptr, tmp, (unsigned long long*)nullptr, (unsigned long long*)nullptr, (int*)nullptr, (int*)nullptr, n);
+    size_t tmp = cubTempBytes(n);
     size_t s = 0;
     s += 2 * sizeof(unsigned long long) * n + 2 * sizeof(int) * n;  // keys, values (double buffer)
     s += sizeof(int2) * n * 2;                                       // range, child
@@ -289,8 +297,7 @@ int buildLbvh(const float4* tri, int n, float4* nodesOut, int* orderOut, void* s
     float* boxes = carve<float>(p, 6 * size_t(n));
     float* cost = carve<float>(p, n);
     int* small = carve<int>(p, 16);  // 0..5 centroid bounds, 6 max depth, 7 kept total
-    size_t tmpBytes = 0;
-    cub::DeviceRadixSort::SortPairs(nullptr, tmpBytes, keysA, keysB, valsA, valsB, n, 0, 63, st);
+    size_t tmpBytes = cubTempBytes(n);
     void* tmp = carve<char>(p, tmpBytes);
     if (size_t(p - static_cast<char*>(scratch)) > scratchBytes) return -2;
 

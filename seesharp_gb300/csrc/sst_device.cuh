@@ -11,6 +11,13 @@ namespace sst {
 
 #define SST_D __device__ __forceinline__
 #define SST_HD __host__ __device__ __forceinline__
+// Large shading functions called from several places are compiled once (SST_DN) to keep the
+// instruction footprint of the shade kernel small.
+#ifdef SST_NOINLINE_MORE
+#define SST_DN __device__ __noinline__
+#else
+#define SST_DN __device__ __forceinline__
+#endif
 
 constexpr float kPi = 3.14159265f;  // MathF.PI
 
@@ -279,7 +286,7 @@ struct Lp {
     float rough, ax, ay;
     float metallic, specTransW, ior;
 };
-SST_D Lp localParams(const DevScene& sc, const DevMaterial& m, float2 uv) {
+SST_DN Lp localParams(const DevScene& sc, const DevMaterial& m, float2 uv) {
     Lp r;
     float3 base = lookupRgb(sc, m.baseTex, m.base, uv);
     float lum = luminance(base);
@@ -305,7 +312,14 @@ SST_D bool shouldReflect(float3 faceN, float3 outW, float3 inW) { return dot(out
 
 // GenericMaterial.ComputeValueAndPdf (GenericMaterial.cs:152-338); returns the BSDF value and the
 // forward pdf (the reverse pdf is not needed by the path tracer).
-SST_D float3 genericEval(const Ctx& c, const Lp& lp, float3 in, float& pdf) {
+// Compiled once and called (not inlined) by default: the shade kernel evaluates it for three
+// directions per bounce, and one copy of the code keeps the instruction cache warm.
+#ifndef SST_EVAL_INLINE
+__device__ __noinline__
+#else
+SST_D
+#endif
+float3 genericEval(const Ctx& c, const Lp& lp, float3 in, float& pdf) {
     Ggx ndf{lp.ax, lp.ay};
     const float3 o = c.out;
     float cO = fabsf(o.z), cI = fabsf(in.z);
@@ -370,7 +384,7 @@ SST_D float3 genericEval(const Ctx& c, const Lp& lp, float3 in, float& pdf) {
 }
 
 // DiffuseMaterial.Evaluate + Pdf (DiffuseMaterial.cs:109-122, 167-188) for a world direction.
-SST_D float3 diffuseEval(const Ctx& c, float3 base, bool transmitter, float3 inW, float& pdf) {
+SST_DN float3 diffuseEval(const Ctx& c, float3 base, bool transmitter, float3 inW, float& pdf) {
     bool refl = shouldReflect(c.faceN, c.outW, inW);
     float3 in = c.f.toLocal(inW);
     bool sh = sameHemi(c.out, in);
@@ -402,7 +416,7 @@ SST_D float3 evalWithCos(const DevScene& sc, const DevMaterial& m, const Lp& lp,
 
 // Material.Sample: GenericMaterial.cs:92-150 / DiffuseMaterial.cs:127-164.  Returns false for an
 // invalid sample (pdf 0).
-SST_D bool sampleMaterial(const DevScene& sc, const DevMaterial& m, const Lp& lp, float3 diffBase, const Ctx& c, float u, float u1, float u2,
+SST_DN bool sampleMaterial(const DevScene& sc, const DevMaterial& m, const Lp& lp, float3 diffBase, const Ctx& c, float u, float u1, float u2,
                           float3& dirW, float& pdf, float3& weight) {
     if (m.type == kGeneric) {
         if (c.out.z == 0.0f) return false;
@@ -492,7 +506,7 @@ SST_D float envPdf(const DevEnv& e, float3 d) {  // :81-85
     return gridPdf(e, px, py) / (sinf(sp.y) * kPi * kPi * 2.0f);
 }
 // :40-73
-SST_D void envSample(const DevEnv& e, float u1, float u2, float3& dir, float& pdf, float3& weight) {
+SST_DN void envSample(const DevEnv& e, float u1, float u2, float3& dir, float& pdf, float3& weight) {
     int row = lowerBound(e.rowCdf, e.h, u2);
     float lo = row == 0 ? 0.0f : __ldg(&e.rowCdf[row - 1]);
     float relRow = (u2 - lo) / (__ldg(&e.rowCdf[row]) - lo);

@@ -13,6 +13,11 @@
 
 namespace cg = cooperative_groups;
 
+// Minimum resident blocks per SM requested for the shade kernel (register budget).
+#ifndef SST_SHADE_MIN_BLOCKS
+#define SST_SHADE_MIN_BLOCKS 1
+#endif
+
 namespace sst {
 
 // =============================================================================================
@@ -310,7 +315,7 @@ SST_D int aggAppend(int* counter) {
 }
 
 template <int NS>
-__global__ void __launch_bounds__(128) k_shade(DevScene sc, PTConfig cfg, PathBuf A, PathBuf B, const float4* __restrict__ hits, float4* nee,
+__global__ void __launch_bounds__(128, SST_SHADE_MIN_BLOCKS) k_shade(DevScene sc, PTConfig cfg, PathBuf A, PathBuf B, const float4* __restrict__ hits, float4* nee,
                                                int cap, float4* shRo, float4* shRd, int* shTgt, const int* nIn, int* nOut, int* nSh,
                                                float* film, DevStats* stats) {
     const int n = *nIn;
