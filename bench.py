@@ -30,7 +30,74 @@ sys.path.insert(0, ROOT)
 CONFIGS = {
     0: dict(name="cornell_box_36tri_256x256_16spp_depth5", builder="cornell", W=256, H=256, spp=16, depth=5),
     1: dict(name="sphere_field_1Mtri_1024x1024_64spp_depth8", builder="spheres", spheres=200, W=1024, H=1024, spp=64, depth=8),
+    2: dict(name="batch_64jobs_10k-1Mtri_128-1024px_4-64spp_depth3-10", builder="batch", jobs=64, seed=2024),
 }
+
+
+def batch_jobs(cfg, seed_offset=0):
+    """The batched configuration: 64 jobs from the sphere-field generator with triangle counts
+    log-uniform in [10k, 1M], resolutions from {128, 256, 512, 1024} squared, spp U{4..64},
+    max depth U{3..10}."""
+    from seesharp_gb300 import PathTracer, workloads
+    rng = np.random.default_rng(cfg["seed"] + seed_offset)
+    out = []
+    for j in range(cfg["jobs"]):
+        tris = math.exp(rng.uniform(math.log(1e4), math.log(1e6)))
+        res = int(rng.choice([128, 256, 512, 1024]))
+        spp = int(rng.integers(4, 65))
+        depth = int(rng.integers(3, 11))
+        sc = workloads.sphere_field(max(2, int(round(tris / 5120))), res, res, seed=1000 + j)
+        out.append((sc, PathTracer(TotalSpp=spp, MaxDepth=depth)))
+    return out
+
+
+def run_batch(args, cfg):
+    """Batched jobs in one shared wavefront vs the same jobs rendered one after another."""
+    import torch
+    from seesharp_gb300 import render_batch
+    pairs = batch_jobs(cfg)
+    for sc, _ in pairs:
+        sc.Prepare()
+    samples = sum(sc.FrameBuffer.Width * sc.FrameBuffer.Height * pt.TotalSpp for sc, pt in pairs)
+    tris = [sum(m.NumFaces for m in sc.Meshes) for sc, _ in pairs]
+
+    def batched():
+        for sc, _ in pairs:
+            sc.FrameBuffer.Reset()
+        return render_batch(pairs).renderTimeMs
+
+    def sequential():
+        ms = 0.0
+        for sc, pt in pairs:
+            sc.FrameBuffer.Reset()
+            pt.Render(sc)
+            ms += pt.last_stats.renderTimeMs
+        return ms
+
+    for _ in range(args.warmup):
+        batched()
+        sequential()
+    with ClockSampler(0) as clk:
+        tb = [batched() for _ in range(args.steps)]
+        ts = [sequential() for _ in range(args.steps)]
+    vb = samples / (np.mean(tb) / 1000) / 1e6
+    vs = samples / (np.mean(ts) / 1000) / 1e6
+    # e2e: wall clock through the public API with host films
+    t0 = time.perf_counter()
+    batched()
+    e2e_b = samples / (time.perf_counter() - t0) / 1e6
+    line = {"metric": "Msamples/s PathTracer (batched jobs)", "value": round(vb, 3), "unit": "Msamples/s", "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(float(np.mean(tb)), 3), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic (seeded scene generator)",
+            "config": {"workload": cfg["name"], "jobs": len(pairs), "total_samples": int(samples), "triangles_min": min(tris), "triangles_max": max(tris),
+                       "triangles_total": int(sum(tris))},
+            "sequential": {"value": round(vs, 3), "ms_per_step": round(float(np.mean(ts)), 3)},
+            "batched_over_sequential": round(vb / vs, 3),
+            "e2e": {"value": round(e2e_b, 3), "unit": "Msamples/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": int(sum(sc.FrameBuffer.Image.data.nbytes for sc, _ in pairs))},
+            "clocks": clk.summary()}
+    print(json.dumps(line), flush=True)
+
 
 
 def make_scene(cfg):
@@ -347,6 +414,8 @@ def main():
     os.environ.setdefault("SST_BVH", "lbvh")
     if args.impl == "reference":
         run_reference(args, cfg)
+    elif cfg["builder"] == "batch":
+        run_batch(args, cfg)
     else:
         run_ours(args, cfg)
 

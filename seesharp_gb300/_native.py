@@ -320,6 +320,19 @@ class SceneHandle:
         return stats
 
 
+def render_batch(ctx, jobs):
+    """jobs: list of (SceneHandle, SstPathTracerParams, film_ptr, memory).  One shared wavefront."""
+    arr = (SstRenderJob * len(jobs))()
+    for k, (sh, params, film, mem) in enumerate(jobs):
+        arr[k].scene = sh.handle
+        arr[k].params = params
+        arr[k].film = film
+        arr[k].memory = mem
+    stats = SstRenderStats()
+    check(ctx.lib.sst_render_batch(ctx.handle, arr, len(jobs), ctypes.byref(stats)))
+    return stats
+
+
 def make_params(width, height, totalSpp, maxDepth, minDepth=1, baseSeed=0xC030114, numShadowRays=1, enableBsdfDI=True,
                 ignoreNanAndInf=True, firstIteration=0, maximumRenderTimeMs=0):
     p = SstPathTracerParams()

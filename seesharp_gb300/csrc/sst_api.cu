@@ -96,8 +96,9 @@ struct sst_ctx {
     cudaStream_t stream = nullptr;
     int numSMs = 0;
     // wavefront buffers
-    DevBuf pathA[8], pathB[8];
-    DevBuf hits, nee, shRo, shRd, shTgt, counters, samples, stats, film;
+    DevBuf pathA[9], pathB[9];
+    DevBuf hits, nee, shRo, shRd, shTgt, shJob, counters, samples, stats, film;
+    DevBuf jobsBuf, chunksBuf, wavesBuf, curWave;
     int cap = 0, shCap = 0, neeSlots = 0;
     size_t sampleCap = 0;
     DevBuf scratchIn, scratchOut, scratchOut2;
@@ -175,7 +176,7 @@ struct sst_scene {
     bool committed = false;
     int W = 0, H = 0;
     // device
-    DevBuf nodes, triv, triN, triAux, triVtx, vnrm, vuv, mats, texs, texData, ems, envImg, envRowCdf, envColCdf, envHasCol, envRowMarg;
+    DevBuf nodes, triv, triN, triAux, triVtx, vnrm, vuv, mats, texs, texData, ems, envImg, envRowCdf, envColCdf, envHasCol, envRowMarg, queryJob;
     DevScene dev{};
     int nTri = 0, nNodes = 0, bvhDepth = 0;
     std::vector<int> meshTriOffset;
@@ -624,16 +625,17 @@ static void commitScene(sst_scene* s, int W, int H) {
 // ---------------------------------------------------------------------------------------------
 static void bindPath(DevBuf* bufs, PathBuf& p, int cap) {
     size_t c = size_t(cap);
-    bufs[0].ensure(c * 4); bufs[1].ensure(c * 4); bufs[2].ensure(c * 4);
-    for (int k = 3; k < 8; ++k) bufs[k].ensure(c * 16);
-    p.pix = bufs[0].as<uint32_t>();
-    p.rng = bufs[1].as<uint32_t>();
-    p.depth = bufs[2].as<uint32_t>();
-    p.pw = bufs[3].as<float4>();
-    p.rad = bufs[4].as<float4>();
-    p.prev = bufs[5].as<float4>();
-    p.ro = bufs[6].as<float4>();
-    p.rd = bufs[7].as<float4>();
+    for (int k = 0; k < 4; ++k) bufs[k].ensure(c * 4);
+    for (int k = 4; k < 9; ++k) bufs[k].ensure(c * 16);
+    p.job = bufs[0].as<uint32_t>();
+    p.pix = bufs[1].as<uint32_t>();
+    p.rng = bufs[2].as<uint32_t>();
+    p.depth = bufs[3].as<uint32_t>();
+    p.pw = bufs[4].as<float4>();
+    p.rad = bufs[5].as<float4>();
+    p.prev = bufs[6].as<float4>();
+    p.ro = bufs[7].as<float4>();
+    p.rd = bufs[8].as<float4>();
 }
 
 static int defaultWaveCapacity() {
@@ -660,6 +662,7 @@ static void ensureWave(sst_ctx* c, int cap, int ns, Wave& w) {
     c->shRo.ensure(shCap * 16);
     c->shRd.ensure(shCap * 16);
     c->shTgt.ensure(shCap * 4);
+    c->shJob.ensure(shCap * 4);
     c->counters.ensure(sizeof(int) * kNumCounters);
     c->stats.ensure(sizeof(DevStats));
     w.wb.hits = c->hits.as<float4>();
@@ -667,6 +670,7 @@ static void ensureWave(sst_ctx* c, int cap, int ns, Wave& w) {
     w.wb.shRo = c->shRo.as<float4>();
     w.wb.shRd = c->shRd.as<float4>();
     w.wb.shTgt = c->shTgt.as<int>();
+    w.wb.shJob = c->shJob.as<uint32_t>();
     w.wb.counters = c->counters.as<int>();
     w.wb.cap = c->cap;
     w.wb.shCap = int(shCap);
@@ -683,91 +687,194 @@ static void checkParams(const sst_scene* s, const SstPathTracerParams* p) {
     if (p->maxDepth > kMaxPathDepth) fail(SST_ERR_UNSUPPORTED, "MaxDepth above 1000 is not supported");
 }
 
-// Renders iterations [iterFirst, iterEnd) of one scene into the device film.
-static void renderDevice(sst_scene* s, const SstPathTracerParams* P, float* dFilm, int iterFirst, int iterEnd, SstRenderStats* out) {
-    sst_ctx* c = s->ctx;
+struct JobIn {
+    sst_scene* s;
+    SstPathTracerParams p;
+    float* dFilm;
+    int iterFirst, iterEnd;
+    int done = 0;  // iterations rendered
+};
+
+// Splits the (job, iteration, pixel) paths into waves of at most `cap` paths.  A job whose
+// image fits a wave contributes chunks of whole iterations; a larger image is cut into pixel
+// ranges of one iteration.  A pixel appears at most once per wave.
+static void planWaves(std::vector<JobIn>& jobs, int cap, bool iterationPerWave, std::vector<WaveChunk>& chunks, std::vector<WaveDesc>& waves,
+                      std::vector<std::vector<int>>& waveIterEnds) {
+    WaveDesc cur{0, 0, 0, 0};
+    auto closeWave = [&]() {
+        if (cur.items == 0) return;
+        cur.chunkEnd = int(chunks.size());
+        waves.push_back(cur);
+        cur = WaveDesc{int(chunks.size()), int(chunks.size()), 0, 0};
+    };
+    for (size_t j = 0; j < jobs.size(); ++j) {
+        const JobIn& jb = jobs[j];
+        int P = jb.p.width * jb.p.height;
+        int it = jb.iterFirst;
+        int pixCursor = 0;
+        while (it < jb.iterEnd) {
+            int space = cap - cur.items;
+            WaveChunk ck{};
+            ck.job = int(j);
+            ck.film = jb.dFilm;
+            ck.itemOffset = cur.items;
+            ck.foldOffset = cur.foldThreads;
+            if (P <= cap) {
+                int k = std::min(jb.iterEnd - it, space / P);
+                if (iterationPerWave) k = std::min(k, 1);
+                if (k == 0) { closeWave(); continue; }
+                ck.iterBase = it; ck.nIter = k; ck.pixStart = 0; ck.pixCount = P;
+                it += k;
+            } else {
+                int cnt = std::min(space, P - pixCursor);
+                if (cnt == 0) { closeWave(); continue; }
+                ck.iterBase = it; ck.nIter = 1; ck.pixStart = pixCursor; ck.pixCount = cnt;
+                pixCursor += cnt;
+                if (pixCursor == P) { pixCursor = 0; ++it; }
+            }
+            chunks.push_back(ck);
+            cur.items += ck.nIter * ck.pixCount;
+            cur.foldThreads += ck.pixCount;
+            if (iterationPerWave || cur.items == cap) closeWave();
+        }
+    }
+    closeWave();
+    (void)waveIterEnds;
+}
+
+// Renders the jobs' iterations [iterFirst, iterEnd) into their device films.
+static void renderJobs(sst_ctx* c, std::vector<JobIn>& jobs, SstRenderStats* out) {
     cudaStream_t st = c->stream;
-    const int pixels = P->width * P->height;
-    const int ns = std::max(1, P->numShadowRays);
-    int cap = std::min(defaultWaveCapacity(), std::max(pixels, 1));
-    // several whole iterations per wave when the image is small
-    int itersPerWave = std::max(1, cap / pixels);
-    int pixPerWave = std::min(pixels, cap);
-    cap = std::max(pixPerWave * itersPerWave, 1);
+    if (jobs.empty()) return;
+    long long totalItems = 0;
+    int ns = 1, maxDepth = 1;
+    bool timeLimit = false;
+    for (auto& j : jobs) {
+        totalItems += (long long)j.p.width * j.p.height * std::max(0, j.iterEnd - j.iterFirst);
+        ns = std::max(ns, j.p.numShadowRays);
+        maxDepth = std::max(maxDepth, j.p.maxDepth);
+        timeLimit |= j.p.maximumRenderTimeMs > 0;
+    }
+    if (totalItems == 0) return;
+    if (timeLimit && jobs.size() > 1) fail(SST_ERR_UNSUPPORTED, "MaximumRenderTimeMs is supported for single renders only");
+    int cap = int(std::min<long long>(defaultWaveCapacity(), totalItems));
+    for (auto& j : jobs) cap = std::max(cap, 1);
     Wave w;
     ensureWave(c, cap, ns, w);
-    size_t sampleBytes = size_t(cap) * 12;
-    c->samples.ensure(sampleBytes);
-    PTConfig cfg{P->width, P->height, P->maxDepth, P->minDepth, P->baseSeed, P->numShadowRays, P->enableBsdfDI, P->ignoreNanAndInf};
+    c->samples.ensure(size_t(w.wb.cap) * 12);
+    // job table
+    std::vector<DevJob> hj(jobs.size());
+    for (size_t k = 0; k < jobs.size(); ++k) {
+        const SstPathTracerParams* P = &jobs[k].p;
+        hj[k].sc = jobs[k].s->dev;
+        hj[k].cfg = PTConfig{P->width, P->height, P->maxDepth, P->minDepth, P->baseSeed, P->numShadowRays, P->enableBsdfDI, P->ignoreNanAndInf};
+    }
+    std::vector<WaveChunk> chunks;
+    std::vector<WaveDesc> waves;
+    std::vector<std::vector<int>> iterEnds;
+    planWaves(jobs, w.wb.cap, timeLimit, chunks, waves, iterEnds);
+    c->jobsBuf.upload(hj, st);
+    c->chunksBuf.upload(chunks, st);
+    c->wavesBuf.upload(waves, st);
+    c->curWave.ensure(sizeof(int) * 2);
+    CUDA_CHECK(cudaMemsetAsync(c->curWave.p, 0, sizeof(int) * 2, st));
+    const DevJob* dj = c->jobsBuf.as<DevJob>();
+    const WaveChunk* dch = c->chunksBuf.as<WaveChunk>();
+    const WaveDesc* dwv = c->wavesBuf.as<WaveDesc>();
+    int* dcur = c->curWave.as<int>();
     DevStats* dstats = c->stats.as<DevStats>();
     CUDA_CHECK(cudaMemsetAsync(dstats, 0, sizeof(DevStats), st));
-    CUDA_CHECK(cudaEventRecord(c->ev0, st));
-    int iterations = 0;
-    auto t0 = std::chrono::steady_clock::now();
-    for (int it = iterFirst; it < iterEnd;) {
-        if (P->maximumRenderTimeMs > 0 && it > iterFirst) {
-            CUDA_CHECK(cudaStreamSynchronize(st));
-            double ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
-            double per = ms / std::max(1, iterations);
-            if (ms + per > double(P->maximumRenderTimeMs)) break;  // PathTracer.cs:221-227
+    int* cnt = w.wb.counters;
+    int maxFold = 0;
+    for (auto& wd : waves) maxFold = std::max(maxFold, wd.foldThreads);
+
+    // One wave: camera, then per bounce closest hit / shade / shadow rays, then the film fold.
+    auto issueWave = [&](int items, bool allowEarlyExit) {
+        CUDA_CHECK(cudaMemsetAsync(cnt, 0, sizeof(int) * kNumCounters, st));
+        {
+            KTimer kt(c, 0);
+            launch_camera(dj, dch, dwv, dcur, w.wb.a, cnt + kCntQueue + 1, items, st);
         }
-        int nIt = std::min(itersPerWave, iterEnd - it);
-        for (int p0 = 0; p0 < pixels; p0 += pixPerWave) {
-            int pc = std::min(pixPerWave, pixels - p0);
-            int n = pc * nIt;
-            int* cnt = w.wb.counters;
-            CUDA_CHECK(cudaMemsetAsync(cnt, 0, sizeof(int) * kNumCounters, st));
+        PathBuf A = w.wb.a, B = w.wb.b;
+        int maxItems = items;
+        for (int d = 1; d <= maxDepth; ++d) {
             {
-                KTimer kt(c, 0);
-                launch_camera(s->dev, cfg, w.wb.a, p0, pc, n, uint32_t(it), cnt + kCntQueue + 1, st);
-            }
-            PathBuf A = w.wb.a, B = w.wb.b;
-            int maxItems = n;
-            for (int d = 1; d <= P->maxDepth; ++d) {
-                {
-                    KTimer kt(c, 1);
-                    launch_trace_closest(s->dev, A.ro, A.rd, cnt + kCntQueue + d, cnt + kCntWork + 2 * d, w.wb.hits, dstats, st);
-                }
-                {
-                    KTimer kt(c, 2);
-                    launch_shade(ns, s->dev, cfg, A, B, w.wb.hits, w.wb.nee, w.wb.cap, w.wb.shRo, w.wb.shRd, w.wb.shTgt, cnt + kCntQueue + d,
-                                 cnt + kCntQueue + d + 1, cnt + kCntShadow + d, c->samples.as<float>(), dstats, maxItems, st);
-                }
-                {
-                    KTimer kt(c, 3);
-                    launch_trace_shadow(s->dev, w.wb.shRo, w.wb.shRd, w.wb.shTgt, cnt + kCntShadow + d, cnt + kCntWork + 2 * d + 1, w.wb.nee,
-                                        dstats, st);
-                }
-                std::swap(A, B);
-                if (d >= 6 && d < P->maxDepth) {
-                    // stop early once the queue is empty (long MaxDepth with Russian roulette)
-                    CUDA_CHECK(cudaMemcpyAsync(c->pinnedCount, cnt + kCntQueue + d + 1, sizeof(int), cudaMemcpyDeviceToHost, st));
-                    CUDA_CHECK(cudaStreamSynchronize(st));
-                    if (*c->pinnedCount == 0) break;
-                    maxItems = *c->pinnedCount;
-                }
+                KTimer kt(c, 1);
+                launch_trace_closest(dj, A.job, A.ro, A.rd, cnt + kCntQueue + d, cnt + kCntWork + 2 * d, w.wb.hits, dstats, st);
             }
             {
-                KTimer kt(c, 4);
-                launch_film_fold(cfg, c->samples.as<float>(), p0, pc, nIt, uint32_t(it), dFilm, dstats, st);
+                KTimer kt(c, 2);
+                launch_shade(ns, dj, A, B, w.wb.hits, w.wb.nee, w.wb.cap, w.wb.shRo, w.wb.shRd, w.wb.shTgt, w.wb.shJob, cnt + kCntQueue + d,
+                             cnt + kCntQueue + d + 1, cnt + kCntShadow + d, c->samples.as<float>(), dstats, maxItems, st);
             }
+            {
+                KTimer kt(c, 3);
+                launch_trace_shadow(dj, w.wb.shJob, w.wb.shRo, w.wb.shRd, w.wb.shTgt, cnt + kCntShadow + d, cnt + kCntWork + 2 * d + 1, w.wb.nee,
+                                    dstats, st);
+            }
+            std::swap(A, B);
+            if (allowEarlyExit && d >= 6 && d < maxDepth) {
+                // stop early once the queue is empty (long MaxDepth with Russian roulette)
+                CUDA_CHECK(cudaMemcpyAsync(c->pinnedCount, cnt + kCntQueue + d + 1, sizeof(int), cudaMemcpyDeviceToHost, st));
+                CUDA_CHECK(cudaStreamSynchronize(st));
+                if (*c->pinnedCount == 0) break;
+                maxItems = *c->pinnedCount;
+            }
+        }
+        {
+            KTimer kt(c, 4);
+            launch_film_fold(dj, dch, dwv, dcur, c->samples.as<float>(), dstats, allowEarlyExit ? maxFold : maxFold, 1, st);
+        }
+    };
+
+    const char* ge = getenv("SST_GRAPH");
+    bool useGraph = !c->profiling && !timeLimit && maxDepth <= 32 && !(ge && std::string(ge) == "0") && waves.size() > 1;
+    CUDA_CHECK(cudaEventRecord(c->ev0, st));
+    auto t0 = std::chrono::steady_clock::now();
+    int wavesDone = 0;
+    if (useGraph) {
+        // capture one wave (fixed grid sizes; wave parameters are read from device memory)
+        cudaGraph_t graph;
+        cudaGraphExec_t exec;
+        CUDA_CHECK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+        try {
+            issueWave(w.wb.cap, false);
+        } catch (...) {
+            cudaStreamEndCapture(st, &graph);
+            throw;
+        }
+        CUDA_CHECK(cudaStreamEndCapture(st, &graph));
+        CUDA_CHECK(cudaGraphInstantiate(&exec, graph, 0));
+        for (size_t k = 0; k < waves.size(); ++k) CUDA_CHECK(cudaGraphLaunch(exec, st));
+        CUDA_CHECK(cudaGetLastError());
+        CUDA_CHECK(cudaStreamSynchronize(st));
+        cudaGraphExecDestroy(exec);
+        cudaGraphDestroy(graph);
+        wavesDone = int(waves.size());
+    } else {
+        for (size_t k = 0; k < waves.size(); ++k) {
+            if (timeLimit && k > 0) {
+                CUDA_CHECK(cudaStreamSynchronize(st));
+                double ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+                double per = ms / double(k);
+                if (ms + per > double(jobs[0].p.maximumRenderTimeMs)) break;  // PathTracer.cs:221-227
+            }
+            issueWave(waves[k].items, true);
             CUDA_CHECK(cudaGetLastError());
             if (c->profiling) {
-                // items per class: queue lengths of this wave
                 std::vector<int> hc(kNumCounters);
                 CUDA_CHECK(cudaMemcpyAsync(hc.data(), cnt, sizeof(int) * kNumCounters, cudaMemcpyDeviceToHost, st));
                 flushTimers(c);
-                c->kItems[0] += n;
-                c->kItems[4] += pc;
-                for (int d = 1; d <= P->maxDepth && d < 1024; ++d) {
+                c->kItems[0] += waves[k].items;
+                c->kItems[4] += waves[k].foldThreads;
+                for (int d = 1; d <= maxDepth && d < 1024; ++d) {
                     c->kItems[1] += hc[kCntQueue + d];
                     c->kItems[2] += hc[kCntQueue + d];
                     c->kItems[3] += hc[kCntShadow + d];
                 }
             }
+            ++wavesDone;
         }
-        it += nIt;
-        iterations += nIt;
     }
     CUDA_CHECK(cudaEventRecord(c->ev1, st));
     CUDA_CHECK(cudaStreamSynchronize(st));
@@ -776,9 +883,16 @@ static void renderDevice(sst_scene* s, const SstPathTracerParams* P, float* dFil
     DevStats hs;
     CUDA_CHECK(cudaMemcpy(&hs, dstats, sizeof(DevStats), cudaMemcpyDeviceToHost));
     if (hs.errorFlags & 1) fail(SST_ERR_DEVICE_LIMIT, "BVH traversal stack overflow");
+    // iterations completed per job
+    for (int k = 0; k < wavesDone; ++k)
+        for (int ci = waves[k].chunkBegin; ci < waves[k].chunkEnd; ++ci) {
+            const WaveChunk& ck = chunks[ci];
+            JobIn& jb = jobs[ck.job];
+            if (ck.pixStart + ck.pixCount == jb.p.width * jb.p.height) jb.done = std::max(jb.done, ck.iterBase + ck.nIter - jb.iterFirst);
+        }
     if (out) {
         out->renderTimeMs += ms;
-        out->numIterations += iterations;
+        out->numIterations += jobs.size() == 1 ? jobs[0].done : 0;
         out->numRays += hs.rays;
         out->numShadowRays += hs.shadowRays;
         uint64_t prev = out->numNanOrInf;
@@ -807,6 +921,15 @@ template <class T> static void hostCopy(T* h, const DevBuf& b, size_t n, cudaStr
     CUDA_CHECK(cudaMemcpyAsync(h, b.p, n * sizeof(T), cudaMemcpyDeviceToHost, st));
 }
 
+// A one-entry job table holding the scene (for the ray-query entry points).
+static const DevJob* jobTable(sst_scene* s) {
+    DevJob j{};
+    j.sc = s->dev;
+    s->queryJob.ensure(sizeof(DevJob));
+    CUDA_CHECK(cudaMemcpyAsync(s->queryJob.p, &j, sizeof(DevJob), cudaMemcpyHostToDevice, s->ctx->stream));
+    return s->queryJob.as<DevJob>();
+}
+
 static void runQuery(sst_scene* s, const SstRay* rays, int n, SstHit* hits, int32_t* occl, int memory, bool anyHit) {
     if (!s || (n > 0 && !rays) || n < 0) fail(SST_ERR_INVALID_ARGUMENT, "invalid query");
     if (!s->committed) fail(SST_ERR_NOT_COMMITTED, "scene is not committed");
@@ -828,15 +951,15 @@ static void runQuery(sst_scene* s, const SstRay* rays, int n, SstHit* hits, int3
     CUDA_CHECK(cudaMemsetAsync(c->stats.p, 0, sizeof(DevStats), st));
     if (anyHit) {
         occBuf.ensure(size_t(n) * 4);
-        launch_trace_query(s->dev, ro.as<float4>(), rd.as<float4>(), cnt.as<int>(), cnt.as<int>() + 1, nullptr, occBuf.as<int>(), c->stats.as<DevStats>(),
-                           true, st);
+        launch_trace_query(jobTable(s), ro.as<float4>(), rd.as<float4>(), cnt.as<int>(), cnt.as<int>() + 1, nullptr, occBuf.as<int>(),
+                           c->stats.as<DevStats>(), true, st);
         CUDA_CHECK(cudaMemcpyAsync(occl, occBuf.p, size_t(n) * 4, memory == SST_MEM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, st));
         CUDA_CHECK(cudaStreamSynchronize(st));
         return;
     }
     hitsBuf.ensure(size_t(n) * 16);
-    launch_trace_query(s->dev, ro.as<float4>(), rd.as<float4>(), cnt.as<int>(), cnt.as<int>() + 1, hitsBuf.as<float4>(), nullptr, c->stats.as<DevStats>(),
-                       false, st);
+    launch_trace_query(jobTable(s), ro.as<float4>(), rd.as<float4>(), cnt.as<int>(), cnt.as<int>() + 1, hitsBuf.as<float4>(), nullptr,
+                       c->stats.as<DevStats>(), false, st);
     std::vector<float4> hh(n);
     CUDA_CHECK(cudaMemcpyAsync(hh.data(), hitsBuf.p, size_t(n) * 16, cudaMemcpyDeviceToHost, st));
     CUDA_CHECK(cudaStreamSynchronize(st));
@@ -1167,7 +1290,15 @@ int sst_render(sst_scene* s, const SstPathTracerParams* p, float* film, int32_t 
         }
         CUDA_CHECK(cudaStreamSynchronize(c->stream));
         double fbMs = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - tfb0).count();
-        if (p->firstIteration < p->totalSpp) renderDevice(s, p, dFilm, p->firstIteration, p->totalSpp, &local);
+        if (p->firstIteration < p->totalSpp) {
+            std::vector<JobIn> jobs(1);
+            jobs[0].s = s;
+            jobs[0].p = *p;
+            jobs[0].dFilm = dFilm;
+            jobs[0].iterFirst = p->firstIteration;
+            jobs[0].iterEnd = p->totalSpp;
+            renderJobs(c, jobs, &local);
+        }
         auto tfb1 = std::chrono::steady_clock::now();
         if (memory != SST_MEM_DEVICE) CUDA_CHECK(cudaMemcpy(film, dFilm, filmBytes, cudaMemcpyDeviceToHost));
         fbMs += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - tfb1).count();
@@ -1179,19 +1310,50 @@ int sst_render(sst_scene* s, const SstPathTracerParams* p, float* film, int32_t 
 int sst_render_batch(sst_ctx* ctx, const SstRenderJob* jobs, int32_t numJobs, SstRenderStats* stats) {
     return guarded([&] {
         if (!ctx || (numJobs > 0 && !jobs) || numJobs < 0) fail(SST_ERR_INVALID_ARGUMENT, "invalid batch");
+        CUDA_CHECK(cudaSetDevice(ctx->device));
         SstRenderStats total{};
         for (int k = 0; k < 4; ++k) { total.nanPixel[k] = -1; total.nanIteration[k] = -1; }
+        std::vector<JobIn> in(numJobs);
+        std::vector<std::unique_ptr<DevBuf>> hostFilms(numJobs);
+        auto t0 = std::chrono::steady_clock::now();
         for (int j = 0; j < numJobs; ++j) {
-            SstRenderStats st{};
-            int rc = sst_render(jobs[j].scene, &jobs[j].params, jobs[j].film, jobs[j].memory, &st);
-            if (rc != SST_OK) fail(rc, "job " + std::to_string(j) + ": " + g_lastError);
-            total.renderTimeMs += st.renderTimeMs;
-            total.frameBufferTimeMs += st.frameBufferTimeMs;
-            total.numIterations += st.numIterations;
-            total.numRays += st.numRays;
-            total.numShadowRays += st.numShadowRays;
-            total.numNanOrInf += st.numNanOrInf;
+            const SstRenderJob& J = jobs[j];
+            if (!J.scene || !J.film) fail(SST_ERR_INVALID_ARGUMENT, "job " + std::to_string(j) + ": NULL scene or film");
+            if (J.scene->ctx != ctx) fail(SST_ERR_INVALID_ARGUMENT, "job " + std::to_string(j) + ": scene belongs to another context");
+            checkParams(J.scene, &J.params);
+            size_t filmBytes = size_t(J.params.width) * J.params.height * 3 * sizeof(float);
+            float* dFilm = J.film;
+            if (J.memory != SST_MEM_DEVICE) {
+                hostFilms[j].reset(new DevBuf());
+                hostFilms[j]->ensure(filmBytes);
+                dFilm = hostFilms[j]->as<float>();
+                if (J.params.firstIteration > 0) CUDA_CHECK(cudaMemcpyAsync(dFilm, J.film, filmBytes, cudaMemcpyHostToDevice, ctx->stream));
+                else CUDA_CHECK(cudaMemsetAsync(dFilm, 0, filmBytes, ctx->stream));
+            } else if (J.params.firstIteration == 0) {
+                CUDA_CHECK(cudaMemsetAsync(dFilm, 0, filmBytes, ctx->stream));
+            }
+            in[j].s = J.scene;
+            in[j].p = J.params;
+            in[j].dFilm = dFilm;
+            in[j].iterFirst = J.params.firstIteration;
+            in[j].iterEnd = std::max(J.params.firstIteration, J.params.totalSpp);
         }
+        CUDA_CHECK(cudaStreamSynchronize(ctx->stream));
+        double fbMs = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+        renderJobs(ctx, in, &total);
+        auto t1 = std::chrono::steady_clock::now();
+        for (int j = 0; j < numJobs; ++j) {
+            if (jobs[j].memory != SST_MEM_DEVICE) {
+                size_t filmBytes = size_t(jobs[j].params.width) * jobs[j].params.height * 3 * sizeof(float);
+                CUDA_CHECK(cudaMemcpyAsync(jobs[j].film, in[j].dFilm, filmBytes, cudaMemcpyDeviceToHost, ctx->stream));
+            }
+        }
+        CUDA_CHECK(cudaStreamSynchronize(ctx->stream));
+        fbMs += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t1).count();
+        total.frameBufferTimeMs = fbMs;
+        int it = 0;
+        for (auto& j : in) it += j.done;
+        total.numIterations = it;
         if (stats) *stats = total;
     });
 }

@@ -61,20 +61,35 @@ void launch_env_build(const float4* img, int w, int h, float* colCdf, float* row
 // =============================================================================================
 // K2: camera rays.  Path p of the wave is pixel pixStart + p of iteration `iter`.
 // =============================================================================================
-__global__ void __launch_bounds__(256) k_camera(DevScene sc, PTConfig cfg, PathBuf A, int pixStart, int pixCount, int n, uint32_t iterBase,
-                                                int* qCount) {
+__device__ __forceinline__ int findChunk(const WaveChunk* ch, int lo, int hi, int item) {
+    // last chunk with itemOffset <= item (chunks are sorted by itemOffset)
+    while (hi - lo > 1) {
+        int mid = (lo + hi) >> 1;
+        if (ch[mid].itemOffset <= item) lo = mid; else hi = mid;
+    }
+    return lo;
+}
+
+__global__ void __launch_bounds__(256) k_camera(const DevJob* __restrict__ jobs, const WaveChunk* __restrict__ chunks, const WaveDesc* waves,
+                                                const int* curWave, PathBuf A, int* qCount) {
+    const WaveDesc wd = waves[*curWave];
     int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i == 0) *qCount = n;
-    if (i >= n) return;
-    int m = i / pixCount;
-    uint32_t pix = (uint32_t)(pixStart + (i - m * pixCount));
-    uint32_t iter = iterBase + (uint32_t)m;
-    uint32_t row = pix / (uint32_t)cfg.W, col = pix - row * (uint32_t)cfg.W;
-    Rng rng{hashSeed(cfg.baseSeed, pix, iter)};  // PathTracer.cs:236-237
-    float ox = rng.nextFloat();                  // PathTracer.cs:289
+    if (i == 0) *qCount = wd.items;
+    if (i >= wd.items) return;
+    int c = findChunk(chunks, wd.chunkBegin, wd.chunkEnd, i);
+    const WaveChunk ck = chunks[c];
+    const DevJob& jb = jobs[ck.job];
+    int local = i - ck.itemOffset;
+    int m = local / ck.pixCount;
+    uint32_t pix = (uint32_t)(ck.pixStart + (local - m * ck.pixCount));
+    uint32_t iter = (uint32_t)(ck.iterBase + m);
+    uint32_t row = pix / (uint32_t)jb.cfg.W, col = pix - row * (uint32_t)jb.cfg.W;
+    Rng rng{hashSeed(jb.cfg.baseSeed, pix, iter)};  // PathTracer.cs:236-237
+    float ox = rng.nextFloat();                      // PathTracer.cs:289
     float oy = rng.nextFloat();
     float3 org, dir;
-    cameraRay(sc.cam, (float)col + ox, (float)row + oy, org, dir);
+    cameraRay(jb.sc.cam, (float)col + ox, (float)row + oy, org, dir);
+    A.job[i] = (uint32_t)ck.job;
     A.pix[i] = (uint32_t)i;  // wave item; the film fold maps it back to (iteration, pixel)
     A.rng[i] = rng.s;
     A.depth[i] = 1u;
@@ -89,33 +104,58 @@ __global__ void __launch_bounds__(256) k_camera(DevScene sc, PTConfig cfg, PathB
 // running mean: for iteration k (1-based) film = film * (k - 1) / k + v / k, non-finite
 // estimates logged and skipped (FrameBuffer.Splat/Normalize, Images/FrameBuffer.cs:166-191, 232).
 // =============================================================================================
-__global__ void k_film_fold(PTConfig cfg, const float* samples, int pixStart, int pixCount, int iters, uint32_t iterBase, float* film,
-                            DevStats* st) {
-    int p = blockIdx.x * blockDim.x + threadIdx.x;
-    if (p >= pixCount) return;
-    size_t pix = (size_t)(pixStart + p);
-    float* f = film + 3 * pix;
-    float3 cur = mk(f[0], f[1], f[2]);
-    for (int m = 0; m < iters; ++m) {
-        uint32_t iter = iterBase + (uint32_t)m;
-        const float* s = samples + 3 * ((size_t)m * pixCount + p);
-        float3 v = mk(s[0], s[1], s[2]);
-        float kf = (float)(iter + 1);
-        if (iter > 0) cur = cur * ((kf - 1.0f) / kf);
-        float a = avg3(v);
-        bool finite = isfinite(a);
-        if (!finite) {
-            unsigned long long k = atomicAdd(&st->nanCount, 1ull);
-            if (k < 4) { st->nanPixel[k] = (int)pix; st->nanIter[k] = (int)iter + 1; }
+__global__ void k_film_fold(const DevJob* __restrict__ jobs, const WaveChunk* __restrict__ chunks, const WaveDesc* waves, int* curWave,
+                            const float* samples, DevStats* st, int advance) {
+    const WaveDesc wd = waves[*curWave];
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < wd.foldThreads) {
+        // chunk of this fold thread (sorted by foldOffset as well)
+        int lo = wd.chunkBegin, hi = wd.chunkEnd;
+        while (hi - lo > 1) {
+            int mid = (lo + hi) >> 1;
+            if (chunks[mid].foldOffset <= t) lo = mid; else hi = mid;
         }
-        if (finite || !cfg.ignoreNan) cur = cur + v / kf;
+        const WaveChunk ck = chunks[lo];
+        const PTConfig& cfg = jobs[ck.job].cfg;
+        int p = t - ck.foldOffset;
+        size_t pix = (size_t)(ck.pixStart + p);
+        float* f = ck.film + 3 * pix;
+        float3 cur = mk(f[0], f[1], f[2]);
+        for (int m = 0; m < ck.nIter; ++m) {
+            uint32_t iter = (uint32_t)(ck.iterBase + m);
+            const float* s = samples + 3 * ((size_t)ck.itemOffset + (size_t)m * ck.pixCount + p);
+            float3 v = mk(s[0], s[1], s[2]);
+            float kf = (float)(iter + 1);
+            if (iter > 0) cur = cur * ((kf - 1.0f) / kf);
+            float a = avg3(v);
+            bool finite = isfinite(a);
+            if (!finite) {
+                unsigned long long k = atomicAdd(&st->nanCount, 1ull);
+                if (k < 4) { st->nanPixel[k] = (int)pix; st->nanIter[k] = (int)iter + 1; }
+            }
+            if (finite || !cfg.ignoreNan) cur = cur + v / kf;
+        }
+        f[0] = cur.x; f[1] = cur.y; f[2] = cur.z;
     }
-    f[0] = cur.x; f[1] = cur.y; f[2] = cur.z;
+    // the last block to finish advances the wave counter (one CUDA graph serves every wave)
+    if (advance) {
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            __threadfence();
+            unsigned done = atomicAdd((unsigned*)(curWave + 1), 1u);
+            if (done == gridDim.x - 1) {
+                curWave[1] = 0;
+                __threadfence();
+                curWave[0] = curWave[0] + 1;
+            }
+        }
+    }
 }
 
-void launch_film_fold(const PTConfig& cfg, const float* samples, int pixStart, int pixCount, int iters, uint32_t iterBase, float* film,
-                      DevStats* st, cudaStream_t s) {
-    k_film_fold<<<(pixCount + 255) / 256, 256, 0, s>>>(cfg, samples, pixStart, pixCount, iters, iterBase, film, st);
+void launch_film_fold(const DevJob* jobs, const WaveChunk* chunks, const WaveDesc* waves, int* curWave, const float* samples, DevStats* st,
+                      int maxFold, int advance, cudaStream_t s) {
+    int grid = std::max(1, (maxFold + 255) / 256);
+    k_film_fold<<<grid, 256, 0, s>>>(jobs, chunks, waves, curWave, samples, st, advance);
 }
 
 // =============================================================================================
@@ -175,8 +215,15 @@ struct TraceResult {
 };
 
 // Closest hit (ANY = false; ties in t resolve to the smaller global triangle id) or any hit.
+struct Bvh {
+    const float4* nodes;
+    const float4* triv;
+    int nNodes;
+};
+SST_D Bvh bvhOf(const DevScene& sc) { return Bvh{sc.nodes, sc.triv, sc.nNodes}; }
+
 template <bool ANY>
-SST_D TraceResult traverse(const DevScene& sc, float3 org, float3 dir, float tmin, float tmax, int* sstack, int* errFlags) {
+SST_D TraceResult traverse(const Bvh sc, float3 org, float3 dir, float tmin, float tmax, int* sstack, int* errFlags) {
     TraceResult r{tmax, 0.f, 0.f, -1};
     if (sc.nNodes == 0 || !(tmax > tmin)) return r;
     int bestGid = 0x7FFFFFFF;
@@ -243,9 +290,9 @@ SST_D TraceResult traverse(const DevScene& sc, float3 org, float3 dir, float tmi
 // mode 0: closest hit -> hits[i]; mode 1: shadow rays, zero nee[tgt[i]] when occluded;
 // mode 2: any hit -> occl[i] = 1/0.
 template <int MODE>
-__global__ void __launch_bounds__(kTraceBlock) k_trace(DevScene sc, const float4* ro, const float4* rd, const int* count, int* work,
-                                                       float4* hits, const int* tgt, float4* nee, int* occl, DevStats* stats,
-                                                       int countRays) {
+__global__ void __launch_bounds__(kTraceBlock) k_trace(const DevJob* __restrict__ jobs, const uint32_t* __restrict__ rayJob, const float4* ro,
+                                                       const float4* rd, const int* count, int* work, float4* hits, const int* tgt, float4* nee,
+                                                       int* occl, DevStats* stats, int countRays) {
     __shared__ int sstack[kSmemStack * kTraceBlock];
     const int n = *count;
     const int lane = threadIdx.x & 31;
@@ -260,7 +307,8 @@ __global__ void __launch_bounds__(kTraceBlock) k_trace(DevScene sc, const float4
         int i = base + lane;
         if (i < n) {
             float4 o = ro[i], d = rd[i];
-            TraceResult h = traverse<MODE != 0>(sc, f3(o), f3(d), o.w, d.w, sstack, &stats->errorFlags);
+            uint32_t jb = rayJob ? rayJob[i] : 0u;
+            TraceResult h = traverse<MODE != 0>(bvhOf(jobs[jb].sc), f3(o), f3(d), o.w, d.w, sstack, &stats->errorFlags);
             if (MODE == 0) {
                 hits[i] = make_float4(h.t, h.u, h.v, __int_as_float(h.tri));
             } else if (MODE == 1) {
@@ -284,18 +332,18 @@ int traceGrid() {
     return g;
 }
 
-void launch_trace_closest(const DevScene& sc, const float4* ro, const float4* rd, const int* count, int* work, float4* hits, DevStats* stats,
-                          cudaStream_t s) {
-    k_trace<0><<<traceGrid(), kTraceBlock, 0, s>>>(sc, ro, rd, count, work, hits, nullptr, nullptr, nullptr, stats, 1);
+void launch_trace_closest(const DevJob* jobs, const uint32_t* rayJob, const float4* ro, const float4* rd, const int* count, int* work, float4* hits,
+                          DevStats* stats, cudaStream_t s) {
+    k_trace<0><<<traceGrid(), kTraceBlock, 0, s>>>(jobs, rayJob, ro, rd, count, work, hits, nullptr, nullptr, nullptr, stats, 1);
 }
-void launch_trace_shadow(const DevScene& sc, const float4* ro, const float4* rd, const int* tgt, const int* count, int* work, float4* nee,
-                         DevStats* stats, cudaStream_t s) {
-    k_trace<1><<<traceGrid(), kTraceBlock, 0, s>>>(sc, ro, rd, count, work, nullptr, tgt, nee, nullptr, stats, 0);
+void launch_trace_shadow(const DevJob* jobs, const uint32_t* rayJob, const float4* ro, const float4* rd, const int* tgt, const int* count, int* work,
+                         float4* nee, DevStats* stats, cudaStream_t s) {
+    k_trace<1><<<traceGrid(), kTraceBlock, 0, s>>>(jobs, rayJob, ro, rd, count, work, nullptr, tgt, nee, nullptr, stats, 0);
 }
-void launch_trace_query(const DevScene& sc, const float4* ro, const float4* rd, const int* count, int* work, float4* hits, int* occl,
+void launch_trace_query(const DevJob* jobs, const float4* ro, const float4* rd, const int* count, int* work, float4* hits, int* occl,
                         DevStats* stats, bool anyHit, cudaStream_t s) {
-    if (anyHit) k_trace<2><<<traceGrid(), kTraceBlock, 0, s>>>(sc, ro, rd, count, work, nullptr, nullptr, nullptr, occl, stats, 0);
-    else k_trace<0><<<traceGrid(), kTraceBlock, 0, s>>>(sc, ro, rd, count, work, hits, nullptr, nullptr, nullptr, stats, 0);
+    if (anyHit) k_trace<2><<<traceGrid(), kTraceBlock, 0, s>>>(jobs, nullptr, ro, rd, count, work, nullptr, nullptr, nullptr, occl, stats, 0);
+    else k_trace<0><<<traceGrid(), kTraceBlock, 0, s>>>(jobs, nullptr, ro, rd, count, work, hits, nullptr, nullptr, nullptr, stats, 0);
 }
 
 // =============================================================================================
@@ -315,15 +363,17 @@ SST_D int aggAppend(int* counter) {
 }
 
 template <int NS>
-__global__ void __launch_bounds__(128, SST_SHADE_MIN_BLOCKS) k_shade(DevScene sc, PTConfig cfg, PathBuf A, PathBuf B, const float4* __restrict__ hits, float4* nee,
-                                               int cap, float4* shRo, float4* shRd, int* shTgt, const int* nIn, int* nOut, int* nSh,
-                                               float* film, DevStats* stats) {
+__global__ void __launch_bounds__(128, SST_SHADE_MIN_BLOCKS) k_shade(const DevJob* __restrict__ jobs, PathBuf A, PathBuf B,
+                                                                   const float4* __restrict__ hits, float4* nee, int cap, float4* shRo,
+                                                                   float4* shRd, int* shTgt, uint32_t* shJob, const int* nIn, int* nOut,
+                                                                   int* nSh, float* samples, DevStats* stats) {
     const int n = *nIn;
     if ((int)(blockIdx.x * blockDim.x) >= n) return;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     const bool valid = i < n;
 
     bool cont = false;
+    uint32_t job = 0;
     uint32_t outDepth = 0;
     float3 prefix = mk(1, 1, 1), radiance = mk(0, 0, 0);
     float prevPdfOut = 0.f;
@@ -337,6 +387,9 @@ __global__ void __launch_bounds__(128, SST_SHADE_MIN_BLOCKS) k_shade(DevScene sc
     int queries = 0;
 
     if (valid) {
+        job = A.job[i];
+        const DevScene& sc = jobs[job].sc;
+        const PTConfig& cfg = jobs[job].cfg;
         pix = A.pix[i];
         rng.s = A.rng[i];
         uint32_t dw = A.depth[i];
@@ -454,6 +507,7 @@ __global__ void __launch_bounds__(128, SST_SHADE_MIN_BLOCKS) k_shade(DevScene sc
                                     if (!isBlack(val)) {
                                         int k = 2 * sIt;
                                         int q = aggAppend(nSh);
+                                        shJob[q] = job;
                                         float3 o = offsetPoint(s.pos, s.n, s.eps, ed);
                                         shRo[q] = make_float4(o.x, o.y, o.z, 0.0f);
                                         shRd[q] = make_float4(ed.x, ed.y, ed.z, CUDART_INF_F);
@@ -494,6 +548,7 @@ __global__ void __launch_bounds__(128, SST_SHADE_MIN_BLOCKS) k_shade(DevScene sc
                                     if (!isBlack(val)) {
                                         int k = 2 * sIt + 1;
                                         int q = aggAppend(nSh);
+                                        shJob[q] = job;
                                         float3 dd = lpPos - s.pos;
                                         float3 o = offsetPoint(s.pos, s.n, s.eps, dd);
                                         float3 e = offsetPoint(lpPos, lpN, lpEps, -dd);
@@ -528,7 +583,7 @@ __global__ void __launch_bounds__(128, SST_SHADE_MIN_BLOCKS) k_shade(DevScene sc
                 }
             }
         }
-        if (terminate) splat(film, pix, radiance);
+        if (terminate) splat(samples, pix, radiance);
         if (!cont) pend = 0;
     }
     // shadow-query statistics (RayTracerStats.NumShadowRays semantics)
@@ -544,6 +599,7 @@ __global__ void __launch_bounds__(128, SST_SHADE_MIN_BLOCKS) k_shade(DevScene sc
     base = __shfl_sync(0xffffffffu, base, 0);
     if (!cont) return;
     int j = base + __popc(m & ((1u << lane) - 1u));
+    B.job[j] = job;
     B.pix[j] = pix;
     B.rng[j] = rng.s;
     B.depth[j] = outDepth;
@@ -562,22 +618,22 @@ __global__ void __launch_bounds__(128, SST_SHADE_MIN_BLOCKS) k_shade(DevScene sc
     }
 }
 
-void launch_shade(int ns, const DevScene& sc, const PTConfig& cfg, const PathBuf& A, const PathBuf& B, const float4* hits, float4* nee, int cap,
-                  float4* shRo, float4* shRd, int* shTgt, const int* nIn, int* nOut, int* nSh, float* film, DevStats* stats, int maxItems,
+void launch_shade(int ns, const DevJob* jobs, const PathBuf& A, const PathBuf& B, const float4* hits, float4* nee, int cap, float4* shRo,
+                  float4* shRd, int* shTgt, uint32_t* shJob, const int* nIn, int* nOut, int* nSh, float* samples, DevStats* stats, int maxItems,
                   cudaStream_t s) {
     int grid = (maxItems + 127) / 128;
     if (grid == 0) return;
     switch (ns) {
-        case 1: k_shade<1><<<grid, 128, 0, s>>>(sc, cfg, A, B, hits, nee, cap, shRo, shRd, shTgt, nIn, nOut, nSh, film, stats); break;
-        case 2: k_shade<2><<<grid, 128, 0, s>>>(sc, cfg, A, B, hits, nee, cap, shRo, shRd, shTgt, nIn, nOut, nSh, film, stats); break;
-        case 3: k_shade<3><<<grid, 128, 0, s>>>(sc, cfg, A, B, hits, nee, cap, shRo, shRd, shTgt, nIn, nOut, nSh, film, stats); break;
-        default: k_shade<4><<<grid, 128, 0, s>>>(sc, cfg, A, B, hits, nee, cap, shRo, shRd, shTgt, nIn, nOut, nSh, film, stats); break;
+        case 1: k_shade<1><<<grid, 128, 0, s>>>(jobs, A, B, hits, nee, cap, shRo, shRd, shTgt, shJob, nIn, nOut, nSh, samples, stats); break;
+        case 2: k_shade<2><<<grid, 128, 0, s>>>(jobs, A, B, hits, nee, cap, shRo, shRd, shTgt, shJob, nIn, nOut, nSh, samples, stats); break;
+        case 3: k_shade<3><<<grid, 128, 0, s>>>(jobs, A, B, hits, nee, cap, shRo, shRd, shTgt, shJob, nIn, nOut, nSh, samples, stats); break;
+        default: k_shade<4><<<grid, 128, 0, s>>>(jobs, A, B, hits, nee, cap, shRo, shRd, shTgt, shJob, nIn, nOut, nSh, samples, stats); break;
     }
 }
 
-void launch_camera(const DevScene& sc, const PTConfig& cfg, const PathBuf& A, int pixStart, int pixCount, int n, uint32_t iterBase, int* qCount,
-                   cudaStream_t s) {
-    k_camera<<<(n + 255) / 256, 256, 0, s>>>(sc, cfg, A, pixStart, pixCount, n, iterBase, qCount);
+void launch_camera(const DevJob* jobs, const WaveChunk* chunks, const WaveDesc* waves, const int* curWave, const PathBuf& A, int* qCount,
+                   int maxItems, cudaStream_t s) {
+    k_camera<<<std::max(1, (maxItems + 255) / 256), 256, 0, s>>>(jobs, chunks, waves, curWave, A, qCount);
 }
 
 // =============================================================================================

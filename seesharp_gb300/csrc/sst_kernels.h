@@ -7,18 +7,18 @@
 namespace sst {
 
 void launch_env_build(const float4* img, int w, int h, float* colCdf, float* rowMarg, int* hasCol, float* rowCdf, cudaStream_t s);
-void launch_camera(const DevScene& sc, const PTConfig& cfg, const PathBuf& A, int pixStart, int pixCount, int n, uint32_t iterBase, int* qCount,
-                   cudaStream_t s);
-void launch_film_fold(const PTConfig& cfg, const float* samples, int pixStart, int pixCount, int iters, uint32_t iterBase, float* film,
-                      DevStats* st, cudaStream_t s);
-void launch_trace_closest(const DevScene& sc, const float4* ro, const float4* rd, const int* count, int* work, float4* hits, DevStats* stats,
-                          cudaStream_t s);
-void launch_trace_shadow(const DevScene& sc, const float4* ro, const float4* rd, const int* tgt, const int* count, int* work, float4* nee,
-                         DevStats* stats, cudaStream_t s);
-void launch_trace_query(const DevScene& sc, const float4* ro, const float4* rd, const int* count, int* work, float4* hits, int* occl,
+void launch_camera(const DevJob* jobs, const WaveChunk* chunks, const WaveDesc* waves, const int* curWave, const PathBuf& A, int* qCount,
+                   int maxItems, cudaStream_t s);
+void launch_film_fold(const DevJob* jobs, const WaveChunk* chunks, const WaveDesc* waves, int* curWave, const float* samples, DevStats* st,
+                      int maxFold, int advance, cudaStream_t s);
+void launch_trace_closest(const DevJob* jobs, const uint32_t* rayJob, const float4* ro, const float4* rd, const int* count, int* work, float4* hits,
+                          DevStats* stats, cudaStream_t s);
+void launch_trace_shadow(const DevJob* jobs, const uint32_t* rayJob, const float4* ro, const float4* rd, const int* tgt, const int* count, int* work,
+                         float4* nee, DevStats* stats, cudaStream_t s);
+void launch_trace_query(const DevJob* jobs, const float4* ro, const float4* rd, const int* count, int* work, float4* hits, int* occl,
                         DevStats* stats, bool anyHit, cudaStream_t s);
-void launch_shade(int ns, const DevScene& sc, const PTConfig& cfg, const PathBuf& A, const PathBuf& B, const float4* hits, float4* nee, int cap,
-                  float4* shRo, float4* shRd, int* shTgt, const int* nIn, int* nOut, int* nSh, float* film, DevStats* stats, int maxItems,
+void launch_shade(int ns, const DevJob* jobs, const PathBuf& A, const PathBuf& B, const float4* hits, float4* nee, int cap, float4* shRo,
+                  float4* shRd, int* shTgt, uint32_t* shJob, const int* nIn, int* nOut, int* nSh, float* samples, DevStats* stats, int maxItems,
                   cudaStream_t s);
 void launch_debug_material_eval(const DevScene& sc, int mat, int n, const float* pts, const float* outs, const float* ins, float* vals, float* pdfs,
                                 cudaStream_t s);

@@ -89,6 +89,36 @@ struct PTConfig {
     int ignoreNan;
 };
 
+// One render job: its scene and path-tracer settings (the kernels index this table by the job
+// id every path carries).
+struct DevJob {
+    DevScene sc;
+    PTConfig cfg;
+};
+
+// A chunk of a wave: nIter consecutive iterations of the pixel range [pixStart, pixStart +
+// pixCount) of one job.  Wave items [itemOffset, itemOffset + nIter * pixCount) are its paths
+// (iteration-major); fold threads [foldOffset, foldOffset + pixCount) fold them into the film.
+struct WaveChunk {
+    int job;
+    int iterBase;
+    int nIter;
+    int pixStart;
+    int pixCount;
+    int itemOffset;
+    int foldOffset;
+    int pad;
+    float* film;
+};
+
+// Per-wave parameters read by the kernels from device memory, so that the same kernel sequence
+// (and one captured CUDA graph) serves every wave.
+struct WaveDesc {
+    int chunkBegin, chunkEnd;  // chunk index range
+    int items;                 // paths in the wave
+    int foldThreads;           // pixels to fold
+};
+
 // Device counters of one render (zeroed per render).
 struct DevStats {
     unsigned long long rays;
@@ -102,6 +132,7 @@ struct DevStats {
 
 // Structure-of-arrays path state for one buffer (double-buffered A/B).
 struct PathBuf {
+    uint32_t* job;     // render job of the path
     uint32_t* pix;
     uint32_t* rng;
     uint32_t* depth;   // bits 0-15 depth, 16-23 pending NEE slots, bit 31 done
@@ -123,6 +154,7 @@ struct WaveBuffers {
     float4* shRo;        // shadow queue: origin, tmin
     float4* shRd;        // direction, tmax
     int* shTgt;          // nee slot index
+    uint32_t* shJob;     // render job of the shadow ray
     int* counters;       // per bounce queue lengths and work counters
     int cap;             // paths per wave
     int shCap;           // shadow queue capacity

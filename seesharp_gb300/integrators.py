@@ -88,3 +88,28 @@ class PathTracer(Integrator):
                 fb.NaNWarnings.append((px % fb.Width, px // fb.Width, stats.nanIteration[k]))
         fb.MetaData["NumNaNOrInf"] = int(stats.numNanOrInf)
         self.last_stats = stats
+
+
+def render_batch(pairs):
+    """Renders many (scene, PathTracer) pairs in one shared wavefront (sst_render_batch).
+
+    Every scene must be prepared on the same device.  The films are the scenes' FrameBuffers,
+    exactly as if each PathTracer had rendered its scene alone.
+    """
+    if not pairs:
+        return None
+    ctx = pairs[0][0].native.ctx
+    jobs = []
+    for sc, pt in pairs:
+        pt._check_hooks()
+        if sc.native.ctx is not ctx:
+            raise ValueError("all scenes of a batch must share one device context")
+        p = pt.params(sc)
+        film = sc.FrameBuffer.Image.data
+        jobs.append((sc.native, p, film.ctypes.data, _native.SST_MEM_HOST))
+    stats = _native.render_batch(ctx, jobs)
+    for sc, pt in pairs:
+        fb = sc.FrameBuffer
+        fb.CurIteration = max(fb.CurIteration, int(pt.TotalSpp))
+        fb.MetaData["NumIterations"] = fb.CurIteration
+    return stats

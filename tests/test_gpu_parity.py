@@ -398,3 +398,57 @@ def test_device_film_pointer():
     p = _native.make_params(32, 32, 2, 4)
     sc.native.render(p, film.data_ptr(), _native.SST_MEM_DEVICE)
     assert np.array_equal(film.cpu().numpy(), host)
+
+
+# ---------------------------------------------------------------------------------------------
+def _batch_scenes():
+    out = []
+    specs = [(workloads.cornell_box, (40, 30), 3, 5), (workloads.cornell_box, (17, 64), 5, 3),
+             (lambda w, h: workloads.sphere_field(6, w, h, level=3), (48, 48), 4, 8),
+             (lambda w, h: workloads.validate_environment(w, h)[0], (33, 21), 2, 5),
+             (lambda w, h: workloads.validate_glossy_light(w, h)[0], (50, 50), 6, 2)]
+    for fn, (w, h), spp, depth in specs:
+        sc = fn(w, h)
+        sc.Prepare()
+        out.append((sc, PathTracer(TotalSpp=spp, MaxDepth=depth)))
+    return out
+
+
+@pytest.mark.parametrize("capacity", [None, "700"])
+def test_batch_equals_individual_renders(capacity):
+    """One shared wavefront over jobs of different sizes, spp and depths gives every job the film
+    its own render gives (bitwise: per-path arithmetic and per-pixel fold order do not depend on
+    how waves are packed)."""
+    import os
+    pairs = _batch_scenes()
+    singles = []
+    for sc, pt in pairs:
+        sc.FrameBuffer.Reset()
+        pt.Render(sc)
+        singles.append(sc.FrameBuffer.Image.data.copy())
+    if capacity:
+        os.environ["SST_WAVE_CAPACITY"] = capacity
+    try:
+        for sc, _ in pairs:
+            sc.FrameBuffer.Reset()
+        from seesharp_gb300 import render_batch
+        render_batch(pairs)
+    finally:
+        os.environ.pop("SST_WAVE_CAPACITY", None)
+    for (sc, _), ref in zip(pairs, singles):
+        assert np.array_equal(sc.FrameBuffer.Image.data, ref)
+
+
+def test_graph_replay_equals_plain_launches():
+    import os
+    sc = workloads.cornell_box(64, 64)
+    sc.Prepare()
+    os.environ["SST_WAVE_CAPACITY"] = "3000"
+    try:
+        g, _ = render_gpu(sc, 4, 5)
+        os.environ["SST_GRAPH"] = "0"
+        p, _ = render_gpu(sc, 4, 5)
+    finally:
+        os.environ.pop("SST_GRAPH", None)
+        os.environ.pop("SST_WAVE_CAPACITY", None)
+    assert np.array_equal(g, p)
