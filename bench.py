@@ -31,6 +31,7 @@ CONFIGS = {
     0: dict(name="cornell_box_36tri_256x256_16spp_depth5", builder="cornell", W=256, H=256, spp=16, depth=5),
     1: dict(name="sphere_field_1Mtri_1024x1024_64spp_depth8", builder="spheres", spheres=200, W=1024, H=1024, spp=64, depth=8),
     2: dict(name="batch_64jobs_10k-1Mtri_128-1024px_4-64spp_depth3-10", builder="batch", jobs=64, seed=2024),
+    3: dict(name="cornell_adjoint_tex256_512x512_32spp_depth5", builder="adjoint", W=512, H=512, spp=32, depth=5, tex=256),
 }
 
 
@@ -98,6 +99,50 @@ def run_batch(args, cfg):
             "clocks": clk.summary()}
     print(json.dumps(line), flush=True)
 
+
+
+def run_adjoint(args, cfg):
+    """Differentiation workload: forward (sst_forward) and path-replay backward (sst_backward) of
+    an L2 image loss; the metric is backward time over forward time."""
+    from seesharp_gb300 import PathTracer, workloads
+    from seesharp_gb300.adjoint import DifferentiableRender, l2_loss
+    W, H, spp = cfg["W"], cfg["H"], cfg["spp"]
+    sc, tex, boxes, lights = workloads.cornell_box_differentiable(W, H, tex_res=cfg["tex"])
+    sc.Prepare()
+    dr = DifferentiableRender(sc, PathTracer(TotalSpp=spp, MaxDepth=cfg["depth"]), texture=tex, roughness_materials=boxes, emitters=[lights])
+    rng = np.random.default_rng(11)
+    tex0 = tex.Image.data.copy()
+    dr.params.baseSeed = 0x5EED
+    target = dr.forward(np.clip(tex0 * (1 + 0.3 * rng.standard_normal(tex0.shape)), 0.02, 0.98), [0.45, 0.4], [13.6, 13.2, 5.2])
+    dr.params.baseSeed = 0xC030114
+    img = dr.forward(tex0, [0.3, 0.6], [17, 12, 4])
+    _, dldi = l2_loss(img, target)
+
+    def step():
+        im = dr.forward()
+        loss, d = l2_loss(im, target)
+        dr.backward(d)
+        return dr.stats_forward.renderTimeMs, dr.stats_backward.renderTimeMs
+
+    for _ in range(args.warmup):
+        step()
+    with ClockSampler(0) as clk:
+        t0 = time.perf_counter()
+        times = [step() for _ in range(args.steps)]
+        wall = (time.perf_counter() - t0) / args.steps
+    fwd = float(np.mean([t[0] for t in times]))
+    bwd = float(np.mean([t[1] for t in times]))
+    samples = W * H * spp
+    line = {"metric": "adjoint/forward cost (PathTracer path-replay backward)", "value": round(bwd / fwd, 3), "unit": "x forward time", "n_gpus": 1,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(fwd + bwd, 3), "higher_is_better": False, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded texture and scene)",
+            "config": {"workload": cfg["name"], "texture": [cfg["tex"], cfg["tex"], 3], "roughness_params": len(boxes), "emitter_params": 3},
+            "forward": {"ms": round(fwd, 3), "Msamples_per_s": round(samples / fwd / 1e3, 3)},
+            "backward": {"ms": round(bwd, 3), "Msamples_per_s": round(samples / bwd / 1e3, 3)},
+            "e2e": {"value": round(wall * 1e3, 3), "unit": "ms per forward+loss+backward step", "h2d_bytes_per_step": int(dldi.nbytes),
+                    "d2h_bytes_per_step": int(img.nbytes + 4 * (dr.n_tex + 4 * dr.n_mat + 3 * dr.n_em))},
+            "clocks": clk.summary()}
+    print(json.dumps(line), flush=True)
 
 
 def make_scene(cfg):
@@ -412,10 +457,15 @@ def main():
             cfg[k] = a
             cfg["name"] = cfg["name"] + f"_{k}{a}"
     os.environ.setdefault("SST_BVH", "lbvh")
-    if args.impl == "reference":
+    if args.impl == "reference" and cfg["builder"] == "adjoint":
+        if dist_info()[1] == 0:
+            print(json.dumps({"impl": "reference", "unavailable": "the reference PathTracer has no adjoint (differentiation is new in this library)"}))
+    elif args.impl == "reference":
         run_reference(args, cfg)
     elif cfg["builder"] == "batch":
         run_batch(args, cfg)
+    elif cfg["builder"] == "adjoint":
+        run_adjoint(args, cfg)
     else:
         run_ours(args, cfg)
 

@@ -186,6 +186,31 @@ typedef struct SstRenderJob {
  * wavefront: all jobs' paths share the ray queues.  Films as in sst_render. */
 int sst_render_batch(sst_ctx* ctx, const SstRenderJob* jobs, int32_t numJobs, SstRenderStats* stats);
 
+/* ---- path-replay adjoint (differentiable rendering) ------------------------------------------
+ * No counterpart in the reference's C# code beyond its replay semantics: a path is a pure
+ * function of (BaseSeed, pixel, iteration) (PathTracerBase.ReplayPixel, PathTracer.cs:61-69), so
+ * the backward pass re-traces every path from its seed instead of storing its vertices.
+ * Gradients use detached sampling: pdfs, MIS weights and Russian roulette are constants; there
+ * are no geometric or visibility derivatives.  The pair behaves like a torch.autograd.Function:
+ * sst_forward(params) -> image, sst_backward(dLoss/dImage) -> dLoss/dparams. */
+typedef struct SstGradients {
+    float* textures;          /* every texture's texels, concatenated in the order they were added */
+    float* materialBaseColor; /* 3 per material: constant base colour */
+    float* materialRoughness; /* 1 per material: constant roughness (GenericMaterial) */
+    float* emitterRadiance;   /* 3 per emitter */
+    int32_t memory;           /* SST_MEM_HOST / SST_MEM_DEVICE for the arrays above */
+    int32_t reserved;
+} SstGradients;
+/* Overwrites the texels of a texture (same size and channels as when it was added). */
+int sst_scene_update_texture(sst_scene* scene, int32_t texture, const float* data);
+/* sst_render of iterations [0, totalSpp) that also keeps every path's radiance for the replay. */
+int sst_forward(sst_scene* scene, const SstPathTracerParams* params, float* image, int32_t memory, SstRenderStats* stats);
+/* Gradients of a scalar loss with respect to the scene parameters, given dLoss/dImage
+ * (width*height*3) of the image that the last sst_forward with the same params produced.  The
+ * gradient arrays are overwritten (any may be NULL). */
+int sst_backward(sst_scene* scene, const SstPathTracerParams* params, const float* dLossDImage, int32_t memory,
+                 SstGradients* gradients, SstRenderStats* stats);
+
 /* ---- kernel timing ------------------------------------------------------------------------------
  * With profiling enabled, sst_render records CUDA events around every kernel launch on the
  * context's stream and accumulates, per kernel class (0 camera, 1 closest-hit traversal,

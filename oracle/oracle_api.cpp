@@ -350,6 +350,58 @@ int ora_material_sample(void* p, int mat, const float* pt, const float* outDir, 
     return 0;
 }
 
+// Reference gradient by FP64 path replay (scene created with fp64 = 1).  dLdI: W*H*3 (float);
+// outputs (double): gTex (all textures' texels concatenated), gMatBase (3 per material),
+// gMatRough (1 per material), gEmitter (3 per emitter).  Each path's total radiance comes from an
+// FP64 render of the same path; non-finite paths are skipped as the frame buffer skips them.
+int ora_adjoint(void* p, const PTParams* P, const float* dLdI, double* gTex, double* gMatBase, double* gMatRough, double* gEmitter, int nthreads) {
+    Handle* H = static_cast<Handle*>(p);
+    if (!H->fp64) return -1;
+    const Scene<double>& sc = H->s64;
+    size_t nTex = 0;
+    std::vector<size_t> offs;
+    for (auto& t : sc.textures) { offs.push_back(nTex); nTex += t.data.size(); }
+    int nt = std::max(1, nthreads);
+    std::vector<Grads<double>> G(nt);
+    for (auto& g : G) {
+        g.tex.assign(nTex, 0.0); g.matBase.assign(3 * sc.materials.size(), 0.0); g.matRough.assign(sc.materials.size(), 0.0);
+        g.emitter.assign(3 * sc.emitters.size(), 0.0); g.texOffset = offs;
+    }
+    std::atomic<int> nextRow(0);
+    auto worker = [&](int tid) {
+        for (;;) {
+            int row = nextRow.fetch_add(1);
+            if (row >= P->height) break;
+            for (int col = 0; col < P->width; ++col) {
+                uint32_t pix = uint32_t(row * P->width + col);
+                const float* d = dLdI + 3 * size_t(pix);
+                Rgb<double> delta(double(d[0]) / P->totalSpp, double(d[1]) / P->totalSpp, double(d[2]) / P->totalSpp);
+                for (int s = 0; s < P->totalSpp; ++s) {
+                    Rng rng(P->baseSeed, pix, uint32_t(s));
+                    Rng rng2 = rng;
+                    Rgb<double> L = RenderPixel(sc, *P, uint32_t(row), uint32_t(col), rng, nullptr);
+                    if (!std::isfinite(L.Average())) continue;
+                    AdjointPixel(sc, *P, uint32_t(row), uint32_t(col), rng2, L, delta, G[tid]);
+                }
+            }
+        }
+    };
+    std::vector<std::thread> th;
+    for (int i = 1; i < nt; ++i) th.emplace_back(worker, i);
+    worker(0);
+    for (auto& t : th) t.join();
+    auto sum = [&](double* out, auto member) {
+        if (!out) return;
+        size_t n = (G[0].*member).size();
+        for (size_t k = 0; k < n; ++k) { double s = 0; for (auto& g : G) s += (g.*member)[k]; out[k] = s; }
+    };
+    sum(gTex, &Grads<double>::tex);
+    sum(gMatBase, &Grads<double>::matBase);
+    sum(gMatRough, &Grads<double>::matRough);
+    sum(gEmitter, &Grads<double>::emitter);
+    return 0;
+}
+
 int ora_env_radiance(void* p, const float* dir, float* rgb) {
     Handle* H = static_cast<Handle*>(p);
     if (!H->s32.env) return -1;

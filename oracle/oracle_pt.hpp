@@ -609,6 +609,11 @@ template <class T> inline bool ShouldReflect(const SurfacePoint<T>& hit, V3<T> o
 template <class T> struct MaterialEval {
     const Scene<T>& scene;
     const Material<T>& mat;
+    // parameter overrides for derivative evaluation (NULL: look up the material)
+    const Rgb<T>* baseOv = nullptr;
+    const T* roughOv = nullptr;
+    Rgb<T> Base(V2<T> uv) const { return baseOv ? *baseOv : scene.TexLookupRgb(mat.baseColor, uv); }
+    T Rough(V2<T> uv) const { return roughOv ? *roughOv : scene.TexLookupMono(mat.roughness, uv); }
 
     struct Local {  // GenericMaterial.cs:343-352
         Rgb<T> colorTint, specularTint;
@@ -618,11 +623,11 @@ template <class T> struct MaterialEval {
     // GenericMaterial.cs:354-381
     Local ComputeLocalParams(const ShadingContext<T>& c) const {
         Local r;
-        Rgb<T> base = scene.TexLookupRgb(mat.baseColor, c.point.uv);
+        Rgb<T> base = Base(c.point.uv);
         T lum = base.Luminance();
         r.colorTint = lum > T(0) ? (base / lum) : Rgb<T>::White();
         r.specularTint = lerp(mat.specularTint, Rgb<T>::White(), r.colorTint);
-        r.roughness = scene.TexLookupMono(mat.roughness, c.point.uv);
+        r.roughness = Rough(c.point.uv);
         T aspect = std::sqrt(T(1) - mat.anisotropic * T(.9f));
         r.alphaX = std::max(T(.001f), r.roughness * r.roughness / aspect);
         r.alphaY = std::max(T(.001f), r.roughness * r.roughness * aspect);
@@ -732,7 +737,7 @@ template <class T> struct MaterialEval {
     Rgb<T> DiffuseEvaluate(const ShadingContext<T>& c, V3<T> inW) const {
         bool refl = ShouldReflect(c.point, c.outDirWorld, inW);
         V3<T> in = c.ToShading(inW);
-        Rgb<T> base = scene.TexLookupRgb(mat.baseColor, c.point.uv);
+        Rgb<T> base = Base(c.point.uv);
         if (mat.transmitter && !refl) {
             if (SameHemisphere(c.outDir, in)) return Rgb<T>::Black();  // :79-84
             return base / PI<T>();
@@ -976,6 +981,202 @@ template <class T> Rgb<T> RenderPixel(const Scene<T>& sc, const PTParams& P, uin
         prevPdf = bs.Pdf * surv;
     }
     return radiance;
+}
+
+// ------------------------------------------------------------------------------------------
+// Path-replay adjoint (reference gradient).  Replays the path of RenderPixel with the same RNG
+// stream and accumulates dLoss/dtheta with detached sampling: emitter radiance at emitter hits
+// and NEE samples, material parameters through the BSDF at NEE samples, and through each sampled
+// BSDF factor times the radiance collected after it (the path's total radiance minus what was
+// collected up to that vertex).  BSDF derivatives are central differences in the template
+// precision (use T = double).
+// ------------------------------------------------------------------------------------------
+template <class T> struct Grads {
+    std::vector<T> tex, matBase, matRough, emitter;
+    std::vector<size_t> texOffset;  // float offset of each texture in the concatenated layout
+};
+
+template <class T> void GradTargets(const Scene<T>& sc, const Grads<T>& G, int matIdx, V2<T> uv, long long& baseTgt, int& roughTgt) {
+    const Material<T>& m = sc.materials[matIdx];
+    baseTgt = -1;
+    if (m.baseColor.tex >= 0) {
+        const Texture<T>& t = sc.textures[m.baseColor.tex];
+        if (t.channels == 3) {
+            int col, row; t.Texel(uv, col, row);
+            baseTgt = (long long)(G.texOffset[m.baseColor.tex] + (size_t(row) * t.w + col) * 3);
+        }
+    } else {
+        baseTgt = -(long long)(matIdx + 2);
+    }
+    roughTgt = (m.type == MAT_GENERIC && m.roughness.tex < 0) ? matIdx : -1;
+}
+template <class T> void AddBase(Grads<T>& G, long long tgt, Rgb<T> g) {
+    if (tgt >= 0) { G.tex[tgt] += g.r; G.tex[tgt + 1] += g.g; G.tex[tgt + 2] += g.b; }
+    else if (tgt <= -2) { size_t m = size_t(-tgt - 2); G.matBase[3 * m] += g.r; G.matBase[3 * m + 1] += g.g; G.matBase[3 * m + 2] += g.b; }
+}
+
+// BSDF value (no cosine) and its derivatives with respect to base r, g, b and roughness.
+template <class T> void BsdfDeriv(const Scene<T>& sc, const Material<T>& mat, const ShadingContext<T>& ctx, V3<T> inW, Rgb<T>& f, Rgb<T> d[4]) {
+    Rgb<T> base = sc.TexLookupRgb(mat.baseColor, ctx.point.uv);
+    T rough = sc.TexLookupMono(mat.roughness, ctx.point.uv);
+    auto eval = [&](Rgb<T> b, T r) {
+        MaterialEval<T> me{sc, mat, &b, &r};
+        if (mat.type == MAT_GENERIC) {
+            Rgb<T> v; T p, pr;
+            me.GenericValueAndPdf(ctx, ctx.ToShading(inW), me.ComputeLocalParams(ctx), v, p, pr, nullptr);
+            return v;
+        }
+        return me.DiffuseEvaluate(ctx, inW);
+    };
+    f = eval(base, rough);
+    const T h = T(1e-6);
+    for (int k = 0; k < 3; ++k) {
+        Rgb<T> bp = base, bm = base;
+        (k == 0 ? bp.r : k == 1 ? bp.g : bp.b) += h;
+        (k == 0 ? bm.r : k == 1 ? bm.g : bm.b) -= h;
+        d[k] = (eval(bp, rough) - eval(bm, rough)) / (T(2) * h);
+    }
+    if (mat.type == MAT_GENERIC && mat.roughness.tex < 0) d[3] = (eval(base, rough + h) - eval(base, rough - h)) / (T(2) * h);
+    else d[3] = Rgb<T>::Black();
+}
+template <class T> T dotc(Rgb<T> a, Rgb<T> b) { return a.r * b.r + a.g * b.g + a.b * b.b; }
+
+template <class T> T EmittedScale(const Emitter<T>& e, const SurfacePoint<T>& p, V3<T> dir) {
+    if (!e.glossy()) return dot(p.shadingNormal, dir) < T(0) ? T(0) : T(1);
+    T c = dot(p.shadingNormal, dir) / length(dir);
+    if (c < T(0)) return T(0);
+    return std::pow(c, e.exponent) * e.normalization;
+}
+
+template <class T> void AdjointPixel(const Scene<T>& sc, const PTParams& P, uint32_t row, uint32_t col, Rng rng, Rgb<T> Ltot, Rgb<T> delta,
+                                     Grads<T>& G) {
+    const int nEm = int(sc.emitters.size());
+    const T nShadow = T(P.numShadowRays);
+    V2<float> off = rng.NextFloat2D();
+    V2<T> film(T(float(col) + off.x), T(float(row) + off.y));
+    Ray<T> ray;
+    sc.camera.GenerateRay(film, ray.org, ray.dir);
+    Rgb<T> prefix = Rgb<T>::White(), approx = Rgb<T>::White();
+    uint32_t depth = 1;
+    SurfacePoint<T> prevHit;
+    T prevPdf = 0;
+    Rgb<T> radiance = Rgb<T>::Black();
+    bool havePending = false;
+    Rgb<T> pendD[4];
+    long long pendBase = -1;
+    int pendRough = -1;
+    auto applyPending = [&]() {
+        if (!havePending) return;
+        Rgb<T> w = delta * (Ltot - radiance);
+        // pendD[k] holds d ln f_c / d theta_k over the colour channels c
+        AddBase(G, pendBase, Rgb<T>(dotc(w, pendD[0]), dotc(w, pendD[1]), dotc(w, pendD[2])));
+        if (pendRough >= 0) G.matRough[pendRough] += dotc(w, pendD[3]);
+        havePending = false;
+    };
+    while (int(depth) <= P.maxDepth) {
+        SurfacePoint<T> hit = sc.Trace(ray);
+        // the previous vertex's sampled BSDF factor: everything not yet collected lies after it
+        applyPending();
+        if (!hit.valid) {
+            if (int(depth) >= P.minDepth && sc.env && P.enableBsdfDI) {
+                T mis = T(1);
+                if (depth > 1) mis = T(1) / (T(1) + sc.env->DirectionPdf(ray.dir) * nShadow / prevPdf);
+                radiance = radiance + prefix * mis * sc.env->EmittedRadiance(ray.dir);
+            }
+            break;
+        }
+        ShadingContext<T> ctx(hit, -ray.dir);
+        const Material<T>& mat = sc.materials[sc.meshes[hit.mesh].material];
+        MaterialEval<T> me{sc, mat};
+        int emIdx = sc.triEmitter[sc.meshTriOffset[hit.mesh] + hit.prim];
+        if (emIdx >= 0 && int(depth) >= P.minDepth) {
+            const Emitter<T>& light = sc.emitters[emIdx];
+            T mis = T(1);
+            if (depth > 1) {
+                T jac = SurfaceAreaToSolidAngle(prevHit, hit);
+                T pdfNE = light.invArea / T(nEm) * nShadow / jac;
+                mis = T(1) / (pdfNE / prevPdf + T(1));
+                if (!P.enableBsdfDI) mis = T(0);
+            }
+            radiance = radiance + prefix * mis * light.EmittedRadiance(hit, -ray.dir);
+            Rgb<T> ge = delta * prefix * (mis * EmittedScale(light, hit, -ray.dir));
+            G.emitter[3 * emIdx] += ge.r; G.emitter[3 * emIdx + 1] += ge.g; G.emitter[3 * emIdx + 2] += ge.b;
+        }
+        long long baseTgt; int roughTgt;
+        GradTargets(sc, G, sc.meshes[hit.mesh].material, hit.uv, baseTgt, roughTgt);
+        T surv = depth > 4 ? std::clamp(approx.Average(), T(0.05f), T(0.95f)) : T(1);
+        if (T(rng.NextFloat()) > surv || int(depth) == P.maxDepth) break;
+        if (int(depth) + 1 >= P.minDepth) {
+            for (int i = 0; i < P.numShadowRays; ++i) {
+                if (sc.env) {
+                    V2<float> u2 = rng.NextFloat2D();
+                    BackgroundSample<T> bs = sc.env->SampleDirection(V2<T>(T(u2.x), T(u2.y)));
+                    if (sc.LeavesScene(hit, bs.Direction)) {
+                        Rgb<T> bsdfCos = me.EvaluateWithCosine(ctx, bs.Direction);
+                        T pdfBsdf, pr; me.Pdf(ctx, bs.Direction, pdfBsdf, pr);
+                        if (!(pdfBsdf == T(0) || bs.Pdf == T(0))) {
+                            T mis = P.enableBsdfDI ? T(1) / (T(1) + pdfBsdf / (bs.Pdf * nShadow)) : T(1);
+                            Rgb<T> val = prefix * (mis * (bs.Weight * bsdfCos / nShadow)) / surv;
+                            radiance = radiance + val;
+                            Rgb<T> f, d[4];
+                            BsdfDeriv(sc, mat, ctx, bs.Direction, f, d);
+                            Rgb<T> coef = delta * prefix * (mis * bs.Weight / nShadow) / surv * std::fabs(ctx.ToShading(bs.Direction).z);
+                            AddBase(G, baseTgt, Rgb<T>(dotc(coef, d[0]), dotc(coef, d[1]), dotc(coef, d[2])));
+                            if (roughTgt >= 0) G.matRough[roughTgt] += dotc(coef, d[3]);
+                        }
+                    }
+                }
+                if (nEm > 0) {
+                    int idx = int(rng.NextInt(uint32_t(nEm)));
+                    const Emitter<T>& light = sc.emitters[idx];
+                    T selProb = T(1) / T(nEm);
+                    V2<float> u2 = rng.NextFloat2D();
+                    SurfacePoint<T> lp = SampleEmitterArea(sc, light, V2<T>(T(u2.x), T(u2.y)));
+                    V3<T> l2s = normalize(hit.position - lp.position);
+                    if (!sc.IsOccluded(hit, lp)) {
+                        Rgb<T> em = light.EmittedRadiance(lp, l2s);
+                        T jac = SurfaceAreaToSolidAngle(hit, lp);
+                        Rgb<T> bsdfCos = me.EvaluateWithCosine(ctx, -l2s);
+                        T pdfNE = light.invArea * selProb * nShadow;
+                        T pdfBsdfSA, pr; me.Pdf(ctx, -l2s, pdfBsdfSA, pr);
+                        if (jac != T(0)) {
+                            T mis = P.enableBsdfDI ? T(1) / (pdfBsdfSA * jac / pdfNE + T(1)) : T(1);
+                            T pdf = light.invArea / jac * selProb * nShadow;
+                            Rgb<T> val = prefix * (mis * (em / pdf * bsdfCos)) / surv;
+                            radiance = radiance + val;
+                            Rgb<T> f, d[4];
+                            BsdfDeriv(sc, mat, ctx, -l2s, f, d);
+                            Rgb<T> coef = delta * prefix * (mis * em / pdf) / surv * std::fabs(ctx.ToShading(-l2s).z);
+                            AddBase(G, baseTgt, Rgb<T>(dotc(coef, d[0]), dotc(coef, d[1]), dotc(coef, d[2])));
+                            if (roughTgt >= 0) G.matRough[roughTgt] += dotc(coef, d[3]);
+                            Rgb<T> ge = delta * prefix * (mis * EmittedScale(light, lp, l2s) / pdf) * bsdfCos / surv;
+                            G.emitter[3 * idx] += ge.r; G.emitter[3 * idx + 1] += ge.g; G.emitter[3 * idx + 2] += ge.b;
+                        }
+                    }
+                }
+            }
+        }
+        T uc = T(rng.NextFloat());
+        V2<float> up = rng.NextFloat2D();
+        BsdfSample<T> bs = me.Sample(ctx, uc, V2<T>(T(up.x), T(up.y)));
+        if (bs.Pdf == T(0) || bs.Weight.IsBlack()) break;
+        {
+            Rgb<T> f, d[4];
+            BsdfDeriv(sc, mat, ctx, bs.Direction, f, d);
+            Rgb<T> inv(f.r != T(0) ? T(1) / f.r : T(0), f.g != T(0) ? T(1) / f.g : T(0), f.b != T(0) ? T(1) / f.b : T(0));
+            for (int k = 0; k < 4; ++k) pendD[k] = d[k] * inv;
+            pendBase = baseTgt;
+            pendRough = roughTgt;
+            havePending = true;
+        }
+        ray = Scene<T>::SpawnRay(hit, bs.Direction);
+        prefix = prefix * (bs.Weight / surv);
+        approx = approx * (bs.Weight / surv);
+        depth++;
+        prevHit = hit;
+        prevPdf = bs.Pdf * surv;
+    }
+    applyPending();
 }
 
 }  // namespace ora

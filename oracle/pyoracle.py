@@ -73,6 +73,7 @@ def lib():
         L.ora_emitter_sample.argtypes = [vp, i, f, f, vp]
         L.ora_emitter_radiance.argtypes = [vp, i, vp, vp, vp]
         L.ora_query_emitter.argtypes = [vp, i, i]
+        L.ora_adjoint.argtypes = [vp, ctypes.POINTER(PTParams), vp, vp, vp, vp, vp, i]
         _lib = L
     return _lib
 
@@ -265,6 +266,22 @@ class OracleScene:
 
     def query_emitter(self, mesh, face):
         return int(self.L.ora_query_emitter(self.h, int(mesh), int(face)))
+
+    def adjoint(self, params, dldi, n_tex, n_mat, n_em, nthreads=None):
+        """FP64 path-replay reference gradient (scene must be fp64)."""
+        nthreads = nthreads or os.cpu_count() or 1
+        d = f32(dldi)
+        out = {"textures": np.zeros(max(n_tex, 1)), "materialBaseColor": np.zeros(max(3 * n_mat, 1)),
+               "materialRoughness": np.zeros(max(n_mat, 1)), "emitterRadiance": np.zeros(max(3 * n_em, 1))}
+        rc = self.L.ora_adjoint(self.h, ctypes.byref(params), _p(d), _p(out["textures"]), _p(out["materialBaseColor"]),
+                                _p(out["materialRoughness"]), _p(out["emitterRadiance"]), int(nthreads))
+        if rc != 0:
+            raise RuntimeError("oracle adjoint needs an fp64 scene")
+        out["textures"] = out["textures"][:n_tex]
+        out["materialBaseColor"] = out["materialBaseColor"][:3 * n_mat].reshape(-1, 3)
+        out["materialRoughness"] = out["materialRoughness"][:n_mat]
+        out["emitterRadiance"] = out["emitterRadiance"][:3 * n_em].reshape(-1, 3)
+        return out
 
     def num_emitters(self):
         return int(self.L.ora_num_emitters(self.h))

@@ -63,6 +63,11 @@ class SstRenderStats(ctypes.Structure):
                 ("numNanOrInf", ctypes.c_uint64), ("nanPixel", ctypes.c_int32 * 4), ("nanIteration", ctypes.c_int32 * 4)]
 
 
+class SstGradients(ctypes.Structure):
+    _fields_ = [("textures", ctypes.c_void_p), ("materialBaseColor", ctypes.c_void_p), ("materialRoughness", ctypes.c_void_p),
+                ("emitterRadiance", ctypes.c_void_p), ("memory", ctypes.c_int32), ("reserved", ctypes.c_int32)]
+
+
 class SstRenderJob(ctypes.Structure):
     _fields_ = [("scene", ctypes.c_void_p), ("params", SstPathTracerParams), ("film", ctypes.c_void_p), ("memory", ctypes.c_int32),
                 ("reserved", ctypes.c_int32)]
@@ -97,6 +102,9 @@ SIGNATURES = {
     "sst_occluded": [_vp, _vp, _i32, _vp, _i32],
     "sst_render": [_vp, _P(SstPathTracerParams), _vp, _i32, _P(SstRenderStats)],
     "sst_render_batch": [_vp, _P(SstRenderJob), _i32, _P(SstRenderStats)],
+    "sst_scene_update_texture": [_vp, _i32, _vp],
+    "sst_forward": [_vp, _P(SstPathTracerParams), _vp, _i32, _P(SstRenderStats)],
+    "sst_backward": [_vp, _P(SstPathTracerParams), _vp, _i32, _P(SstGradients), _P(SstRenderStats)],
     "sst_set_profiling": [_vp, _i32],
     "sst_get_kernel_times": [_vp, _vp, _vp, _vp, _i32],
     "sst_debug_material_eval": [_vp, _i32, _i32, _vp, _vp, _vp, _vp, _vp],
@@ -205,6 +213,7 @@ class SceneHandle:
         check(self.lib.sst_scene_create(ctx.handle, ctypes.byref(h)))
         self.handle = h
         self._textures = {}
+        self.texture_sizes = []   # floats per texture, in id order (the gradient pool's layout)
 
     def close(self):
         if self.handle:
@@ -220,6 +229,7 @@ class SceneHandle:
         out = ctypes.c_int32()
         check(self.lib.sst_scene_add_texture(self.handle, ptr(d), d.shape[1], d.shape[0], d.shape[2], int(border), ctypes.byref(out)))
         self._textures[key] = out.value
+        self.texture_sizes.append(d.size)
         return out.value
 
     def _tex_rgb(self, tex):
@@ -313,6 +323,32 @@ class SceneHandle:
         occ = np.zeros(rays.shape[0], np.int32)
         check(self.lib.sst_occluded(self.handle, ptr(rays), rays.shape[0], ptr(occ), SST_MEM_HOST))
         return occ
+
+    def update_texture(self, tex_id, data):
+        d = np.ascontiguousarray(data, np.float32)
+        check(self.lib.sst_scene_update_texture(self.handle, int(tex_id), ptr(d)))
+
+    def forward(self, params, film, memory=SST_MEM_HOST):
+        stats = SstRenderStats()
+        check(self.lib.sst_forward(self.handle, ctypes.byref(params), ctypes.c_void_p(film), int(memory), ctypes.byref(stats)))
+        return stats
+
+    def backward(self, params, dldi, n_tex, n_mat, n_em, memory=SST_MEM_HOST):
+        """dldi: (H, W, 3) float32 host array.  Returns host gradient arrays and the stats."""
+        d = np.ascontiguousarray(dldi, np.float32)
+        g = SstGradients()
+        out = {"textures": np.zeros(max(n_tex, 1), np.float32), "materialBaseColor": np.zeros(max(3 * n_mat, 1), np.float32),
+               "materialRoughness": np.zeros(max(n_mat, 1), np.float32), "emitterRadiance": np.zeros(max(3 * n_em, 1), np.float32)}
+        g.textures, g.materialBaseColor = out["textures"].ctypes.data, out["materialBaseColor"].ctypes.data
+        g.materialRoughness, g.emitterRadiance = out["materialRoughness"].ctypes.data, out["emitterRadiance"].ctypes.data
+        g.memory = SST_MEM_HOST
+        stats = SstRenderStats()
+        check(self.lib.sst_backward(self.handle, ctypes.byref(params), ptr(d), int(memory), ctypes.byref(g), ctypes.byref(stats)))
+        out["textures"] = out["textures"][:n_tex]
+        out["materialBaseColor"] = out["materialBaseColor"][:3 * n_mat].reshape(-1, 3)
+        out["materialRoughness"] = out["materialRoughness"][:n_mat]
+        out["emitterRadiance"] = out["emitterRadiance"][:3 * n_em].reshape(-1, 3)
+        return out, stats
 
     def render(self, params, film, memory=SST_MEM_HOST):
         stats = SstRenderStats()

@@ -99,6 +99,7 @@ struct sst_ctx {
     DevBuf pathA[9], pathB[9];
     DevBuf hits, nee, shRo, shRd, shTgt, shJob, counters, samples, stats, film;
     DevBuf jobsBuf, chunksBuf, wavesBuf, curWave;
+    DevBuf adjA[3], adjB[3], neeG;
     int cap = 0, shCap = 0, neeSlots = 0;
     size_t sampleCap = 0;
     DevBuf scratchIn, scratchOut, scratchOut2;
@@ -179,6 +180,10 @@ struct sst_scene {
     DevBuf nodes, triv, triN, triAux, triVtx, vnrm, vuv, mats, texs, texData, ems, envImg, envRowCdf, envColCdf, envHasCol, envRowMarg, queryJob;
     DevScene dev{};
     int nTri = 0, nNodes = 0, bvhDepth = 0;
+    // adjoint: per-path radiance of the last sst_forward and its settings
+    DevBuf record, gTex, gMatBase, gMatRough, gEmitter, dLdI;
+    bool recordValid = false;
+    SstPathTracerParams recordParams{};
     std::vector<int> meshTriOffset;
 };
 
@@ -693,6 +698,7 @@ struct JobIn {
     float* dFilm;
     int iterFirst, iterEnd;
     int done = 0;  // iterations rendered
+    DevAdj adj{};  // adjoint buffers (forward record or replay)
 };
 
 // Splits the (job, iteration, pixel) paths into waves of at most `cap` paths.  A job whose
@@ -743,7 +749,7 @@ static void planWaves(std::vector<JobIn>& jobs, int cap, bool iterationPerWave, 
 }
 
 // Renders the jobs' iterations [iterFirst, iterEnd) into their device films.
-static void renderJobs(sst_ctx* c, std::vector<JobIn>& jobs, SstRenderStats* out) {
+static void renderJobs(sst_ctx* c, std::vector<JobIn>& jobs, SstRenderStats* out, bool replay = false) {
     cudaStream_t st = c->stream;
     if (jobs.empty()) return;
     long long totalItems = 0;
@@ -762,12 +768,26 @@ static void renderJobs(sst_ctx* c, std::vector<JobIn>& jobs, SstRenderStats* out
     Wave w;
     ensureWave(c, cap, ns, w);
     c->samples.ensure(size_t(w.wb.cap) * 12);
+    w.wb.a.adjL = w.wb.a.adjD = w.wb.a.adjP = nullptr;
+    w.wb.b.adjL = w.wb.b.adjD = w.wb.b.adjP = nullptr;
+    w.wb.neeG = nullptr;
+    if (replay) {
+        size_t cp = size_t(w.wb.cap);
+        for (int k = 0; k < 2; ++k) { c->adjA[k].ensure(cp * 16); c->adjB[k].ensure(cp * 16); }
+        c->adjA[2].ensure(cp * 48);
+        c->adjB[2].ensure(cp * 48);
+        c->neeG.ensure(cp * 48 * 2 * ns);
+        w.wb.a.adjL = c->adjA[0].as<float4>(); w.wb.a.adjD = c->adjA[1].as<float4>(); w.wb.a.adjP = c->adjA[2].as<float4>();
+        w.wb.b.adjL = c->adjB[0].as<float4>(); w.wb.b.adjD = c->adjB[1].as<float4>(); w.wb.b.adjP = c->adjB[2].as<float4>();
+        w.wb.neeG = c->neeG.as<float4>();
+    }
     // job table
     std::vector<DevJob> hj(jobs.size());
     for (size_t k = 0; k < jobs.size(); ++k) {
         const SstPathTracerParams* P = &jobs[k].p;
         hj[k].sc = jobs[k].s->dev;
         hj[k].cfg = PTConfig{P->width, P->height, P->maxDepth, P->minDepth, P->baseSeed, P->numShadowRays, P->enableBsdfDI, P->ignoreNanAndInf};
+        hj[k].adj = jobs[k].adj;
     }
     std::vector<WaveChunk> chunks;
     std::vector<WaveDesc> waves;
@@ -804,8 +824,8 @@ static void renderJobs(sst_ctx* c, std::vector<JobIn>& jobs, SstRenderStats* out
             }
             {
                 KTimer kt(c, 2);
-                launch_shade(ns, dj, A, B, w.wb.hits, w.wb.nee, w.wb.cap, w.wb.shRo, w.wb.shRd, w.wb.shTgt, w.wb.shJob, cnt + kCntQueue + d,
-                             cnt + kCntQueue + d + 1, cnt + kCntShadow + d, c->samples.as<float>(), dstats, maxItems, st);
+                launch_shade(ns, replay, dj, A, B, w.wb.hits, w.wb.nee, w.wb.neeG, w.wb.cap, w.wb.shRo, w.wb.shRd, w.wb.shTgt, w.wb.shJob,
+                             cnt + kCntQueue + d, cnt + kCntQueue + d + 1, cnt + kCntShadow + d, c->samples.as<float>(), dstats, maxItems, st);
             }
             {
                 KTimer kt(c, 3);
@@ -823,7 +843,7 @@ static void renderJobs(sst_ctx* c, std::vector<JobIn>& jobs, SstRenderStats* out
         }
         {
             KTimer kt(c, 4);
-            launch_film_fold(dj, dch, dwv, dcur, c->samples.as<float>(), dstats, allowEarlyExit ? maxFold : maxFold, 1, st);
+            launch_film_fold(dj, dch, dwv, dcur, replay ? nullptr : c->samples.as<float>(), dstats, maxFold, 1, st);
         }
     };
 
@@ -1355,6 +1375,113 @@ int sst_render_batch(sst_ctx* ctx, const SstRenderJob* jobs, int32_t numJobs, Ss
         for (auto& j : in) it += j.done;
         total.numIterations = it;
         if (stats) *stats = total;
+    });
+}
+
+int sst_scene_update_texture(sst_scene* s, int32_t texture, const float* data) {
+    return guarded([&] {
+        if (!s || !data || texture < 0 || texture >= int(s->textures.size())) fail(SST_ERR_INVALID_ARGUMENT, "invalid texture");
+        HostTexture& t = s->textures[texture];
+        std::copy(data, data + t.data.size(), t.data.begin());
+        if (s->committed) {
+            size_t off = 0;
+            for (int k = 0; k < texture; ++k) off += s->textures[k].data.size();
+            CUDA_CHECK(cudaMemcpyAsync(s->texData.as<float>() + off, t.data.data(), sizeof(float) * t.data.size(), cudaMemcpyHostToDevice,
+                                       s->ctx->stream));
+            CUDA_CHECK(cudaStreamSynchronize(s->ctx->stream));
+        }
+    });
+}
+
+static size_t texPoolFloats(const sst_scene* s) {
+    size_t n = 0;
+    for (auto& t : s->textures) n += t.data.size();
+    return n;
+}
+
+int sst_forward(sst_scene* s, const SstPathTracerParams* p, float* film, int32_t memory, SstRenderStats* stats) {
+    return guarded([&] {
+        if (!s || !p || !film) fail(SST_ERR_INVALID_ARGUMENT, "NULL argument");
+        checkParams(s, p);
+        if (p->firstIteration != 0 || p->maximumRenderTimeMs > 0) fail(SST_ERR_UNSUPPORTED, "sst_forward renders all iterations from zero");
+        sst_ctx* c = s->ctx;
+        CUDA_CHECK(cudaSetDevice(c->device));
+        size_t P = size_t(p->width) * p->height;
+        s->record.ensure(std::max<size_t>(1, P * size_t(p->totalSpp) * 12));
+        SstRenderStats local{};
+        for (int k = 0; k < 4; ++k) { local.nanPixel[k] = -1; local.nanIteration[k] = -1; }
+        size_t filmBytes = P * 3 * sizeof(float);
+        float* dFilm = film;
+        if (memory != SST_MEM_DEVICE) {
+            c->film.ensure(filmBytes);
+            dFilm = c->film.as<float>();
+        }
+        CUDA_CHECK(cudaMemsetAsync(dFilm, 0, filmBytes, c->stream));
+        std::vector<JobIn> jobs(1);
+        jobs[0].s = s;
+        jobs[0].p = *p;
+        jobs[0].dFilm = dFilm;
+        jobs[0].iterFirst = 0;
+        jobs[0].iterEnd = p->totalSpp;
+        jobs[0].adj.record = s->record.as<float>();
+        renderJobs(c, jobs, &local);
+        if (memory != SST_MEM_DEVICE) CUDA_CHECK(cudaMemcpy(film, dFilm, filmBytes, cudaMemcpyDeviceToHost));
+        s->recordValid = true;
+        s->recordParams = *p;
+        if (stats) *stats = local;
+    });
+}
+
+int sst_backward(sst_scene* s, const SstPathTracerParams* p, const float* dLdI, int32_t memory, SstGradients* g, SstRenderStats* stats) {
+    return guarded([&] {
+        if (!s || !p || !dLdI || !g) fail(SST_ERR_INVALID_ARGUMENT, "NULL argument");
+        checkParams(s, p);
+        const SstPathTracerParams& r = s->recordParams;
+        if (!s->recordValid || r.width != p->width || r.height != p->height || r.totalSpp != p->totalSpp || r.maxDepth != p->maxDepth ||
+            r.minDepth != p->minDepth || r.baseSeed != p->baseSeed || r.numShadowRays != p->numShadowRays || r.enableBsdfDI != p->enableBsdfDI)
+            fail(SST_ERR_INVALID_ARGUMENT, "sst_backward needs a preceding sst_forward with the same parameters");
+        sst_ctx* c = s->ctx;
+        cudaStream_t st = c->stream;
+        CUDA_CHECK(cudaSetDevice(c->device));
+        size_t P = size_t(p->width) * p->height;
+        const float* dG = toDevice(c, s->dLdI, dLdI, P * 3, memory);
+        size_t nTex = texPoolFloats(s), nMat = s->materials.size(), nEm = s->emitters.size();
+        s->gTex.ensure(std::max<size_t>(1, nTex * 4));
+        s->gMatBase.ensure(std::max<size_t>(1, nMat * 12));
+        s->gMatRough.ensure(std::max<size_t>(1, nMat * 4));
+        s->gEmitter.ensure(std::max<size_t>(1, nEm * 12));
+        CUDA_CHECK(cudaMemsetAsync(s->gTex.p, 0, std::max<size_t>(1, nTex * 4), st));
+        CUDA_CHECK(cudaMemsetAsync(s->gMatBase.p, 0, std::max<size_t>(1, nMat * 12), st));
+        CUDA_CHECK(cudaMemsetAsync(s->gMatRough.p, 0, std::max<size_t>(1, nMat * 4), st));
+        CUDA_CHECK(cudaMemsetAsync(s->gEmitter.p, 0, std::max<size_t>(1, nEm * 12), st));
+        SstRenderStats local{};
+        for (int k = 0; k < 4; ++k) { local.nanPixel[k] = -1; local.nanIteration[k] = -1; }
+        std::vector<JobIn> jobs(1);
+        jobs[0].s = s;
+        jobs[0].p = *p;
+        jobs[0].p.firstIteration = 0;
+        jobs[0].dFilm = nullptr;
+        jobs[0].iterFirst = 0;
+        jobs[0].iterEnd = p->totalSpp;
+        DevAdj& a = jobs[0].adj;
+        a.record = s->record.as<float>();
+        a.dLdI = dG;
+        a.invSpp = 1.0f / float(std::max(1, p->totalSpp));
+        a.gTex = s->gTex.as<float>();
+        a.gMatBase = s->gMatBase.as<float>();
+        a.gMatRough = s->gMatRough.as<float>();
+        a.gEmitter = s->gEmitter.as<float>();
+        renderJobs(c, jobs, &local, true);
+        auto out = [&](float* dst, const DevBuf& src, size_t n) {
+            if (!dst || n == 0) return;
+            CUDA_CHECK(cudaMemcpyAsync(dst, src.p, n * 4, g->memory == SST_MEM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, st));
+        };
+        out(g->textures, s->gTex, nTex);
+        out(g->materialBaseColor, s->gMatBase, nMat * 3);
+        out(g->materialRoughness, s->gMatRough, nMat);
+        out(g->emitterRadiance, s->gEmitter, nEm * 3);
+        CUDA_CHECK(cudaStreamSynchronize(st));
+        if (stats) *stats = local;
     });
 }
 

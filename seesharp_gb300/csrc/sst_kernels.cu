@@ -8,6 +8,7 @@
 #include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
+#include "sst_adjoint.cuh"
 #include "sst_device.cuh"
 #include "sst_kernels.h"
 
@@ -97,6 +98,18 @@ __global__ void __launch_bounds__(256) k_camera(const DevJob* __restrict__ jobs,
     A.rad[i] = make_float4(0.f, 0.f, 0.f, 0.f);
     A.ro[i] = make_float4(org.x, org.y, org.z, 0.f);
     A.rd[i] = make_float4(dir.x, dir.y, dir.z, CUDART_INF_F);
+    if (A.adjL) {
+        // adjoint replay: the path's radiance from the forward pass and dLoss/dSample of its pixel
+        const DevAdj& adj = jb.adj;
+        size_t P = (size_t)jb.cfg.W * jb.cfg.H;
+        const float* L = adj.record + 3 * ((size_t)iter * P + pix);
+        float3 Lt = mk(L[0], L[1], L[2]);
+        const float* g = adj.dLdI + 3 * (size_t)pix;
+        float3 d = mk(g[0], g[1], g[2]) * adj.invSpp;
+        if (!isfinite(avg3(Lt))) { Lt = mk(0, 0, 0); d = mk(0, 0, 0); }  // the film dropped this sample
+        A.adjL[i] = make_float4(Lt.x, Lt.y, Lt.z, __int_as_float(-1));
+        A.adjD[i] = make_float4(d.x, d.y, d.z, __int_as_float(-1));
+    }
 }
 
 // =============================================================================================
@@ -108,7 +121,7 @@ __global__ void k_film_fold(const DevJob* __restrict__ jobs, const WaveChunk* __
                             const float* samples, DevStats* st, int advance) {
     const WaveDesc wd = waves[*curWave];
     int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t < wd.foldThreads) {
+    if (samples && t < wd.foldThreads) {
         // chunk of this fold thread (sorted by foldOffset as well)
         int lo = wd.chunkBegin, hi = wd.chunkEnd;
         while (hi - lo > 1) {
@@ -125,6 +138,11 @@ __global__ void k_film_fold(const DevJob* __restrict__ jobs, const WaveChunk* __
             uint32_t iter = (uint32_t)(ck.iterBase + m);
             const float* s = samples + 3 * ((size_t)ck.itemOffset + (size_t)m * ck.pixCount + p);
             float3 v = mk(s[0], s[1], s[2]);
+            float* rec = jobs[ck.job].adj.record;
+            if (rec) {  // forward pass of the adjoint: keep every path's radiance
+                float* r = rec + 3 * ((size_t)iter * cfg.W * cfg.H + pix);
+                r[0] = v.x; r[1] = v.y; r[2] = v.z;
+            }
             float kf = (float)(iter + 1);
             if (iter > 0) cur = cur * ((kf - 1.0f) / kf);
             float a = avg3(v);
@@ -362,11 +380,20 @@ SST_D int aggAppend(int* counter) {
     return g.shfl(base, 0) + (int)g.thread_rank();
 }
 
-template <int NS>
+// ADJ = true: path-replay adjoint.  The same decisions as the forward pass (same code, same
+// RNG stream); in addition the pass accumulates parameter gradients with detached sampling:
+//   - at an emitter hit: d/d radiance of prefix * mis * Le;
+//   - at each NEE sample: d/d(material parameters) and d/d radiance of the contribution, applied
+//     once the shadow ray has found the sample visible (payload in neeG);
+//   - for the sampled BSDF factor f_k: d ln f_k / d(theta) times the radiance collected after it,
+//     which is the forward pass's path radiance minus what has been collected up to vertex k
+//     (applied at the next vertex, after that vertex has resolved vertex k's NEE).
+// Every term is weighted by dLoss/dSample of the path's pixel.
+template <int NS, bool ADJ>
 __global__ void __launch_bounds__(128, SST_SHADE_MIN_BLOCKS) k_shade(const DevJob* __restrict__ jobs, PathBuf A, PathBuf B,
-                                                                   const float4* __restrict__ hits, float4* nee, int cap, float4* shRo,
-                                                                   float4* shRd, int* shTgt, uint32_t* shJob, const int* nIn, int* nOut,
-                                                                   int* nSh, float* samples, DevStats* stats) {
+                                                                   const float4* __restrict__ hits, float4* nee, float4* neeG, int cap,
+                                                                   float4* shRo, float4* shRd, int* shTgt, uint32_t* shJob, const int* nIn,
+                                                                   int* nOut, int* nSh, float* samples, DevStats* stats) {
     const int n = *nIn;
     if ((int)(blockIdx.x * blockDim.x) >= n) return;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -385,6 +412,12 @@ __global__ void __launch_bounds__(128, SST_SHADE_MIN_BLOCKS) k_shade(const DevJo
     float3 shC[2 * NS];
     uint32_t pend = 0;
     int queries = 0;
+    // adjoint state
+    float3 adjLt = mk(0, 0, 0), adjDl = mk(0, 0, 0);
+    int vBaseTgt = -1, vRoughTgt = -1;   // targets of this vertex (for the factor left pending)
+    float4 fP[3] = {};                   // d ln f_c / d theta of this vertex's sampled BSDF factor
+    bool factorPending = false;
+    float4 shG[ADJ ? 2 * NS : 1][3];
 
     if (valid) {
         job = A.job[i];
@@ -398,11 +431,42 @@ __global__ void __launch_bounds__(128, SST_SHADE_MIN_BLOCKS) k_shade(const DevJo
         prefix = f3(pw);
         float prevPdf = pw.w;
         radiance = f3(rad4);
+        const DevAdj& adj = jobs[job].adj;
         // resolve the NEE of the previous bounce (PathTracer.cs:363) in slot order
         uint32_t pm = (dw >> kNeeShift) & 0xFFu;
+        if (ADJ) {
+            float4 l4 = A.adjL[i], d4 = A.adjD[i];
+            adjLt = f3(l4);
+            adjDl = f3(d4);
 #pragma unroll
-        for (int k = 0; k < 2 * NS; ++k)
-            if (pm & (1u << k)) radiance = radiance + f3(nee[(size_t)k * cap + i]);
+            for (int k = 0; k < 2 * NS; ++k) {
+                if (!(pm & (1u << k))) continue;
+                size_t slot = (size_t)k * cap + i;
+                float4 nv = nee[slot];
+                if (nv.w == 0.0f) continue;  // occluded
+                radiance = radiance + f3(nv);
+                float4 g0 = neeG[3 * slot], g1 = neeG[3 * slot + 1], g2 = neeG[3 * slot + 2];
+                addBaseGrad(adj, __float_as_int(g0.x), g0.y, g0.z, g0.w);
+                addRoughGrad(adj, __float_as_int(g1.x), g1.y);
+                addEmitterGrad(adj, __float_as_int(g1.z), f3(g2));
+            }
+            // the sampled-BSDF factor of the previous vertex: d ln f * radiance collected after it
+            if (dw & kAdjFactorFlag) {
+                float3 fut = adjLt - radiance;
+                float3 w3 = adjDl * fut;
+                float4 p0 = A.adjP[3 * (size_t)i], p1 = A.adjP[3 * (size_t)i + 1], p2 = A.adjP[3 * (size_t)i + 2];
+                float gb0 = w3.x * p0.x + w3.y * p1.x + w3.z * p2.x;
+                float gb1 = w3.x * p0.y + w3.y * p1.y + w3.z * p2.y;
+                float gb2 = w3.x * p0.z + w3.y * p1.z + w3.z * p2.z;
+                float gr = w3.x * p0.w + w3.y * p1.w + w3.z * p2.w;
+                addBaseGrad(adj, __float_as_int(l4.w), gb0, gb1, gb2);
+                addRoughGrad(adj, __float_as_int(d4.w), gr);
+            }
+        } else {
+#pragma unroll
+            for (int k = 0; k < 2 * NS; ++k)
+                if (pm & (1u << k)) radiance = radiance + f3(nee[(size_t)k * cap + i]);
+        }
         const uint32_t depth = dw & kDepthMask;
         bool terminate = false;
         if (dw & kDoneFlag) {
@@ -480,6 +544,15 @@ __global__ void __launch_bounds__(128, SST_SHADE_MIN_BLOCKS) k_shade(const DevJo
                         if (!cfg.enableBsdfDI) mis = 0.0f;
                     }
                     radiance = radiance + prefix * mis * emitted(em, s.sn, -rdir);
+                    if (ADJ) addEmitterGrad(adj, emIdx, adjDl * prefix * (mis * emittedScale(em, s.sn, -rdir)));
+                }
+                // adjoint: parameter values and gradient targets of this shading point
+                float3 baseV = mk(0, 0, 0);
+                float roughV = 0.0f;
+                if (ADJ) {
+                    baseV = lookupRgb(sc, m.baseTex, m.base, s.uv);
+                    roughV = m.type == kGeneric ? lookupMono(sc, m.roughTex, m.rough, s.uv) : 1.0f;
+                    gradTargets(sc, s.mat, s.uv, vBaseTgt, vRoughTgt);
                 }
 
                 // Russian roulette (PathTracer.cs:277-282, :352-354)
@@ -506,6 +579,17 @@ __global__ void __launch_bounds__(128, SST_SHADE_MIN_BLOCKS) k_shade(const DevJo
                                     float3 val = neeScale * (mis * contrib) / surv;
                                     if (!isBlack(val)) {
                                         int k = 2 * sIt;
+                                        if (ADJ) {
+                                            // d val / d(material): prefix * mis * weight / ns / surv * |cos| * df
+                                            float3 coef = adjDl * neeScale * (mis * ew / (float)cfg.numShadowRays) / surv * fabsf(c.f.toLocal(ed).z);
+                                            Dl3 df = bsdfDeriv(m, baseV, roughV, c, ed);
+                                            shG[k][0] = make_float4(__int_as_float(vBaseTgt), coef.x * df.x.d[0] + coef.y * df.y.d[0] + coef.z * df.z.d[0],
+                                                                    coef.x * df.x.d[1] + coef.y * df.y.d[1] + coef.z * df.z.d[1],
+                                                                    coef.x * df.x.d[2] + coef.y * df.y.d[2] + coef.z * df.z.d[2]);
+                                            shG[k][1] = make_float4(__int_as_float(vRoughTgt), coef.x * df.x.d[3] + coef.y * df.y.d[3] + coef.z * df.z.d[3],
+                                                                    __int_as_float(-1), 0.f);
+                                            shG[k][2] = make_float4(0.f, 0.f, 0.f, 0.f);
+                                        }
                                         int q = aggAppend(nSh);
                                         shJob[q] = job;
                                         float3 o = offsetPoint(s.pos, s.n, s.eps, ed);
@@ -547,6 +631,17 @@ __global__ void __launch_bounds__(128, SST_SHADE_MIN_BLOCKS) k_shade(const DevJo
                                     float3 val = neeScale * (mis * contrib) / surv;
                                     if (!isBlack(val)) {
                                         int k = 2 * sIt + 1;
+                                        if (ADJ) {
+                                            float3 coef = adjDl * neeScale * (mis * emis / pdf) / surv * fabsf(c.f.toLocal(-l2s).z);
+                                            Dl3 df = bsdfDeriv(m, baseV, roughV, c, -l2s);
+                                            float3 ge = adjDl * neeScale * (mis * emittedScale(em, lpSn, l2s) / pdf) * bc / surv;
+                                            shG[k][0] = make_float4(__int_as_float(vBaseTgt), coef.x * df.x.d[0] + coef.y * df.y.d[0] + coef.z * df.z.d[0],
+                                                                    coef.x * df.x.d[1] + coef.y * df.y.d[1] + coef.z * df.z.d[1],
+                                                                    coef.x * df.x.d[2] + coef.y * df.y.d[2] + coef.z * df.z.d[2]);
+                                            shG[k][1] = make_float4(__int_as_float(vRoughTgt), coef.x * df.x.d[3] + coef.y * df.y.d[3] + coef.z * df.z.d[3],
+                                                                    __int_as_float(idx), 0.f);
+                                            shG[k][2] = make_float4(ge.x, ge.y, ge.z, 0.f);
+                                        }
                                         int q = aggAppend(nSh);
                                         shJob[q] = job;
                                         float3 dd = lpPos - s.pos;
@@ -573,6 +668,16 @@ __global__ void __launch_bounds__(128, SST_SHADE_MIN_BLOCKS) k_shade(const DevJo
                         else terminate = true;
                     } else {
                         cont = true;
+                        if (ADJ) {
+                            Dl3 df = bsdfDeriv(m, baseV, roughV, c, dirW);
+                            float ix = df.x.v != 0.0f ? 1.0f / df.x.v : 0.0f;
+                            float iy = df.y.v != 0.0f ? 1.0f / df.y.v : 0.0f;
+                            float iz = df.z.v != 0.0f ? 1.0f / df.z.v : 0.0f;
+                            fP[0] = make_float4(df.x.d[0] * ix, df.x.d[1] * ix, df.x.d[2] * ix, df.x.d[3] * ix);
+                            fP[1] = make_float4(df.y.d[0] * iy, df.y.d[1] * iy, df.y.d[2] * iy, df.y.d[3] * iy);
+                            fP[2] = make_float4(df.z.d[0] * iz, df.z.d[1] * iz, df.z.d[2] * iz, df.z.d[3] * iz);
+                            factorPending = true;
+                        }
                         prefix = prefix * (bw / surv);  // PathTracer.cs:372-378
                         prevPdfOut = bpdf * surv;
                         outDepth = depth + 1;
@@ -583,7 +688,7 @@ __global__ void __launch_bounds__(128, SST_SHADE_MIN_BLOCKS) k_shade(const DevJo
                 }
             }
         }
-        if (terminate) splat(samples, pix, radiance);
+        if (terminate && !ADJ) splat(samples, pix, radiance);
         if (!cont) pend = 0;
     }
     // shadow-query statistics (RayTracerStats.NumShadowRays semantics)
@@ -608,27 +713,47 @@ __global__ void __launch_bounds__(128, SST_SHADE_MIN_BLOCKS) k_shade(const DevJo
     B.prev[j] = make_float4(hitPos.x, hitPos.y, hitPos.z, 0.f);
     B.ro[j] = make_float4(nRo.x, nRo.y, nRo.z, 0.f);
     B.rd[j] = make_float4(nRd.x, nRd.y, nRd.z, (outDepth & kDoneFlag) ? -1.0f : nTmax);
+    if (ADJ) {
+        B.depth[j] = outDepth | (factorPending ? kAdjFactorFlag : 0u);
+        B.adjL[j] = make_float4(adjLt.x, adjLt.y, adjLt.z, __int_as_float(vBaseTgt));
+        B.adjD[j] = make_float4(adjDl.x, adjDl.y, adjDl.z, __int_as_float(vRoughTgt));
+        B.adjP[3 * (size_t)j] = fP[0];
+        B.adjP[3 * (size_t)j + 1] = fP[1];
+        B.adjP[3 * (size_t)j + 2] = fP[2];
+    }
 #pragma unroll
     for (int k = 0; k < 2 * NS; ++k) {
         if (pend & (1u << k)) {
             int slot = k * cap + j;
             shTgt[shIdx[k]] = slot;
-            nee[slot] = make_float4(shC[k].x, shC[k].y, shC[k].z, 0.f);
+            nee[slot] = make_float4(shC[k].x, shC[k].y, shC[k].z, 1.f);
+            if (ADJ) {
+                neeG[3 * (size_t)slot] = shG[k][0];
+                neeG[3 * (size_t)slot + 1] = shG[k][1];
+                neeG[3 * (size_t)slot + 2] = shG[k][2];
+            }
         }
     }
 }
 
-void launch_shade(int ns, const DevJob* jobs, const PathBuf& A, const PathBuf& B, const float4* hits, float4* nee, int cap, float4* shRo,
-                  float4* shRd, int* shTgt, uint32_t* shJob, const int* nIn, int* nOut, int* nSh, float* samples, DevStats* stats, int maxItems,
-                  cudaStream_t s) {
+void launch_shade(int ns, bool adj, const DevJob* jobs, const PathBuf& A, const PathBuf& B, const float4* hits, float4* nee, float4* neeG, int cap,
+                  float4* shRo, float4* shRd, int* shTgt, uint32_t* shJob, const int* nIn, int* nOut, int* nSh, float* samples, DevStats* stats,
+                  int maxItems, cudaStream_t s) {
     int grid = (maxItems + 127) / 128;
     if (grid == 0) return;
+#define SST_SHADE_CASE(N)                                                                                                                    \
+    case N:                                                                                                                                  \
+        if (adj) k_shade<N, true><<<grid, 128, 0, s>>>(jobs, A, B, hits, nee, neeG, cap, shRo, shRd, shTgt, shJob, nIn, nOut, nSh, samples, stats); \
+        else k_shade<N, false><<<grid, 128, 0, s>>>(jobs, A, B, hits, nee, neeG, cap, shRo, shRd, shTgt, shJob, nIn, nOut, nSh, samples, stats); \
+        break;
     switch (ns) {
-        case 1: k_shade<1><<<grid, 128, 0, s>>>(jobs, A, B, hits, nee, cap, shRo, shRd, shTgt, shJob, nIn, nOut, nSh, samples, stats); break;
-        case 2: k_shade<2><<<grid, 128, 0, s>>>(jobs, A, B, hits, nee, cap, shRo, shRd, shTgt, shJob, nIn, nOut, nSh, samples, stats); break;
-        case 3: k_shade<3><<<grid, 128, 0, s>>>(jobs, A, B, hits, nee, cap, shRo, shRd, shTgt, shJob, nIn, nOut, nSh, samples, stats); break;
-        default: k_shade<4><<<grid, 128, 0, s>>>(jobs, A, B, hits, nee, cap, shRo, shRd, shTgt, shJob, nIn, nOut, nSh, samples, stats); break;
+        SST_SHADE_CASE(1)
+        SST_SHADE_CASE(2)
+        SST_SHADE_CASE(3)
+        default:
+        SST_SHADE_CASE(4)
     }
+#undef SST_SHADE_CASE
 }
 
 void launch_camera(const DevJob* jobs, const WaveChunk* chunks, const WaveDesc* waves, const int* curWave, const PathBuf& A, int* qCount,

@@ -89,11 +89,23 @@ struct PTConfig {
     int ignoreNan;
 };
 
+// Path-replay adjoint buffers of a job (all NULL for a plain render).
+struct DevAdj {
+    float* record;        // per (iteration, pixel) path radiance: written by the forward fold, read by the replay
+    const float* dLdI;    // dLoss/dImage (W*H*3) for the replay
+    float invSpp;         // 1 / totalSpp: dImage/dSample
+    float* gTex;          // gradient of the texel pool (layout of DevScene.texData)
+    float* gMatBase;      // 3 per material: constant base colour
+    float* gMatRough;     // 1 per material: constant roughness
+    float* gEmitter;      // 3 per emitter: radiance
+};
+
 // One render job: its scene and path-tracer settings (the kernels index this table by the job
 // id every path carries).
 struct DevJob {
     DevScene sc;
     PTConfig cfg;
+    DevAdj adj;
 };
 
 // A chunk of a wave: nIter consecutive iterations of the pixel range [pixStart, pixStart +
@@ -141,16 +153,22 @@ struct PathBuf {
     float4* prev;      // previous hit position
     float4* ro;        // ray origin, tmin
     float4* rd;        // ray direction, tmax
+    // adjoint replay only (NULL otherwise)
+    float4* adjL;      // path radiance from the forward pass, w = base-colour target (int bits)
+    float4* adjD;      // dLoss/dSample per channel, w = roughness target (int bits)
+    float4* adjP;      // 3 float4 per path: d ln f_c / d(base r, g, b, roughness) of the pending BSDF factor
 };
 
 constexpr uint32_t kDepthMask = 0xFFFFu;
 constexpr int kNeeShift = 16;
 constexpr uint32_t kDoneFlag = 0x80000000u;
+constexpr uint32_t kAdjFactorFlag = 0x40000000u;  // adjoint: a BSDF-factor gradient is pending
 
 struct WaveBuffers {
     PathBuf a, b;
     float4* hits;        // per path of the current queue: t, u, v, leaf triangle (int bits, -1 miss)
-    float4* nee;         // [slot * cap + path]: pending NEE contribution
+    float4* nee;         // [slot * cap + path]: pending NEE contribution, w = 1 until occluded
+    float4* neeG;        // adjoint: 3 float4 per NEE slot, the gradient payload
     float4* shRo;        // shadow queue: origin, tmin
     float4* shRd;        // direction, tmax
     int* shTgt;          // nee slot index

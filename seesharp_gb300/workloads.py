@@ -76,6 +76,32 @@ def cornell_box(width=256, height=256, seed=7):
     return sc
 
 
+def cornell_box_differentiable(width=512, height=512, seed=7, tex_res=256, texture=None, roughness=(0.3, 0.6), radiance=(17, 12, 4)):
+    """The differentiation configuration: the Cornell box with a GenericMaterial back wall whose
+    base colour is a tex_res^2 RGB texture, a GenericMaterial with a scalar roughness on each box,
+    and the ceiling light's RGB radiance.  Returns (scene, texture, box_materials, light_emitters)."""
+    rng = np.random.default_rng(seed)
+    sc = cornell_box(width, height, seed)
+    if texture is None:
+        yy, xx = np.meshgrid(np.linspace(0, 1, tex_res), np.linspace(0, 1, tex_res), indexing="ij")
+        texture = np.stack([0.35 + 0.3 * np.sin(6.0 * xx + 1.0) * np.cos(4.0 * yy), 0.5 + 0.25 * np.cos(5.0 * yy + 0.5),
+                            0.45 + 0.2 * np.sin(3.0 * (xx + yy))], -1) + 0.05 * rng.standard_normal((tex_res, tex_res, 3))
+        texture = np.clip(texture, 0.05, 0.95).astype(np.float32)
+    tex = TextureRgb(RgbImage(np.asarray(texture, np.float32)))
+    back = sc.Meshes[2]
+    back.TextureCoordinates = np.array([[0, 1], [1, 1], [1, 0], [0, 0]], np.float32)
+    back.Material = GenericMaterial(GenericMaterial.Parameters(BaseColor=tex, Roughness=TextureMono(0.8), SpecularTintStrength=0.0))
+    boxes = []
+    for k, mesh in enumerate(sc.Meshes[5:7]):
+        mat = GenericMaterial(GenericMaterial.Parameters(BaseColor=TextureRgb(RgbColor(0.725, 0.725, 0.725)), Roughness=TextureMono(roughness[k]),
+                                                         Metallic=0.3))
+        mesh.Material = mat
+        boxes.append(mat)
+    for e in sc.Emitters:
+        e.Radiance = RgbColor(*radiance)
+    return sc, tex, boxes, list(sc.Emitters)
+
+
 # ---------------------------------------------------------------------------------------------
 # icospheres
 # ---------------------------------------------------------------------------------------------
