@@ -167,6 +167,28 @@ int sst_scene_info(sst_scene* scene, int32_t* numEmitters, int32_t* numTriangles
 int sst_trace(sst_scene* scene, const SstRay* rays, int32_t n, SstHit* hits, int32_t memory);
 int sst_occluded(sst_scene* scene, const SstRay* rays, int32_t n, int32_t* occluded, int32_t memory);
 
+/* ---- allocation-free occlusion query: no counterpart in the reference --------------------------
+ * The same any-hit queries as sst_occluded, with the same arguments and the same results, but the
+ * call allocates no memory: no cudaMalloc or cudaFree, and no allocating CUDA library routine.
+ * sst_occluded allocates its temporary device buffers on every call.  Some callers cannot do that:
+ *  - a caller whose device memory is fully budgeted, e.g. one that shares the GPU with another
+ *    process holding the rest of it, where a new allocation can fail in the middle of a frame;
+ *  - a caller on a latency-bound loop (shadow or picking queries per frame): cudaFree waits for
+ *    the whole device, and cudaMalloc may, which stalls every stream on the GPU, not just this one.
+ * The scratch it uses (split ray arrays, queue counters, job record, ray statistics, result flags)
+ * is one array of 2,360,320 bytes that is part of this library's device code.  Every GPU that
+ * loads the library holds it until the process exits.
+ * Limits and rules:
+ *  - n <= SST_NOALLOC_MAX_RAYS; a larger n returns SST_ERR_INVALID_ARGUMENT and does nothing.
+ *  - The first call on a device looks up the array's device address (cudaGetSymbolAddress).
+ *    Make that first call before any CUDA stream capture begins.
+ *  - All calls on a device share the array, so two calls whose GPU work overlapped would race.
+ *    The function holds a process-wide lock for the whole call and returns only after its GPU
+ *    work has finished, so its own calls in one process never overlap.
+ *  - rays / occluded are host arrays (SST_MEM_HOST) or device arrays (SST_MEM_DEVICE). */
+#define SST_NOALLOC_MAX_RAYS 65536
+int sst_occluded_noalloc(sst_scene* scene, const SstRay* rays, int32_t n, int32_t* occluded, int32_t memory);
+
 /* ---- rendering (PathTracerBase.Render, PathTracer.cs:199-267) -------------------------------- */
 /* Renders iterations [firstIteration, totalSpp) into film (width*height*3 floats, row-major,
  * top row first) with the frame buffer's running mean.  When firstIteration > 0 the film must

@@ -16,6 +16,7 @@ LIB_PATH = os.path.join(HERE, "libsst.so")
 
 SST_MEM_HOST = 0
 SST_MEM_DEVICE = 1
+SST_NOALLOC_MAX_RAYS = 65536  # rays per sst_occluded_noalloc call
 
 _ERRORS = {
     -1: "invalid argument",
@@ -100,6 +101,7 @@ SIGNATURES = {
     "sst_scene_info": [_vp, _P(_i32), _P(_i32), _P(_i32)],
     "sst_trace": [_vp, _vp, _i32, _vp, _i32],
     "sst_occluded": [_vp, _vp, _i32, _vp, _i32],
+    "sst_occluded_noalloc": [_vp, _vp, _i32, _vp, _i32],
     "sst_render": [_vp, _P(SstPathTracerParams), _vp, _i32, _P(SstRenderStats)],
     "sst_render_batch": [_vp, _P(SstRenderJob), _i32, _P(SstRenderStats)],
     "sst_scene_update_texture": [_vp, _i32, _vp],
@@ -322,6 +324,14 @@ class SceneHandle:
         rays = np.ascontiguousarray(rays, np.float32).reshape(-1, 8)
         occ = np.zeros(rays.shape[0], np.int32)
         check(self.lib.sst_occluded(self.handle, ptr(rays), rays.shape[0], ptr(occ), SST_MEM_HOST))
+        return occ
+
+    def occluded_noalloc(self, rays):
+        """sst_occluded_noalloc: the same results as occluded(), without any device allocation;
+        at most SST_NOALLOC_MAX_RAYS rays per call."""
+        rays = np.ascontiguousarray(rays, np.float32).reshape(-1, 8)
+        occ = np.zeros(rays.shape[0], np.int32)
+        check(self.lib.sst_occluded_noalloc(self.handle, ptr(rays), rays.shape[0], ptr(occ), SST_MEM_HOST))
         return occ
 
     def update_texture(self, tex_id, data):

@@ -14,6 +14,7 @@
 #include <cstdio>
 #include <cstring>
 #include <memory>
+#include <mutex>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -1604,3 +1605,78 @@ int sst_debug_camera(sst_scene* s, int32_t n, const float* film, float* org, flo
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------------------------
+// Allocation-free occlusion query (sst_occluded_noalloc).  Its scratch is one array of fixed size
+// in this library's device image, laid out as
+//   [0, 256)      queue length and work counter of the traversal kernel
+//   [256, 512)    DevStats (ray counts)
+//   [512, 1024)   DevJob (the scene record the traversal kernel reads)
+//   then          ray origins (float4 x max rays), ray directions (float4 x max rays),
+//                 occlusion flags (int x max rays).
+// ---------------------------------------------------------------------------------------------
+namespace {
+constexpr size_t kNaCounters = 0, kNaStats = 256, kNaJob = 512, kNaHeader = 1024;
+constexpr size_t kNaMaxRays = SST_NOALLOC_MAX_RAYS;
+constexpr size_t kNaBytes = kNaHeader + 2 * 16 * kNaMaxRays + 4 * kNaMaxRays;
+static_assert(kNaBytes == 2360320, "the header states the scratch size");
+static_assert(sizeof(DevStats) <= kNaJob - kNaStats && sizeof(DevJob) <= kNaHeader - kNaJob, "scratch header too small");
+static_assert(alignof(DevJob) <= 256 && alignof(DevStats) <= 256, "scratch header alignment");
+constexpr int kNaMaxDevices = 64;
+}  // namespace
+
+static __device__ __align__(256) unsigned char g_noallocScratch[kNaBytes];
+static std::mutex g_noallocLock;
+static void* g_noallocAddr[kNaMaxDevices] = {};
+
+// Device address of the scratch array on `device` (the current device).  Looked up on the first
+// call for each device and kept; the caller holds g_noallocLock.
+static unsigned char* noallocScratch(int device) {
+    if (device < 0 || device >= kNaMaxDevices) fail(SST_ERR_INVALID_ARGUMENT, "device ordinal beyond the allocation-free query's table");
+    if (!g_noallocAddr[device]) {
+        void* ptr = nullptr;
+        cudaError_t e = cudaGetSymbolAddress((void**)&ptr, g_noallocScratch);
+        if (e != cudaSuccess || !ptr) fail(SST_ERR_CUDA, std::string("cudaGetSymbolAddress(scratch): ") + cudaGetErrorString(e));
+        g_noallocAddr[device] = ptr;
+    }
+    return static_cast<unsigned char*>(g_noallocAddr[device]);
+}
+
+extern "C" int sst_occluded_noalloc(sst_scene* s, const SstRay* rays, int32_t n, int32_t* occluded, int32_t memory) {
+    return guarded([&] {
+        if (!s || n < 0 || (n > 0 && (!rays || !occluded))) fail(SST_ERR_INVALID_ARGUMENT, "invalid query");
+        if (memory != SST_MEM_HOST && memory != SST_MEM_DEVICE) fail(SST_ERR_INVALID_ARGUMENT, "memory must be SST_MEM_HOST or SST_MEM_DEVICE");
+        if (size_t(n) > kNaMaxRays)
+            fail(SST_ERR_INVALID_ARGUMENT, "sst_occluded_noalloc: " + std::to_string(n) + " rays exceed the limit of " + std::to_string(kNaMaxRays) +
+                                               " rays per call (SST_NOALLOC_MAX_RAYS)");
+        if (!s->committed) fail(SST_ERR_NOT_COMMITTED, "scene is not committed");
+        if (n == 0) return;
+        std::lock_guard<std::mutex> lock(g_noallocLock);
+        sst_ctx* c = s->ctx;
+        CUDA_CHECK(cudaSetDevice(c->device));
+        unsigned char* base = noallocScratch(c->device);
+        cudaStream_t st = c->stream;
+        int* cnt = reinterpret_cast<int*>(base + kNaCounters);
+        DevStats* stats = reinterpret_cast<DevStats*>(base + kNaStats);
+        DevJob* job = reinterpret_cast<DevJob*>(base + kNaJob);
+        float4* ro = reinterpret_cast<float4*>(base + kNaHeader);
+        float4* rd = ro + kNaMaxRays;
+        int* occ = reinterpret_cast<int*>(rd + kNaMaxRays);
+        const cudaMemcpyKind in = memory == SST_MEM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+        const cudaMemcpyKind out = memory == SST_MEM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+        // SstRay = {org, tmin, dir, tmax}: split into the origin and direction arrays
+        CUDA_CHECK(cudaMemcpy2DAsync(ro, 16, rays, 32, 16, size_t(n), in, st));
+        CUDA_CHECK(cudaMemcpy2DAsync(rd, 16, reinterpret_cast<const char*>(rays) + 16, 32, 16, size_t(n), in, st));
+        // set every call: the queue length (n), the work counter and the statistics (zero), the job
+        const int hostCnt[2] = {n, 0};
+        CUDA_CHECK(cudaMemcpyAsync(cnt, hostCnt, sizeof(hostCnt), cudaMemcpyHostToDevice, st));
+        CUDA_CHECK(cudaMemsetAsync(stats, 0, sizeof(DevStats), st));
+        DevJob j{};
+        j.sc = s->dev;
+        CUDA_CHECK(cudaMemcpyAsync(job, &j, sizeof(DevJob), cudaMemcpyHostToDevice, st));
+        launch_trace_query(job, ro, rd, cnt, cnt + 1, nullptr, occ, stats, true, st);
+        CUDA_CHECK(cudaGetLastError());
+        CUDA_CHECK(cudaMemcpyAsync(occluded, occ, size_t(n) * 4, out, st));
+        CUDA_CHECK(cudaStreamSynchronize(st));
+    });
+}
