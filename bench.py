@@ -62,10 +62,14 @@ def run_batch(args, cfg):
     samples = sum(sc.FrameBuffer.Width * sc.FrameBuffer.Height * pt.TotalSpp for sc, pt in pairs)
     tris = [sum(m.NumFaces for m in sc.Meshes) for sc, _ in pairs]
 
+    nlaunch = [0]
+
     def batched():
         for sc, _ in pairs:
             sc.FrameBuffer.Reset()
-        return render_batch(pairs).renderTimeMs
+        st = render_batch(pairs)
+        nlaunch[0] += st.numKernelLaunches
+        return st.renderTimeMs
 
     def sequential():
         ms = 0.0
@@ -79,7 +83,9 @@ def run_batch(args, cfg):
         batched()
         sequential()
     with ClockSampler(0) as clk:
+        nlaunch[0] = 0
         tb = [batched() for _ in range(args.steps)]
+        batched_launches = nlaunch[0]
         ts = [sequential() for _ in range(args.steps)]
     vb = samples / (np.mean(tb) / 1000) / 1e6
     vs = samples / (np.mean(ts) / 1000) / 1e6
@@ -94,6 +100,7 @@ def run_batch(args, cfg):
                        "triangles_total": int(sum(tris))},
             "sequential": {"value": round(vs, 3), "ms_per_step": round(float(np.mean(ts)), 3)},
             "batched_over_sequential": round(vb / vs, 3),
+            "gpu_launches": int(batched_launches),
             "e2e": {"value": round(e2e_b, 3), "unit": "Msamples/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": int(sum(sc.FrameBuffer.Image.data.nbytes for sc, _ in pairs))},
             "clocks": clk.summary()}
@@ -122,7 +129,7 @@ def run_adjoint(args, cfg):
         im = dr.forward()
         loss, d = l2_loss(im, target)
         dr.backward(d)
-        return dr.stats_forward.renderTimeMs, dr.stats_backward.renderTimeMs
+        return dr.stats_forward.renderTimeMs, dr.stats_backward.renderTimeMs, dr.stats_forward.numKernelLaunches + dr.stats_backward.numKernelLaunches
 
     for _ in range(args.warmup):
         step()
@@ -137,6 +144,7 @@ def run_adjoint(args, cfg):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(fwd + bwd, 3), "higher_is_better": False, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded texture and scene)",
             "config": {"workload": cfg["name"], "texture": [cfg["tex"], cfg["tex"], 3], "roughness_params": len(boxes), "emitter_params": 3},
+            "gpu_launches": int(sum(t[2] for t in times)),
             "forward": {"ms": round(fwd, 3), "Msamples_per_s": round(samples / fwd / 1e3, 3)},
             "backward": {"ms": round(bwd, 3), "Msamples_per_s": round(samples / bwd / 1e3, 3)},
             "e2e": {"value": round(wall * 1e3, 3), "unit": "ms per forward+loss+backward step", "h2d_bytes_per_step": int(dldi.nbytes),
@@ -348,11 +356,17 @@ def run_ours(args, cfg):
     def step():
         return sc.native.render(params, film.data_ptr(), _native.SST_MEM_DEVICE)
 
+    # launch configuration for this scene (sst_autotune: short trial renders, results unchanged)
+    tuning, tune_s = _native.get_tuning(ctx), 0.0
+    if not args.no_autotune:
+        t0 = time.perf_counter()
+        tuning, _ = _native.autotune(sc.native, params, 2)
+        tune_s = time.perf_counter() - t0
     for _ in range(args.warmup):
         step()
-    # timed region: K renders, L2 flushed between them, kernel events on the renderer's stream
-    _native.set_profiling(ctx, True)
-    render_ms, rays, srays = 0.0, 0, 0
+    # timed region: K renders (the production path: one CUDA graph per wave), L2 flushed between
+    # them, the renderer's CUDA-event time per render
+    render_ms, rays, srays, launches = 0.0, 0, 0, 0
     barrier(ws)
     torch.cuda.synchronize()
     with ClockSampler(local) as clk:
@@ -364,9 +378,15 @@ def run_ours(args, cfg):
             render_ms += st.renderTimeMs
             rays += st.numRays
             srays += st.numShadowRays
+            launches += st.numKernelLaunches
         torch.cuda.synchronize()
         wall = time.perf_counter() - wall0
     barrier(ws)
+    # one more render with per-kernel CUDA events (kernel split and the roofline's kernel time)
+    _native.set_profiling(ctx, True)
+    flush.fill_(-1.0)
+    torch.cuda.synchronize()
+    step()
     ktimes = _native.kernel_times(ctx)
     _native.set_profiling(ctx, False)
     ms_per_step = max_over_ranks(ws, render_ms / args.steps)
@@ -405,7 +425,6 @@ def run_ours(args, cfg):
     steps = args.steps
     ext, sh = rays / steps / samples, srays / steps / samples
     b_sample = ext * (bpr + 172) + sh * (bpr - 12) + 12
-    launches = sum(v["launches"] for v in ktimes.values())
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -427,6 +446,8 @@ def run_ours(args, cfg):
             "bytes_per_sample": round(b_sample, 1), "rays_per_sample": round(ext, 4), "shadow_rays_per_sample": round(sh, 4),
             "gpu_launches": launches,
             "kernel_ms": {k: round(v["ms"], 3) for k, v in ktimes.items()},
+            "kernel_ms_note": "one extra render with per-kernel CUDA events after the timed region",
+            "tuning": tuning, "autotune_s": round(tune_s, 3),
             "prepare_s": round(prep_s, 3), "bvh": os.environ.get("SST_BVH", "lbvh"),
             "clocks": clocks,
             "cpu_baseline": cpu,
@@ -447,6 +468,7 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--width", type=int, default=None, help="override (profiling cases)")
     ap.add_argument("--height", type=int, default=None)
     ap.add_argument("--spp", type=int, default=None)

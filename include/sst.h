@@ -95,7 +95,7 @@ typedef struct SstRenderStats {
     double renderTimeMs;      /* GPU time of the iterations, frame-buffer work excluded */
     double frameBufferTimeMs; /* film initialisation / copies */
     int32_t numIterations;
-    int32_t reserved;
+    int32_t numKernelLaunches; /* kernels this library launched for the render (graph replays counted per node) */
     uint64_t numRays;       /* RayTracerStats.NumRays */
     uint64_t numShadowRays; /* RayTracerStats.NumShadowRays */
     uint64_t numNanOrInf;   /* FrameBuffer.NaNWarnings count */
@@ -166,6 +166,25 @@ int sst_scene_info(sst_scene* scene, int32_t* numEmitters, int32_t* numTriangles
 /* ---- ray queries (TinyEmbree Raytracer.Trace / IsOccluded, PathTracer.cs:319,467) ----------- */
 int sst_trace(sst_scene* scene, const SstRay* rays, int32_t n, SstHit* hits, int32_t memory);
 int sst_occluded(sst_scene* scene, const SstRay* rays, int32_t n, int32_t* occluded, int32_t memory);
+
+/* ---- launch configuration and autotuner (no counterpart in the reference) ---------------------
+ * The wavefront's queue capacity and the traversal kernels' launch shape.  None of them changes
+ * a result: films and query results are bitwise the same under every valid setting. */
+typedef struct SstTuning {
+    int32_t waveCapacity;     /* paths in flight per wave; 0 = the default (2^21) */
+    int32_t traceBlock;       /* threads per traversal block: 64, 128 or 256 */
+    int32_t traceStackShared; /* traversal stack entries per thread kept in shared memory: 16, 24 or 32 */
+    int32_t traceBlocksPerSM; /* resident traversal blocks per SM; 0 = as many as fit */
+} SstTuning;
+int sst_get_tuning(sst_ctx* ctx, SstTuning* out);
+/* Invalid values return SST_ERR_INVALID_ARGUMENT and leave the setting unchanged. */
+int sst_set_tuning(sst_ctx* ctx, const SstTuning* tuning);
+/* Chooses the setting for this scene and these parameters by timing trial renders of
+ * trialIterations iterations (into a scratch film; the caller's films are not touched):
+ * first the traversal variant (block size x shared stack entries), then the resident blocks per
+ * SM, then the wave capacity, keeping the fastest of two runs per candidate.  The choice is
+ * applied to the scene's context and returned in `chosen` (bestTrialMs may be NULL). */
+int sst_autotune(sst_scene* scene, const SstPathTracerParams* params, int32_t trialIterations, SstTuning* chosen, double* bestTrialMs);
 
 /* ---- allocation-free occlusion query: no counterpart in the reference --------------------------
  * The same any-hit queries as sst_occluded, with the same arguments and the same results, but the

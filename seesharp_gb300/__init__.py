@@ -5,11 +5,11 @@ libsst.so (CUDA, C ABI in include/sst.h).
 """
 from .images import (BorderHandling, FrameBuffer, MonochromeImage, RgbColor, RgbImage, TextureMono, TextureRgb, mean_rgb,
                      rel_mse)
-from .integrators import Integrator, PathTracer, render_batch
+from .integrators import Integrator, PathTracer, autotune, render_batch
 from .scene import (ArgumentException, DiffuseEmitter, DiffuseMaterial, EnvironmentMap, GenericMaterial, GlossyEmitter,
                     InvalidOperationException, Matrix4x4, Mesh, PerspectiveCamera, Scene, Triangle)
 
 __all__ = ["BorderHandling", "FrameBuffer", "MonochromeImage", "RgbColor", "RgbImage", "TextureMono", "TextureRgb", "mean_rgb",
-           "rel_mse", "Integrator", "PathTracer", "render_batch", "ArgumentException", "DiffuseEmitter", "DiffuseMaterial", "EnvironmentMap",
+           "rel_mse", "Integrator", "PathTracer", "autotune", "render_batch", "ArgumentException", "DiffuseEmitter", "DiffuseMaterial", "EnvironmentMap",
            "GenericMaterial", "GlossyEmitter", "InvalidOperationException", "Matrix4x4", "Mesh", "PerspectiveCamera", "Scene",
            "Triangle"]

@@ -60,13 +60,21 @@ class SstPathTracerParams(ctypes.Structure):
 
 class SstRenderStats(ctypes.Structure):
     _fields_ = [("renderTimeMs", ctypes.c_double), ("frameBufferTimeMs", ctypes.c_double), ("numIterations", ctypes.c_int32),
-                ("reserved", ctypes.c_int32), ("numRays", ctypes.c_uint64), ("numShadowRays", ctypes.c_uint64),
+                ("numKernelLaunches", ctypes.c_int32), ("numRays", ctypes.c_uint64), ("numShadowRays", ctypes.c_uint64),
                 ("numNanOrInf", ctypes.c_uint64), ("nanPixel", ctypes.c_int32 * 4), ("nanIteration", ctypes.c_int32 * 4)]
 
 
 class SstGradients(ctypes.Structure):
     _fields_ = [("textures", ctypes.c_void_p), ("materialBaseColor", ctypes.c_void_p), ("materialRoughness", ctypes.c_void_p),
                 ("emitterRadiance", ctypes.c_void_p), ("memory", ctypes.c_int32), ("reserved", ctypes.c_int32)]
+
+
+class SstTuning(ctypes.Structure):
+    _fields_ = [("waveCapacity", ctypes.c_int32), ("traceBlock", ctypes.c_int32), ("traceStackShared", ctypes.c_int32),
+                ("traceBlocksPerSM", ctypes.c_int32)]
+
+    def as_dict(self):
+        return {k: int(getattr(self, k)) for k, _ in self._fields_}
 
 
 class SstRenderJob(ctypes.Structure):
@@ -107,6 +115,9 @@ SIGNATURES = {
     "sst_scene_update_texture": [_vp, _i32, _vp],
     "sst_forward": [_vp, _P(SstPathTracerParams), _vp, _i32, _P(SstRenderStats)],
     "sst_backward": [_vp, _P(SstPathTracerParams), _vp, _i32, _P(SstGradients), _P(SstRenderStats)],
+    "sst_get_tuning": [_vp, _P(SstTuning)],
+    "sst_set_tuning": [_vp, _P(SstTuning)],
+    "sst_autotune": [_vp, _P(SstPathTracerParams), _i32, _P(SstTuning), _P(ctypes.c_double)],
     "sst_set_profiling": [_vp, _i32],
     "sst_get_kernel_times": [_vp, _vp, _vp, _vp, _i32],
     "sst_debug_material_eval": [_vp, _i32, _i32, _vp, _vp, _vp, _vp, _vp],
@@ -194,6 +205,31 @@ KERNEL_CLASSES = ["camera", "trace_closest", "shade", "trace_shadow", "film_fold
 
 def set_profiling(ctx, enable):
     check(ctx.lib.sst_set_profiling(ctx.handle, int(bool(enable))))
+
+
+def get_tuning(ctx):
+    t = SstTuning()
+    check(ctx.lib.sst_get_tuning(ctx.handle, ctypes.byref(t)))
+    return t.as_dict()
+
+
+def set_tuning(ctx, **kw):
+    """Changes the named fields of the context's launch configuration (SstTuning)."""
+    t = SstTuning()
+    check(ctx.lib.sst_get_tuning(ctx.handle, ctypes.byref(t)))
+    for k, v in kw.items():
+        if k not in dict(SstTuning._fields_):
+            raise AttributeError(k)
+        setattr(t, k, int(v))
+    check(ctx.lib.sst_set_tuning(ctx.handle, ctypes.byref(t)))
+
+
+def autotune(scene_handle, params, trial_iterations=2):
+    """sst_autotune: returns (chosen tuning as a dict, best trial time in ms)."""
+    t = SstTuning()
+    ms = ctypes.c_double()
+    check(scene_handle.lib.sst_autotune(scene_handle.handle, ctypes.byref(params), int(trial_iterations), ctypes.byref(t), ctypes.byref(ms)))
+    return t.as_dict(), ms.value
 
 
 def kernel_times(ctx):

@@ -106,6 +106,9 @@ struct sst_ctx {
     DevBuf scratchIn, scratchOut, scratchOut2;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     int* pinnedCount = nullptr;
+    // launch configuration (sst_set_tuning / sst_autotune)
+    TraceTuning trace;
+    int waveCapacity = 0;  // 0: the default
     // kernel timing (sst_set_profiling)
     bool profiling = false;
     std::vector<cudaEvent_t> evPool;
@@ -764,7 +767,7 @@ static void renderJobs(sst_ctx* c, std::vector<JobIn>& jobs, SstRenderStats* out
     }
     if (totalItems == 0) return;
     if (timeLimit && jobs.size() > 1) fail(SST_ERR_UNSUPPORTED, "MaximumRenderTimeMs is supported for single renders only");
-    int cap = int(std::min<long long>(defaultWaveCapacity(), totalItems));
+    int cap = int(std::min<long long>(c->waveCapacity > 0 ? c->waveCapacity : defaultWaveCapacity(), totalItems));
     for (auto& j : jobs) cap = std::max(cap, 1);
     Wave w;
     ensureWave(c, cap, ns, w);
@@ -810,7 +813,9 @@ static void renderJobs(sst_ctx* c, std::vector<JobIn>& jobs, SstRenderStats* out
     for (auto& wd : waves) maxFold = std::max(maxFold, wd.foldThreads);
 
     // One wave: camera, then per bounce closest hit / shade / shadow rays, then the film fold.
+    long long launches = 0;  // kernels issued (in graph mode: the nodes of one wave)
     auto issueWave = [&](int items, bool allowEarlyExit) {
+        launches += 2;  // camera and film fold
         CUDA_CHECK(cudaMemsetAsync(cnt, 0, sizeof(int) * kNumCounters, st));
         {
             KTimer kt(c, 0);
@@ -821,7 +826,7 @@ static void renderJobs(sst_ctx* c, std::vector<JobIn>& jobs, SstRenderStats* out
         for (int d = 1; d <= maxDepth; ++d) {
             {
                 KTimer kt(c, 1);
-                launch_trace_closest(dj, A.job, A.ro, A.rd, cnt + kCntQueue + d, cnt + kCntWork + 2 * d, w.wb.hits, dstats, st);
+                launch_trace_closest(c->trace, dj, A.job, A.ro, A.rd, cnt + kCntQueue + d, cnt + kCntWork + 2 * d, w.wb.hits, dstats, st);
             }
             {
                 KTimer kt(c, 2);
@@ -830,9 +835,10 @@ static void renderJobs(sst_ctx* c, std::vector<JobIn>& jobs, SstRenderStats* out
             }
             {
                 KTimer kt(c, 3);
-                launch_trace_shadow(dj, w.wb.shJob, w.wb.shRo, w.wb.shRd, w.wb.shTgt, cnt + kCntShadow + d, cnt + kCntWork + 2 * d + 1, w.wb.nee,
+                launch_trace_shadow(c->trace, dj, w.wb.shJob, w.wb.shRo, w.wb.shRd, w.wb.shTgt, cnt + kCntShadow + d, cnt + kCntWork + 2 * d + 1, w.wb.nee,
                                     dstats, st);
             }
+            launches += 3;  // closest hit, shade, shadow rays
             std::swap(A, B);
             if (allowEarlyExit && d >= 6 && d < maxDepth) {
                 // stop early once the queue is empty (long MaxDepth with Russian roulette)
@@ -867,6 +873,7 @@ static void renderJobs(sst_ctx* c, std::vector<JobIn>& jobs, SstRenderStats* out
         CUDA_CHECK(cudaStreamEndCapture(st, &graph));
         CUDA_CHECK(cudaGraphInstantiate(&exec, graph, 0));
         for (size_t k = 0; k < waves.size(); ++k) CUDA_CHECK(cudaGraphLaunch(exec, st));
+        launches *= (long long)waves.size();
         CUDA_CHECK(cudaGetLastError());
         CUDA_CHECK(cudaStreamSynchronize(st));
         cudaGraphExecDestroy(exec);
@@ -914,6 +921,7 @@ static void renderJobs(sst_ctx* c, std::vector<JobIn>& jobs, SstRenderStats* out
     if (out) {
         out->renderTimeMs += ms;
         out->numIterations += jobs.size() == 1 ? jobs[0].done : 0;
+        out->numKernelLaunches += int(std::min<long long>(launches, 0x7FFFFFFF));
         out->numRays += hs.rays;
         out->numShadowRays += hs.shadowRays;
         uint64_t prev = out->numNanOrInf;
@@ -972,14 +980,14 @@ static void runQuery(sst_scene* s, const SstRay* rays, int n, SstHit* hits, int3
     CUDA_CHECK(cudaMemsetAsync(c->stats.p, 0, sizeof(DevStats), st));
     if (anyHit) {
         occBuf.ensure(size_t(n) * 4);
-        launch_trace_query(jobTable(s), ro.as<float4>(), rd.as<float4>(), cnt.as<int>(), cnt.as<int>() + 1, nullptr, occBuf.as<int>(),
+        launch_trace_query(c->trace, jobTable(s), ro.as<float4>(), rd.as<float4>(), cnt.as<int>(), cnt.as<int>() + 1, nullptr, occBuf.as<int>(),
                            c->stats.as<DevStats>(), true, st);
         CUDA_CHECK(cudaMemcpyAsync(occl, occBuf.p, size_t(n) * 4, memory == SST_MEM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, st));
         CUDA_CHECK(cudaStreamSynchronize(st));
         return;
     }
     hitsBuf.ensure(size_t(n) * 16);
-    launch_trace_query(jobTable(s), ro.as<float4>(), rd.as<float4>(), cnt.as<int>(), cnt.as<int>() + 1, hitsBuf.as<float4>(), nullptr,
+    launch_trace_query(c->trace, jobTable(s), ro.as<float4>(), rd.as<float4>(), cnt.as<int>(), cnt.as<int>() + 1, hitsBuf.as<float4>(), nullptr,
                        c->stats.as<DevStats>(), false, st);
     std::vector<float4> hh(n);
     CUDA_CHECK(cudaMemcpyAsync(hh.data(), hitsBuf.p, size_t(n) * 16, cudaMemcpyDeviceToHost, st));
@@ -1325,6 +1333,120 @@ int sst_render(sst_scene* s, const SstPathTracerParams* p, float* film, int32_t 
         fbMs += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - tfb1).count();
         local.frameBufferTimeMs = fbMs;
         if (stats) *stats = local;
+    });
+}
+
+static TraceTuning toTrace(const SstTuning& t) { return TraceTuning{t.traceBlock, t.traceStackShared, t.traceBlocksPerSM}; }
+
+static void checkTuning(const SstTuning& t) {
+    if (!traceTuningValid(toTrace(t))) fail(SST_ERR_INVALID_ARGUMENT, "traceBlock must be 64, 128 or 256 and traceStackShared 16, 24 or 32");
+    if (t.waveCapacity != 0 && (t.waveCapacity < 1024 || t.waveCapacity > (1 << 24)))
+        fail(SST_ERR_INVALID_ARGUMENT, "waveCapacity must be 0 or in [1024, 2^24]");
+    if (t.traceBlocksPerSM < 0 || t.traceBlocksPerSM > 64) fail(SST_ERR_INVALID_ARGUMENT, "traceBlocksPerSM must be in [0, 64]");
+}
+
+static SstTuning currentTuning(const sst_ctx* c) {
+    SstTuning t{};
+    t.waveCapacity = c->waveCapacity;
+    t.traceBlock = c->trace.block;
+    t.traceStackShared = c->trace.smemStack;
+    t.traceBlocksPerSM = c->trace.blocksPerSM;
+    return t;
+}
+
+int sst_get_tuning(sst_ctx* c, SstTuning* out) {
+    return guarded([&] {
+        if (!c || !out) fail(SST_ERR_INVALID_ARGUMENT, "NULL argument");
+        *out = currentTuning(c);
+    });
+}
+
+int sst_set_tuning(sst_ctx* c, const SstTuning* t) {
+    return guarded([&] {
+        if (!c || !t) fail(SST_ERR_INVALID_ARGUMENT, "NULL argument");
+        checkTuning(*t);
+        c->trace = toTrace(*t);
+        c->waveCapacity = t->waveCapacity;
+    });
+}
+
+int sst_autotune(sst_scene* s, const SstPathTracerParams* p, int32_t trialIterations, SstTuning* chosen, double* bestTrialMs) {
+    return guarded([&] {
+        if (!s || !p || trialIterations < 1) fail(SST_ERR_INVALID_ARGUMENT, "invalid autotune arguments");
+        SstPathTracerParams tp = *p;
+        tp.firstIteration = 0;
+        tp.totalSpp = trialIterations;
+        tp.maximumRenderTimeMs = 0;
+        checkParams(s, &tp);
+        sst_ctx* c = s->ctx;
+        CUDA_CHECK(cudaSetDevice(c->device));
+        const SstTuning start = currentTuning(c);
+        DevBuf film;
+        film.ensure(size_t(tp.width) * tp.height * 3 * sizeof(float));
+        const bool prof = c->profiling;
+        c->profiling = false;
+        // one candidate: the faster of two trial renders
+        auto trial = [&](const SstTuning& t) {
+            c->trace = toTrace(t);
+            c->waveCapacity = t.waveCapacity;
+            double best = 1e300;
+            for (int r = 0; r < 2; ++r) {
+                std::vector<JobIn> jobs(1);
+                jobs[0].s = s;
+                jobs[0].p = tp;
+                jobs[0].dFilm = film.as<float>();
+                jobs[0].iterFirst = 0;
+                jobs[0].iterEnd = tp.totalSpp;
+                SstRenderStats st{};
+                renderJobs(c, jobs, &st);
+                best = std::min(best, st.renderTimeMs);
+            }
+            return best;
+        };
+        SstTuning best = start;
+        double bestMs = 1e300;
+        try {
+            // traversal variant
+            for (int b : {64, 128, 256})
+                for (int k : {16, 24, 32}) {
+                    SstTuning t = best;
+                    t.traceBlock = b;
+                    t.traceStackShared = k;
+                    t.traceBlocksPerSM = 0;
+                    double ms = trial(t);
+                    if (ms < bestMs) { bestMs = ms; best = t; }
+                }
+            // resident traversal blocks per SM
+            int m = traceMaxBlocksPerSM(toTrace(best));
+            for (int bps : {m / 2, (3 * m) / 4}) {
+                if (bps < 1 || bps >= m) continue;
+                SstTuning t = best;
+                t.traceBlocksPerSM = bps;
+                double ms = trial(t);
+                if (ms < bestMs) { bestMs = ms; best = t; }
+            }
+            // wave capacity
+            long long items = (long long)tp.width * tp.height * tp.totalSpp;
+            for (int capLog = 19; capLog <= 22; ++capLog) {
+                int cap = 1 << capLog;
+                if (cap == (best.waveCapacity > 0 ? best.waveCapacity : defaultWaveCapacity())) continue;
+                if ((long long)cap > 2 * items) break;
+                SstTuning t = best;
+                t.waveCapacity = cap;
+                double ms = trial(t);
+                if (ms < bestMs) { bestMs = ms; best = t; }
+            }
+        } catch (...) {
+            c->trace = toTrace(start);
+            c->waveCapacity = start.waveCapacity;
+            c->profiling = prof;
+            throw;
+        }
+        c->profiling = prof;
+        c->trace = toTrace(best);
+        c->waveCapacity = best.waveCapacity;
+        if (chosen) *chosen = best;
+        if (bestTrialMs) *bestTrialMs = bestMs;
     });
 }
 
@@ -1674,7 +1796,7 @@ extern "C" int sst_occluded_noalloc(sst_scene* s, const SstRay* rays, int32_t n,
         DevJob j{};
         j.sc = s->dev;
         CUDA_CHECK(cudaMemcpyAsync(job, &j, sizeof(DevJob), cudaMemcpyHostToDevice, st));
-        launch_trace_query(job, ro, rd, cnt, cnt + 1, nullptr, occ, stats, true, st);
+        launch_trace_query(c->trace, job, ro, rd, cnt, cnt + 1, nullptr, occ, stats, true, st);
         CUDA_CHECK(cudaGetLastError());
         CUDA_CHECK(cudaMemcpyAsync(occluded, occ, size_t(n) * 4, out, st));
         CUDA_CHECK(cudaStreamSynchronize(st));

@@ -14,7 +14,7 @@ namespace sst {
 // Large shading functions called from several places are compiled once (SST_DN) to keep the
 // instruction footprint of the shade kernel small.
 #ifdef SST_NOINLINE_MORE
-#define SST_DN __device__ __noinline__
+#define SST_DN static __device__ __noinline__
 #else
 #define SST_DN __device__ __forceinline__
 #endif
@@ -315,7 +315,7 @@ SST_D bool shouldReflect(float3 faceN, float3 outW, float3 inW) { return dot(out
 // Compiled once and called (not inlined) by default: the shade kernel evaluates it for three
 // directions per bounce, and one copy of the code keeps the instruction cache warm.
 #ifndef SST_EVAL_INLINE
-__device__ __noinline__
+static __device__ __noinline__
 #else
 SST_D
 #endif

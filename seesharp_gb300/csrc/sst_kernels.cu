@@ -177,194 +177,6 @@ void launch_film_fold(const DevJob* jobs, const WaveChunk* chunks, const WaveDes
 }
 
 // =============================================================================================
-// K3/K4: BVH traversal.  Binary BVH, both child boxes stored in the parent (64-byte nodes read
-// as four 128-bit loads), watertight ray/triangle test (Woop, Benthin, Wald 2013), per-thread
-// stack in shared memory with a local-memory tail, persistent warps fetching 32 rays at a time.
-// =============================================================================================
-struct RayPre {
-    int kx, ky, kz;
-    float Sx, Sy, Sz;
-};
-SST_D float comp(float3 a, int k) { return k == 0 ? a.x : (k == 1 ? a.y : a.z); }
-SST_D RayPre rayPre(float3 d) {
-    RayPre p;
-    float ax = fabsf(d.x), ay = fabsf(d.y), az = fabsf(d.z);
-    p.kz = (ax > ay) ? (ax > az ? 0 : 2) : (ay > az ? 1 : 2);
-    p.kx = p.kz == 2 ? 0 : p.kz + 1;
-    p.ky = p.kx == 2 ? 0 : p.kx + 1;
-    float dz = comp(d, p.kz);
-    if (dz < 0.0f) { int t = p.kx; p.kx = p.ky; p.ky = t; }
-    p.Sx = comp(d, p.kx) / dz;
-    p.Sy = comp(d, p.ky) / dz;
-    p.Sz = 1.0f / dz;
-    return p;
-}
-// Returns true with t, u (2nd vertex weight), v (3rd vertex weight) when tmin < t < tmax.
-SST_D bool isectTri(float3 o, const RayPre& p, float3 v0, float3 v1, float3 v2, float tmin, float tmax, float& t, float& u, float& v) {
-    float3 A = v0 - o, B = v1 - o, C = v2 - o;
-    float Az_ = comp(A, p.kz), Bz_ = comp(B, p.kz), Cz_ = comp(C, p.kz);
-    float Ax = comp(A, p.kx) - p.Sx * Az_, Ay = comp(A, p.ky) - p.Sy * Az_;
-    float Bx = comp(B, p.kx) - p.Sx * Bz_, By = comp(B, p.ky) - p.Sy * Bz_;
-    float Cx = comp(C, p.kx) - p.Sx * Cz_, Cy = comp(C, p.ky) - p.Sy * Cz_;
-    float U = Cx * By - Cy * Bx;
-    float V = Ax * Cy - Ay * Cx;
-    float W = Bx * Ay - By * Ax;
-    if (U == 0.0f || V == 0.0f || W == 0.0f) {  // edge case: exact evaluation in double
-        U = (float)((double)Cx * (double)By - (double)Cy * (double)Bx);
-        V = (float)((double)Ax * (double)Cy - (double)Ay * (double)Cx);
-        W = (float)((double)Bx * (double)Ay - (double)By * (double)Ax);
-    }
-    if ((U < 0.0f || V < 0.0f || W < 0.0f) && (U > 0.0f || V > 0.0f || W > 0.0f)) return false;
-    float det = U + V + W;
-    if (det == 0.0f) return false;
-    float T = U * (p.Sz * Az_) + V * (p.Sz * Bz_) + W * (p.Sz * Cz_);
-    float rcp = 1.0f / det;
-    float tt = T * rcp;
-    if (!(tt > tmin) || !(tt < tmax)) return false;
-    t = tt;
-    u = V * rcp;
-    v = W * rcp;
-    return true;
-}
-
-struct TraceResult {
-    float t, u, v;
-    int tri;  // leaf-ordered triangle, -1 for a miss
-};
-
-// Closest hit (ANY = false; ties in t resolve to the smaller global triangle id) or any hit.
-struct Bvh {
-    const float4* nodes;
-    const float4* triv;
-    int nNodes;
-};
-SST_D Bvh bvhOf(const DevScene& sc) { return Bvh{sc.nodes, sc.triv, sc.nNodes}; }
-
-template <bool ANY>
-SST_D TraceResult traverse(const Bvh sc, float3 org, float3 dir, float tmin, float tmax, int* sstack, int* errFlags) {
-    TraceResult r{tmax, 0.f, 0.f, -1};
-    if (sc.nNodes == 0 || !(tmax > tmin)) return r;
-    int bestGid = 0x7FFFFFFF;
-    RayPre pre = rayPre(dir);
-    float3 inv = mk(1.0f / dir.x, 1.0f / dir.y, 1.0f / dir.z);
-    float3 oi = mk(-org.x * inv.x, -org.y * inv.y, -org.z * inv.z);
-    int lstack[kMaxStack - kSmemStack];
-    int sp = 0;
-    uint32_t ref = 0;  // root inner node
-    const int tid = threadIdx.x;
-    for (;;) {
-        if (!(ref & kLeafFlag)) {
-            const float4* nd = sc.nodes + 4 * (size_t)ref;
-            float4 n0 = __ldg(nd), n1 = __ldg(nd + 1), n2 = __ldg(nd + 2), n3 = __ldg(nd + 3);
-            float hitT = r.t * 1.0000004f;  // conservative far bound (box/triangle rounding)
-            // child 0
-            float a0 = fmaf(n0.x, inv.x, oi.x), b0 = fmaf(n0.y, inv.x, oi.x);
-            float c0 = fmaf(n0.z, inv.y, oi.y), d0 = fmaf(n0.w, inv.y, oi.y);
-            float e0 = fmaf(n2.x, inv.z, oi.z), f0 = fmaf(n2.y, inv.z, oi.z);
-            float tn0 = fmaxf(fmaxf(fminf(a0, b0), fminf(c0, d0)), fmaxf(fminf(e0, f0), tmin));
-            float tf0 = fminf(fminf(fmaxf(a0, b0), fmaxf(c0, d0)), fminf(fmaxf(e0, f0), hitT));
-            // child 1
-            float a1 = fmaf(n1.x, inv.x, oi.x), b1 = fmaf(n1.y, inv.x, oi.x);
-            float c1 = fmaf(n1.z, inv.y, oi.y), d1 = fmaf(n1.w, inv.y, oi.y);
-            float e1 = fmaf(n2.z, inv.z, oi.z), f1 = fmaf(n2.w, inv.z, oi.z);
-            float tn1 = fmaxf(fmaxf(fminf(a1, b1), fminf(c1, d1)), fmaxf(fminf(e1, f1), tmin));
-            float tf1 = fminf(fminf(fmaxf(a1, b1), fmaxf(c1, d1)), fminf(fmaxf(e1, f1), hitT));
-            bool h0 = tn0 <= tf0 * 1.0000004f, h1 = tn1 <= tf1 * 1.0000004f;
-            uint32_t r0 = __float_as_uint(n3.x), r1 = __float_as_uint(n3.y);
-            if (h0 && h1) {
-                uint32_t nearR = r0, farR = r1;
-                if (tn1 < tn0) { nearR = r1; farR = r0; }
-                if (sp < kSmemStack) sstack[sp * kTraceBlock + tid] = (int)farR;
-                else if (sp < kMaxStack) lstack[sp - kSmemStack] = (int)farR;
-                else { atomicOr(errFlags, 1); return r; }
-                ++sp;
-                ref = nearR;
-                continue;
-            } else if (h0) { ref = r0; continue; }
-            else if (h1) { ref = r1; continue; }
-        } else {
-            int first = (int)(ref & kLeafFirstMask);
-            int cnt = (int)((ref >> kLeafCountShift) & 0xF) + 1;
-            for (int k = 0; k < cnt; ++k) {
-                int ti = first + k;
-                float4 a = __ldg(&sc.triv[3 * (size_t)ti]), b = __ldg(&sc.triv[3 * (size_t)ti + 1]), c = __ldg(&sc.triv[3 * (size_t)ti + 2]);
-                float t, u, v;
-                // allow an equal distance so that ties can resolve to the smaller id
-                float lim = ANY ? r.t : __uint_as_float(__float_as_uint(r.t) + (r.t < CUDART_INF_F ? 1u : 0u));
-                if (isectTri(org, pre, f3(a), f3(b), f3(c), tmin, lim, t, u, v)) {
-                    int gid = __float_as_int(a.w);
-                    if (ANY) { r.t = t; r.u = u; r.v = v; r.tri = ti; return r; }
-                    if (t < r.t || (t == r.t && gid < bestGid)) { r.t = t; r.u = u; r.v = v; r.tri = ti; bestGid = gid; }
-                }
-            }
-        }
-        if (sp == 0) break;
-        --sp;
-        ref = (uint32_t)(sp < kSmemStack ? sstack[sp * kTraceBlock + tid] : lstack[sp - kSmemStack]);
-    }
-    return r;
-}
-
-// mode 0: closest hit -> hits[i]; mode 1: shadow rays, zero nee[tgt[i]] when occluded;
-// mode 2: any hit -> occl[i] = 1/0.
-template <int MODE>
-__global__ void __launch_bounds__(kTraceBlock) k_trace(const DevJob* __restrict__ jobs, const uint32_t* __restrict__ rayJob, const float4* ro,
-                                                       const float4* rd, const int* count, int* work, float4* hits, const int* tgt, float4* nee,
-                                                       int* occl, DevStats* stats, int countRays) {
-    __shared__ int sstack[kSmemStack * kTraceBlock];
-    const int n = *count;
-    const int lane = threadIdx.x & 31;
-    if (countRays && blockIdx.x == 0 && threadIdx.x == 0) {
-        if (MODE == 0) atomicAdd(&stats->rays, (unsigned long long)n);
-    }
-    for (;;) {
-        int base = 0;
-        if (lane == 0) base = atomicAdd(work, 32);
-        base = __shfl_sync(0xffffffffu, base, 0);
-        if (base >= n) break;
-        int i = base + lane;
-        if (i < n) {
-            float4 o = ro[i], d = rd[i];
-            uint32_t jb = rayJob ? rayJob[i] : 0u;
-            TraceResult h = traverse<MODE != 0>(bvhOf(jobs[jb].sc), f3(o), f3(d), o.w, d.w, sstack, &stats->errorFlags);
-            if (MODE == 0) {
-                hits[i] = make_float4(h.t, h.u, h.v, __int_as_float(h.tri));
-            } else if (MODE == 1) {
-                if (h.tri >= 0) nee[tgt[i]] = make_float4(0.f, 0.f, 0.f, 0.f);
-            } else {
-                occl[i] = h.tri >= 0 ? 1 : 0;
-            }
-        }
-    }
-}
-
-int traceGrid() {
-    static int g = 0;
-    if (g == 0) {
-        int dev, sms, bps;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, k_trace<0>, kTraceBlock, 0);
-        g = sms * (bps > 0 ? bps : 1);
-    }
-    return g;
-}
-
-void launch_trace_closest(const DevJob* jobs, const uint32_t* rayJob, const float4* ro, const float4* rd, const int* count, int* work, float4* hits,
-                          DevStats* stats, cudaStream_t s) {
-    k_trace<0><<<traceGrid(), kTraceBlock, 0, s>>>(jobs, rayJob, ro, rd, count, work, hits, nullptr, nullptr, nullptr, stats, 1);
-}
-void launch_trace_shadow(const DevJob* jobs, const uint32_t* rayJob, const float4* ro, const float4* rd, const int* tgt, const int* count, int* work,
-                         float4* nee, DevStats* stats, cudaStream_t s) {
-    k_trace<1><<<traceGrid(), kTraceBlock, 0, s>>>(jobs, rayJob, ro, rd, count, work, nullptr, tgt, nee, nullptr, stats, 0);
-}
-void launch_trace_query(const DevJob* jobs, const float4* ro, const float4* rd, const int* count, int* work, float4* hits, int* occl,
-                        DevStats* stats, bool anyHit, cudaStream_t s) {
-    if (anyHit) k_trace<2><<<traceGrid(), kTraceBlock, 0, s>>>(jobs, nullptr, ro, rd, count, work, nullptr, nullptr, nullptr, occl, stats, 0);
-    else k_trace<0><<<traceGrid(), kTraceBlock, 0, s>>>(jobs, nullptr, ro, rd, count, work, hits, nullptr, nullptr, nullptr, stats, 0);
-}
-
-// =============================================================================================
 // K5 + K7 + K8: one bounce of the estimator for every queued path.
 // =============================================================================================
 SST_D void splat(float* samples, uint32_t item, float3 v) {

@@ -1,4 +1,4 @@
-// Launch wrappers of the kernels in sst_kernels.cu (called by the host driver in sst_api.cu).
+// Launch wrappers of the kernels in sst_kernels.cu and sst_trace.cu (called by the host driver in sst_api.cu).
 #pragma once
 #include <cuda_runtime.h>
 
@@ -11,12 +11,22 @@ void launch_camera(const DevJob* jobs, const WaveChunk* chunks, const WaveDesc* 
                    int maxItems, cudaStream_t s);
 void launch_film_fold(const DevJob* jobs, const WaveChunk* chunks, const WaveDesc* waves, int* curWave, const float* samples, DevStats* st,
                       int maxFold, int advance, cudaStream_t s);
-void launch_trace_closest(const DevJob* jobs, const uint32_t* rayJob, const float4* ro, const float4* rd, const int* count, int* work, float4* hits,
-                          DevStats* stats, cudaStream_t s);
-void launch_trace_shadow(const DevJob* jobs, const uint32_t* rayJob, const float4* ro, const float4* rd, const int* tgt, const int* count, int* work,
-                         float4* nee, DevStats* stats, cudaStream_t s);
-void launch_trace_query(const DevJob* jobs, const float4* ro, const float4* rd, const int* count, int* work, float4* hits, int* occl,
-                        DevStats* stats, bool anyHit, cudaStream_t s);
+// Traversal launch configuration (sst_trace.cu): threads per block (64, 128 or 256), stack
+// entries per thread kept in shared memory (16, 24 or 32), resident blocks per SM (0: as many as fit).
+struct TraceTuning {
+    int block = kTraceBlock;
+    int smemStack = kSmemStack;
+    int blocksPerSM = 0;
+};
+bool traceTuningValid(const TraceTuning& t);
+int traceGrid(const TraceTuning& t);
+int traceMaxBlocksPerSM(const TraceTuning& t);
+void launch_trace_closest(const TraceTuning& t, const DevJob* jobs, const uint32_t* rayJob, const float4* ro, const float4* rd, const int* count,
+                          int* work, float4* hits, DevStats* stats, cudaStream_t s);
+void launch_trace_shadow(const TraceTuning& t, const DevJob* jobs, const uint32_t* rayJob, const float4* ro, const float4* rd, const int* tgt,
+                         const int* count, int* work, float4* nee, DevStats* stats, cudaStream_t s);
+void launch_trace_query(const TraceTuning& t, const DevJob* jobs, const float4* ro, const float4* rd, const int* count, int* work, float4* hits,
+                        int* occl, DevStats* stats, bool anyHit, cudaStream_t s);
 void launch_shade(int ns, bool adj, const DevJob* jobs, const PathBuf& A, const PathBuf& B, const float4* hits, float4* nee, float4* neeG, int cap,
                   float4* shRo, float4* shRd, int* shTgt, uint32_t* shJob, const int* nIn, int* nOut, int* nSh, float* samples, DevStats* stats,
                   int maxItems, cudaStream_t s);
@@ -28,6 +38,5 @@ void launch_debug_env(const DevScene& sc, int n, const float* us, float* dirs, f
                       cudaStream_t s);
 void launch_debug_rng(uint32_t base, uint32_t sample, int n, const uint32_t* pixels, int draws, uint32_t* out, cudaStream_t s);
 void launch_debug_camera(const DevScene& sc, int n, const float* film, float* org, float* dir, cudaStream_t s);
-int traceGrid();
 
 }  // namespace sst

@@ -90,6 +90,14 @@ class PathTracer(Integrator):
         self.last_stats = stats
 
 
+def autotune(scene, integrator, trial_iterations=2):
+    """Chooses the launch configuration (wave capacity, traversal block size, shared stack
+    entries, resident traversal blocks) for rendering `scene` with `integrator` by timing short
+    trial renders, and applies it to the scene's device context.  Images do not depend on it."""
+    integrator._check_hooks()
+    return _native.autotune(scene.native, integrator.params(scene), trial_iterations)
+
+
 def render_batch(pairs):
     """Renders many (scene, PathTracer) pairs in one shared wavefront (sst_render_batch).
 

@@ -329,6 +329,35 @@ def test_validation_scenes(name):
     assert per_path_agreement(g, r, 1e-2, 1e-3) >= 0.97
 
 
+def _relmse_ratio(sc, spp, depth, ref_spp):
+    """relMSE of the GPU render and of the oracle render (same seeds, equal spp) against a
+    converged GPU render with other seeds; returns (ratio, relMSE of the oracle render)."""
+    from seesharp_gb300 import rel_mse
+    ref, _ = render_gpu(sc, ref_spp, depth, seed=0x5EED1234)
+    g, _ = render_gpu(sc, spp, depth)
+    r, _, _ = render_oracle(sc, spp, depth)
+    eg, er = rel_mse(g, ref), rel_mse(r, ref)
+    return eg / er, er
+
+
+def test_relmse_ratio_cornell_box():
+    """Equal relMSE at equal spp: the 256x256, 16 spp, depth-5 Cornell box against a 65536-spp
+    reference; the GPU's relMSE within a factor 1.05 of the oracle's."""
+    sc = workloads.cornell_box(256, 256)
+    sc.Prepare()
+    ratio, er = _relmse_ratio(sc, 16, 5, 65536)
+    assert er > 0 and 1 / 1.05 <= ratio <= 1.05, ratio
+
+
+def test_relmse_ratio_sphere_field_1m_triangles():
+    """The 1M-triangle scene (200 icospheres, 50 emitters, sky) at 256x256, 64 spp, depth 8
+    against a 16384-spp reference (the reference's own noise is 1/256 of the test render's)."""
+    sc = workloads.sphere_field(200, 256, 256)
+    sc.Prepare()
+    ratio, er = _relmse_ratio(sc, 64, 8, 16384)
+    assert er > 0 and 1 / 1.05 <= ratio <= 1.05, ratio
+
+
 def test_sphere_field_paths_match():
     sc = workloads.sphere_field(12, 80, 80, level=3)
     sc.Prepare()
@@ -452,3 +481,45 @@ def test_graph_replay_equals_plain_launches():
         os.environ.pop("SST_GRAPH", None)
         os.environ.pop("SST_WAVE_CAPACITY", None)
     assert np.array_equal(g, p)
+
+
+def test_tuning_and_autotune_leave_images_and_queries_unchanged():
+    """Wave capacity, traversal block size, shared stack entries and resident traversal blocks
+    change the launch shape only: the film and the query results stay bitwise the same."""
+    from seesharp_gb300 import autotune
+    sc = workloads.sphere_field(12, 96, 80, level=3)
+    sc.Prepare()
+    ctx = sc.native.ctx
+    base = _native.get_tuning(ctx)
+    rng = np.random.default_rng(4)
+    rays = np.zeros((4000, 8), np.float32)
+    rays[:, 0:3] = rng.uniform(-10, 10, size=(4000, 3))
+    d = rng.standard_normal((4000, 3))
+    rays[:, 4:7] = d / np.linalg.norm(d, axis=1, keepdims=True)
+    rays[:, 7] = np.inf
+    try:
+        ref, st0 = render_gpu(sc, 4, 6)
+        hits0, occ0 = sc.native.trace(rays), sc.native.occluded(rays)
+        assert st0.numKernelLaunches > 0
+        for t in [dict(traceBlock=64, traceStackShared=16, traceBlocksPerSM=1, waveCapacity=4096),
+                  dict(traceBlock=256, traceStackShared=32, traceBlocksPerSM=0, waveCapacity=0),
+                  dict(traceBlock=128, traceStackShared=24, traceBlocksPerSM=2, waveCapacity=1 << 20)]:
+            _native.set_tuning(ctx, **t)
+            assert _native.get_tuning(ctx) == t
+            img, _ = render_gpu(sc, 4, 6)
+            assert np.array_equal(img, ref), t
+            # SstHit rows hold int32 fields (primId, meshId = -1 on a miss): compare the bits
+            hits, occ = sc.native.trace(rays), sc.native.occluded(rays)
+            assert np.array_equal(hits.view(np.uint32), hits0.view(np.uint32)), t
+            assert np.array_equal(occ, occ0), t
+        _native.set_tuning(ctx, **base)
+        chosen, ms = autotune(sc, PathTracer(TotalSpp=4, MaxDepth=6))
+        assert chosen == _native.get_tuning(ctx) and ms > 0
+        img, _ = render_gpu(sc, 4, 6)
+        assert np.array_equal(img, ref)
+        for bad in (dict(traceBlock=96), dict(traceStackShared=20), dict(waveCapacity=100), dict(traceBlocksPerSM=-1)):
+            with pytest.raises(_native.SstError):
+                _native.set_tuning(ctx, **bad)
+            assert _native.get_tuning(ctx) == chosen
+    finally:
+        _native.set_tuning(ctx, **base)
