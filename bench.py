@@ -32,6 +32,7 @@ CONFIGS = {
     1: dict(name="sphere_field_1Mtri_1024x1024_64spp_depth8", builder="spheres", spheres=200, W=1024, H=1024, spp=64, depth=8),
     2: dict(name="batch_64jobs_10k-1Mtri_128-1024px_4-64spp_depth3-10", builder="batch", jobs=64, seed=2024),
     3: dict(name="cornell_adjoint_tex256_512x512_32spp_depth5", builder="adjoint", W=512, H=512, spp=32, depth=5, tex=256),
+    4: dict(name="large_12.3Mtri_8views_1920x1080_256spp_depth10_adjoint_tex1024_rough2000", builder="large", W=1920, H=1080, spp=256, depth=10),
 }
 
 
@@ -149,6 +150,69 @@ def run_adjoint(args, cfg):
             "backward": {"ms": round(bwd, 3), "Msamples_per_s": round(samples / bwd / 1e3, 3)},
             "e2e": {"value": round(wall * 1e3, 3), "unit": "ms per forward+loss+backward step", "h2d_bytes_per_step": int(dldi.nbytes),
                     "d2h_bytes_per_step": int(img.nbytes + 4 * (dr.n_tex + 4 * dr.n_mat + 3 * dr.n_em))},
+            "clocks": clk.summary()}
+    print(json.dumps(line), flush=True)
+
+
+def run_large(args, cfg):
+    """The large combined job: 8 camera views of the 12.3M-triangle scene rendered in one batch
+    with the path radiance kept (sst_forward_batch), an L2 loss against target views rendered
+    with perturbed parameters, and the batched path-replay backward (sst_backward_batch) to the
+    1024^2 x 3 terrain texture and the 2000 sphere roughness values."""
+    from seesharp_gb300 import PathTracer, workloads
+    from seesharp_gb300.adjoint import DifferentiableRender, l2_loss
+    W, H, spp, depth = cfg["W"], cfg["H"], cfg["spp"], cfg["depth"]
+    t0 = time.perf_counter()
+    sc, tex, mats, views = workloads.large_combined(W, H)
+    gen_s = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    sc.Prepare()
+    prep_s = time.perf_counter() - t0
+    info = sc.native.info()
+    pt = PathTracer(TotalSpp=spp, MaxDepth=depth)
+    tuning, tune_s = None, 0.0
+    if not args.no_autotune:
+        from seesharp_gb300 import _native
+        t0 = time.perf_counter()
+        tuning, _ = _native.autotune(sc.native, pt.params(sc), 1)
+        tune_s = time.perf_counter() - t0
+    dr = DifferentiableRender(sc, pt, texture=tex, roughness_materials=mats, views=views)
+    rng = np.random.default_rng(5)
+    tex0 = tex.Image.data.copy()
+    r0 = np.array([m.MaterialParameters.Roughness.constColor for m in mats])
+    dr.params.baseSeed = 0x5EED
+    targets = dr.forward(np.clip(tex0 * (1 + 0.25 * rng.standard_normal(tex0.shape)), 0.02, 0.98), np.clip(r0 + 0.1 * rng.standard_normal(r0.shape), 0.05, 1.0))
+    dr.params.baseSeed = 0xC030114
+    dr.set_parameters(texture=tex0, roughness=r0)
+
+    def step():
+        imgs = dr.forward()
+        losses = [l2_loss(i, t) for i, t in zip(imgs, targets)]
+        g = dr.backward([d for _, d in losses])
+        assert np.isfinite(g["texture"]).all() and np.isfinite(g["roughness"]).all()
+        return dr.stats_forward.renderTimeMs, dr.stats_backward.renderTimeMs, dr.stats_forward.numKernelLaunches + dr.stats_backward.numKernelLaunches
+
+    for _ in range(args.warmup):
+        step()
+    with ClockSampler(0) as clk:
+        t0 = time.perf_counter()
+        times = [step() for _ in range(args.steps)]
+        wall = (time.perf_counter() - t0) / args.steps
+    fwd = float(np.mean([t[0] for t in times]))
+    bwd = float(np.mean([t[1] for t in times]))
+    samples = len(views) * W * H * spp
+    line = {"metric": "Msamples/s PathTracer, 8 views batched (forward) and adjoint/forward cost", "value": round(samples / fwd / 1e3, 3),
+            "unit": "Msamples/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(fwd + bwd, 3), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scene generator)",
+            "config": {"workload": cfg["name"], "triangles": info["triangles"], "emitters": info["emitters"], "views": len(views), "width": W, "height": H,
+                       "spp": spp, "max_depth": depth, "texture": list(tex0.shape), "roughness_params": len(mats)},
+            "forward": {"ms": round(fwd, 3), "Msamples_per_s": round(samples / fwd / 1e3, 3)},
+            "backward": {"ms": round(bwd, 3), "Msamples_per_s": round(samples / bwd / 1e3, 3)},
+            "adjoint_over_forward": round(bwd / fwd, 3),
+            "gpu_launches": int(sum(t[2] for t in times)),
+            "e2e": {"value": round(samples / wall / 1e6, 3), "unit": "Msamples/s (forward samples per forward+loss+backward second)",
+                    "h2d_bytes_per_step": int(len(views) * W * H * 12), "d2h_bytes_per_step": int(len(views) * W * H * 12 + 4 * (tex0.size + len(mats)))},
+            "setup_s": {"generate": round(gen_s, 2), "prepare": round(prep_s, 2), "autotune": round(tune_s, 2)}, "tuning": tuning,
             "clocks": clk.summary()}
     print(json.dumps(line), flush=True)
 
@@ -479,7 +543,7 @@ def main():
             cfg[k] = a
             cfg["name"] = cfg["name"] + f"_{k}{a}"
     os.environ.setdefault("SST_BVH", "lbvh")
-    if args.impl == "reference" and cfg["builder"] == "adjoint":
+    if args.impl == "reference" and cfg["builder"] in ("adjoint", "large"):
         if dist_info()[1] == 0:
             print(json.dumps({"impl": "reference", "unavailable": "the reference PathTracer has no adjoint (differentiation is new in this library)"}))
     elif args.impl == "reference":
@@ -488,6 +552,8 @@ def main():
         run_batch(args, cfg)
     elif cfg["builder"] == "adjoint":
         run_adjoint(args, cfg)
+    elif cfg["builder"] == "large":
+        run_large(args, cfg)
     else:
         run_ours(args, cfg)
 

@@ -175,14 +175,15 @@ typedef struct SstTuning {
     int32_t traceBlock;       /* threads per traversal block: 64, 128 or 256 */
     int32_t traceStackShared; /* traversal stack entries per thread kept in shared memory: 16, 24 or 32 */
     int32_t traceBlocksPerSM; /* resident traversal blocks per SM; 0 = as many as fit */
+    int32_t traceBvhWidth;    /* BVH traversed: 2 (binary) or 4 (4-wide, same leaves) */
 } SstTuning;
 int sst_get_tuning(sst_ctx* ctx, SstTuning* out);
 /* Invalid values return SST_ERR_INVALID_ARGUMENT and leave the setting unchanged. */
 int sst_set_tuning(sst_ctx* ctx, const SstTuning* tuning);
 /* Chooses the setting for this scene and these parameters by timing trial renders of
  * trialIterations iterations (into a scratch film; the caller's films are not touched):
- * first the traversal variant (block size x shared stack entries), then the resident blocks per
- * SM, then the wave capacity, keeping the fastest of two runs per candidate.  The choice is
+ * first the traversal variant (BVH width x block size x shared stack entries), then the resident
+ * blocks per SM, then the wave capacity, keeping the fastest of two runs per candidate.  The choice is
  * applied to the scene's context and returned in `chosen` (bestTrialMs may be NULL). */
 int sst_autotune(sst_scene* scene, const SstPathTracerParams* params, int32_t trialIterations, SstTuning* chosen, double* bestTrialMs);
 
@@ -215,6 +216,14 @@ int sst_occluded_noalloc(sst_scene* scene, const SstRay* rays, int32_t n, int32_
 int sst_render(sst_scene* scene, const SstPathTracerParams* params, float* film, int32_t memory,
                SstRenderStats* stats);
 
+/* A camera view for one job of a batch (PerspectiveCamera(worldToCamera, fov), as
+ * sst_scene_set_camera); the image size is the job's width and height. */
+typedef struct SstCamera {
+    float worldToCamera[16];
+    float verticalFovDegrees;
+    int32_t reserved;
+} SstCamera;
+
 /* One render job of a batch. */
 typedef struct SstRenderJob {
     sst_scene* scene;
@@ -222,6 +231,7 @@ typedef struct SstRenderJob {
     float* film;
     int32_t memory;
     int32_t reserved;
+    const SstCamera* camera; /* NULL: the scene's camera; otherwise this view of the scene */
 } SstRenderJob;
 /* Renders many independent jobs (uneven resolutions, spp and depths) in one persistent
  * wavefront: all jobs' paths share the ray queues.  Films as in sst_render. */
@@ -242,6 +252,15 @@ typedef struct SstGradients {
     int32_t memory;           /* SST_MEM_HOST / SST_MEM_DEVICE for the arrays above */
     int32_t reserved;
 } SstGradients;
+/* Batched forms over many jobs (for example several camera views of one scene) in one shared
+ * wavefront.  sst_forward_batch renders every job like sst_forward and keeps each job's path
+ * radiance; sst_backward_batch takes one dLoss/dImage per job (the jobs must equal those of the
+ * last sst_forward_batch on the context).  The gradients of a scene are summed over all of its
+ * jobs and written to the SstGradients of the scene's first job in the list; the entries of its
+ * other jobs are not used. */
+int sst_forward_batch(sst_ctx* ctx, const SstRenderJob* jobs, int32_t numJobs, SstRenderStats* stats);
+int sst_backward_batch(sst_ctx* ctx, const SstRenderJob* jobs, int32_t numJobs, const float* const* dLossDImage, int32_t memory,
+                       SstGradients* grads, SstRenderStats* stats);
 /* Overwrites the texels of a texture (same size and channels as when it was added). */
 int sst_scene_update_texture(sst_scene* scene, int32_t texture, const float* data);
 /* sst_render of iterations [0, totalSpp) that also keeps every path's radiance for the replay. */

@@ -71,15 +71,19 @@ class SstGradients(ctypes.Structure):
 
 class SstTuning(ctypes.Structure):
     _fields_ = [("waveCapacity", ctypes.c_int32), ("traceBlock", ctypes.c_int32), ("traceStackShared", ctypes.c_int32),
-                ("traceBlocksPerSM", ctypes.c_int32)]
+                ("traceBlocksPerSM", ctypes.c_int32), ("traceBvhWidth", ctypes.c_int32)]
 
     def as_dict(self):
         return {k: int(getattr(self, k)) for k, _ in self._fields_}
 
 
+class SstCamera(ctypes.Structure):
+    _fields_ = [("worldToCamera", ctypes.c_float * 16), ("verticalFovDegrees", ctypes.c_float), ("reserved", ctypes.c_int32)]
+
+
 class SstRenderJob(ctypes.Structure):
     _fields_ = [("scene", ctypes.c_void_p), ("params", SstPathTracerParams), ("film", ctypes.c_void_p), ("memory", ctypes.c_int32),
-                ("reserved", ctypes.c_int32)]
+                ("reserved", ctypes.c_int32), ("camera", ctypes.POINTER(SstCamera))]
 
 
 # Every exported symbol with its argument types (restype int unless noted).
@@ -113,6 +117,8 @@ SIGNATURES = {
     "sst_render": [_vp, _P(SstPathTracerParams), _vp, _i32, _P(SstRenderStats)],
     "sst_render_batch": [_vp, _P(SstRenderJob), _i32, _P(SstRenderStats)],
     "sst_scene_update_texture": [_vp, _i32, _vp],
+    "sst_forward_batch": [_vp, _vp, _i32, _P(SstRenderStats)],
+    "sst_backward_batch": [_vp, _vp, _i32, _vp, _i32, _vp, _P(SstRenderStats)],
     "sst_forward": [_vp, _P(SstPathTracerParams), _vp, _i32, _P(SstRenderStats)],
     "sst_backward": [_vp, _P(SstPathTracerParams), _vp, _i32, _P(SstGradients), _P(SstRenderStats)],
     "sst_get_tuning": [_vp, _P(SstTuning)],
@@ -402,17 +408,73 @@ class SceneHandle:
         return stats
 
 
-def render_batch(ctx, jobs):
-    """jobs: list of (SceneHandle, SstPathTracerParams, film_ptr, memory).  One shared wavefront."""
+def make_camera(world_to_camera, fov):
+    c = SstCamera()
+    c.worldToCamera[:] = [float(x) for x in np.asarray(world_to_camera, np.float32).reshape(16)]
+    c.verticalFovDegrees = float(fov)
+    return c
+
+
+def _job_array(jobs):
+    """jobs: list of (SceneHandle, SstPathTracerParams, film_ptr, memory[, SstCamera or None])."""
     arr = (SstRenderJob * len(jobs))()
-    for k, (sh, params, film, mem) in enumerate(jobs):
+    keep = []
+    for k, job in enumerate(jobs):
+        sh, params, film, mem = job[:4]
+        cam = job[4] if len(job) > 4 else None
         arr[k].scene = sh.handle
         arr[k].params = params
         arr[k].film = film
         arr[k].memory = mem
+        if cam is not None:
+            keep.append(cam)
+            arr[k].camera = ctypes.pointer(cam)
+    return arr, keep
+
+
+def render_batch(ctx, jobs):
+    """One shared wavefront over jobs (SceneHandle, params, film_ptr, memory[, camera view])."""
+    arr, _keep = _job_array(jobs)
     stats = SstRenderStats()
     check(ctx.lib.sst_render_batch(ctx.handle, arr, len(jobs), ctypes.byref(stats)))
     return stats
+
+
+def forward_batch(ctx, jobs):
+    arr, _keep = _job_array(jobs)
+    stats = SstRenderStats()
+    check(ctx.lib.sst_forward_batch(ctx.handle, arr, len(jobs), ctypes.byref(stats)))
+    return stats
+
+
+def backward_batch(ctx, jobs, dldis, n_tex, n_mat, n_em):
+    """dldis: one (H, W, 3) float32 host array per job.  Returns per distinct scene (in order of
+    first appearance) the host gradient arrays, summed over the scene's jobs, and the stats."""
+    arr, _keep = _job_array(jobs)
+    ds = [np.ascontiguousarray(d, np.float32) for d in dldis]
+    dp = (ctypes.c_void_p * len(ds))(*[d.ctypes.data for d in ds])
+    grads = (SstGradients * len(jobs))()
+    outs, seen = [], {}
+    for k, job in enumerate(jobs):
+        key = id(job[0])
+        if key in seen:
+            continue
+        o = {"textures": np.zeros(max(n_tex, 1), np.float32), "materialBaseColor": np.zeros(max(3 * n_mat, 1), np.float32),
+             "materialRoughness": np.zeros(max(n_mat, 1), np.float32), "emitterRadiance": np.zeros(max(3 * n_em, 1), np.float32)}
+        g = grads[k]
+        g.textures, g.materialBaseColor = o["textures"].ctypes.data, o["materialBaseColor"].ctypes.data
+        g.materialRoughness, g.emitterRadiance = o["materialRoughness"].ctypes.data, o["emitterRadiance"].ctypes.data
+        g.memory = SST_MEM_HOST
+        seen[key] = len(outs)
+        outs.append(o)
+    stats = SstRenderStats()
+    check(ctx.lib.sst_backward_batch(ctx.handle, arr, len(jobs), dp, SST_MEM_HOST, grads, ctypes.byref(stats)))
+    for o in outs:
+        o["textures"] = o["textures"][:n_tex]
+        o["materialBaseColor"] = o["materialBaseColor"][:3 * n_mat].reshape(-1, 3)
+        o["materialRoughness"] = o["materialRoughness"][:n_mat]
+        o["emitterRadiance"] = o["emitterRadiance"][:3 * n_em].reshape(-1, 3)
+    return outs, stats
 
 
 def make_params(width, height, totalSpp, maxDepth, minDepth=1, baseSeed=0xC030114, numShadowRays=1, enableBsdfDI=True,

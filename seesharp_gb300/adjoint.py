@@ -15,10 +15,12 @@ from .images import RgbColor
 
 
 class DifferentiableRender:
-    def __init__(self, scene, integrator, texture=None, roughness_materials=(), emitters=()):
+    def __init__(self, scene, integrator, texture=None, roughness_materials=(), emitters=(), views=None):
         """texture: the TextureRgb whose image is a parameter (or None); roughness_materials:
         GenericMaterials whose constant roughness is a parameter; emitters: list of groups, each a
-        list of Emitter objects sharing one RGB radiance parameter."""
+        list of Emitter objects sharing one RGB radiance parameter; views: None (the scene's
+        camera) or a list of (worldToCamera, fov) camera views rendered in one batch, in which
+        case forward returns one image per view and backward takes one dLoss/dImage per view."""
         self.scene = scene
         self.pt = integrator
         self.texture = texture
@@ -37,6 +39,7 @@ class DifferentiableRender:
         self.tex_offset = None if self.tex_id is None else int(sum(sizes[:self.tex_id]))
         self.stats_forward = None
         self.stats_backward = None
+        self.views = None if views is None else [_native.make_camera(m, f) for m, f in views]
 
     def set_parameters(self, texture=None, roughness=None, radiance=None):
         sc = self.scene.native
@@ -55,15 +58,27 @@ class DifferentiableRender:
                     e.Radiance = RgbColor(r)
                     sc.set_emitter_radiance(k, r)
 
+    def _jobs(self, films):
+        sh = self.scene.native
+        return [(sh, self.params, f.ctypes.data, _native.SST_MEM_HOST, v) for f, v in zip(films, self.views)]
+
     def forward(self, texture=None, roughness=None, radiance=None):
         self.set_parameters(texture, roughness, radiance)
         fb = self.scene.FrameBuffer
+        if self.views is not None:
+            self._films = [np.zeros((fb.Height, fb.Width, 3), np.float32) for _ in self.views]
+            self.stats_forward = _native.forward_batch(self.scene.native.ctx, self._jobs(self._films))
+            return [f.copy() for f in self._films]
         film = np.zeros((fb.Height, fb.Width, 3), np.float32)
         self.stats_forward = self.scene.native.forward(self.params, film.ctypes.data)
         return film
 
     def backward(self, dloss_dimage):
-        g, st = self.scene.native.backward(self.params, dloss_dimage, self.n_tex, self.n_mat, self.n_em)
+        if self.views is not None:
+            outs, st = _native.backward_batch(self.scene.native.ctx, self._jobs(self._films), dloss_dimage, self.n_tex, self.n_mat, self.n_em)
+            g = outs[0]
+        else:
+            g, st = self.scene.native.backward(self.params, dloss_dimage, self.n_tex, self.n_mat, self.n_em)
         self.stats_backward = st
         out = {}
         if self.texture is not None:

@@ -92,6 +92,14 @@ struct DevBuf {
 // ---------------------------------------------------------------------------------------------
 // context
 // ---------------------------------------------------------------------------------------------
+// A job of the last sst_forward_batch (what sst_backward_batch must match).
+struct BatchSig {
+    sst_scene* scene;
+    SstPathTracerParams params;
+    bool hasCam;
+    SstCamera cam;
+};
+
 struct sst_ctx {
     int device = 0;
     cudaStream_t stream = nullptr;
@@ -106,6 +114,9 @@ struct sst_ctx {
     DevBuf scratchIn, scratchOut, scratchOut2;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     int* pinnedCount = nullptr;
+    // batched adjoint: the jobs of the last sst_forward_batch, their path radiance, dLoss/dImage
+    std::vector<BatchSig> batchSig;
+    std::vector<std::unique_ptr<DevBuf>> batchRecord, batchDLdI;
     // launch configuration (sst_set_tuning / sst_autotune)
     TraceTuning trace;
     int waveCapacity = 0;  // 0: the default
@@ -181,9 +192,9 @@ struct sst_scene {
     bool committed = false;
     int W = 0, H = 0;
     // device
-    DevBuf nodes, triv, triN, triAux, triVtx, vnrm, vuv, mats, texs, texData, ems, envImg, envRowCdf, envColCdf, envHasCol, envRowMarg, queryJob;
+    DevBuf nodes, nodes4, triv, triN, triAux, triVtx, vnrm, vuv, mats, texs, texData, ems, envImg, envRowCdf, envColCdf, envHasCol, envRowMarg, queryJob;
     DevScene dev{};
-    int nTri = 0, nNodes = 0, bvhDepth = 0;
+    int nTri = 0, nNodes = 0, bvhDepth = 0, nNodes4 = 0, bvh4Depth = 0;
     // adjoint: per-path radiance of the last sst_forward and its settings
     DevBuf record, gTex, gMatBase, gMatRough, gEmitter, dLdI;
     bool recordValid = false;
@@ -404,6 +415,18 @@ struct BvhBuilder {
 // ---------------------------------------------------------------------------------------------
 // scene commit
 // ---------------------------------------------------------------------------------------------
+// Camera matrices of a perspective view (Camera.cs:34-42, PerspectiveCamera.cs:42-52).
+static DevCamera makeCamera(const float w2c[16], float fovDeg, int W, int H) {
+    DevCamera cam{};
+    float c2v[16];
+    if (!invert4(w2c, cam.c2w)) fail(SST_ERR_INVALID_ARGUMENT, "World to camera transform must be invertible.");
+    perspective(fovDeg * 3.14159265f / 180.0f, float(W) / float(H), 0.001f, 1000.0f, c2v);
+    if (!invert4(c2v, cam.v2c)) fail(SST_ERR_INVALID_ARGUMENT, "degenerate projection");
+    cam.W = W;
+    cam.H = H;
+    return cam;
+}
+
 static void commitScene(sst_scene* s, int W, int H) {
     if (W <= 0 || H <= 0) fail(SST_ERR_INVALID_ARGUMENT, "frame buffer size must be positive");
     // Scene.IsValid (Scene.cs:170-197)
@@ -523,6 +546,16 @@ static void commitScene(sst_scene* s, int W, int H) {
         s->triAux.upload(triAux, st);
         s->triVtx.upload(triVtx, st);
     }
+    // 4-wide BVH over the same leaves (the traversal variant picked by the launch tuning)
+    s->nNodes4 = 0;
+    s->bvh4Depth = 0;
+    if (s->nNodes > 0) {
+        DevBuf scratch4;
+        s->nodes4.ensure(sizeof(float4) * 8 * size_t(s->nNodes));
+        scratch4.ensure(bvh4ScratchBytes(s->nNodes));
+        int rc = buildBvh4(s->nodes.as<float4>(), s->nNodes, s->nodes4.as<float4>(), scratch4.p, &s->nNodes4, &s->bvh4Depth, st);
+        if (rc != 0) fail(SST_ERR_CUDA, "4-wide BVH build failed (" + std::to_string(rc) + "): " + cudaGetErrorString(cudaGetLastError()));
+    }
     std::vector<float> vnrm, vuv;
     if (anyNormals) {
         vnrm.assign(3 * size_t(nv), 0.f);
@@ -596,6 +629,8 @@ static void commitScene(sst_scene* s, int W, int H) {
     d.nEmitters = int(s->emitters.size());
     d.nTri = nt;
     d.nNodes = s->nNodes;
+    d.nodes4 = s->nNodes4 > 0 ? s->nodes4.as<float4>() : nullptr;
+    d.nNodes4 = s->nNodes4;
     // environment map (EnvironmentMap.cs:139-156)
     d.hasEnv = s->envW > 0;
     if (d.hasEnv) {
@@ -616,13 +651,7 @@ static void commitScene(sst_scene* s, int W, int H) {
         d.env.colCdf = s->envColCdf.as<float>();
         d.env.hasCol = s->envHasCol.as<int>();
     }
-    // camera (Camera.cs:34-42, PerspectiveCamera.cs:42-52)
-    float c2v[16];
-    if (!invert4(s->w2c, d.cam.c2w)) fail(SST_ERR_INVALID_ARGUMENT, "World to camera transform must be invertible.");
-    perspective(s->fovDeg * 3.14159265f / 180.0f, float(W) / float(H), 0.001f, 1000.0f, c2v);
-    if (!invert4(c2v, d.cam.v2c)) fail(SST_ERR_INVALID_ARGUMENT, "degenerate projection");
-    d.cam.W = W;
-    d.cam.H = H;
+    d.cam = makeCamera(s->w2c, s->fovDeg, W, H);
     CUDA_CHECK(cudaStreamSynchronize(st));
     s->W = W;
     s->H = H;
@@ -703,6 +732,8 @@ struct JobIn {
     int iterFirst, iterEnd;
     int done = 0;  // iterations rendered
     DevAdj adj{};  // adjoint buffers (forward record or replay)
+    bool hasCam = false;  // a camera view that replaces the scene's camera for this job
+    DevCamera cam{};
 };
 
 // Splits the (job, iteration, pixel) paths into waves of at most `cap` paths.  A job whose
@@ -790,6 +821,7 @@ static void renderJobs(sst_ctx* c, std::vector<JobIn>& jobs, SstRenderStats* out
     for (size_t k = 0; k < jobs.size(); ++k) {
         const SstPathTracerParams* P = &jobs[k].p;
         hj[k].sc = jobs[k].s->dev;
+        if (jobs[k].hasCam) hj[k].sc.cam = jobs[k].cam;
         hj[k].cfg = PTConfig{P->width, P->height, P->maxDepth, P->minDepth, P->baseSeed, P->numShadowRays, P->enableBsdfDI, P->ignoreNanAndInf};
         hj[k].adj = jobs[k].adj;
     }
@@ -1336,10 +1368,11 @@ int sst_render(sst_scene* s, const SstPathTracerParams* p, float* film, int32_t 
     });
 }
 
-static TraceTuning toTrace(const SstTuning& t) { return TraceTuning{t.traceBlock, t.traceStackShared, t.traceBlocksPerSM}; }
+static TraceTuning toTrace(const SstTuning& t) { return TraceTuning{t.traceBlock, t.traceStackShared, t.traceBlocksPerSM, t.traceBvhWidth}; }
 
 static void checkTuning(const SstTuning& t) {
-    if (!traceTuningValid(toTrace(t))) fail(SST_ERR_INVALID_ARGUMENT, "traceBlock must be 64, 128 or 256 and traceStackShared 16, 24 or 32");
+    if (!traceTuningValid(toTrace(t)))
+        fail(SST_ERR_INVALID_ARGUMENT, "traceBlock must be 64, 128 or 256, traceStackShared 16, 24 or 32, and traceBvhWidth 2 or 4");
     if (t.waveCapacity != 0 && (t.waveCapacity < 1024 || t.waveCapacity > (1 << 24)))
         fail(SST_ERR_INVALID_ARGUMENT, "waveCapacity must be 0 or in [1024, 2^24]");
     if (t.traceBlocksPerSM < 0 || t.traceBlocksPerSM > 64) fail(SST_ERR_INVALID_ARGUMENT, "traceBlocksPerSM must be in [0, 64]");
@@ -1351,6 +1384,7 @@ static SstTuning currentTuning(const sst_ctx* c) {
     t.traceBlock = c->trace.block;
     t.traceStackShared = c->trace.smemStack;
     t.traceBlocksPerSM = c->trace.blocksPerSM;
+    t.traceBvhWidth = c->trace.width;
     return t;
 }
 
@@ -1407,15 +1441,17 @@ int sst_autotune(sst_scene* s, const SstPathTracerParams* p, int32_t trialIterat
         double bestMs = 1e300;
         try {
             // traversal variant
-            for (int b : {64, 128, 256})
-                for (int k : {16, 24, 32}) {
-                    SstTuning t = best;
-                    t.traceBlock = b;
-                    t.traceStackShared = k;
-                    t.traceBlocksPerSM = 0;
-                    double ms = trial(t);
-                    if (ms < bestMs) { bestMs = ms; best = t; }
-                }
+            for (int wdt : {2, 4})
+                for (int b : {64, 128, 256})
+                    for (int k : {16, 24, 32}) {
+                        SstTuning t = best;
+                        t.traceBvhWidth = wdt;
+                        t.traceBlock = b;
+                        t.traceStackShared = k;
+                        t.traceBlocksPerSM = 0;
+                        double ms = trial(t);
+                        if (ms < bestMs) { bestMs = ms; best = t; }
+                    }
             // resident traversal blocks per SM
             int m = traceMaxBlocksPerSM(toTrace(best));
             for (int bps : {m / 2, (3 * m) / 4}) {
@@ -1450,53 +1486,193 @@ int sst_autotune(sst_scene* s, const SstPathTracerParams* p, int32_t trialIterat
     });
 }
 
+static size_t texPoolFloats(const sst_scene* s) {
+    size_t n = 0;
+    for (auto& t : s->textures) n += t.data.size();
+    return n;
+}
+
+// Validates the jobs of a batch and fills the renderer's job list.  Films given in host memory
+// are staged in device buffers (`staged`); with fromZero every film starts black.
+static void batchJobs(sst_ctx* ctx, const SstRenderJob* jobs, int numJobs, std::vector<JobIn>& in, std::vector<std::unique_ptr<DevBuf>>& staged,
+                      bool fromZero) {
+    if (!ctx || (numJobs > 0 && !jobs) || numJobs < 0) fail(SST_ERR_INVALID_ARGUMENT, "invalid batch");
+    in.assign(numJobs, JobIn{});
+    staged.resize(numJobs);
+    for (int j = 0; j < numJobs; ++j) {
+        const SstRenderJob& J = jobs[j];
+        if (!J.scene || !J.film) fail(SST_ERR_INVALID_ARGUMENT, "job " + std::to_string(j) + ": NULL scene or film");
+        if (J.scene->ctx != ctx) fail(SST_ERR_INVALID_ARGUMENT, "job " + std::to_string(j) + ": scene belongs to another context");
+        checkParams(J.scene, &J.params);
+        if (fromZero && (J.params.firstIteration != 0 || J.params.maximumRenderTimeMs > 0))
+            fail(SST_ERR_UNSUPPORTED, "job " + std::to_string(j) + ": the adjoint renders all iterations from zero");
+        size_t filmBytes = size_t(J.params.width) * J.params.height * 3 * sizeof(float);
+        float* dFilm = J.film;
+        if (J.memory != SST_MEM_DEVICE) {
+            staged[j].reset(new DevBuf());
+            staged[j]->ensure(filmBytes);
+            dFilm = staged[j]->as<float>();
+            if (J.params.firstIteration > 0) CUDA_CHECK(cudaMemcpyAsync(dFilm, J.film, filmBytes, cudaMemcpyHostToDevice, ctx->stream));
+            else CUDA_CHECK(cudaMemsetAsync(dFilm, 0, filmBytes, ctx->stream));
+        } else if (J.params.firstIteration == 0) {
+            CUDA_CHECK(cudaMemsetAsync(dFilm, 0, filmBytes, ctx->stream));
+        }
+        in[j].s = J.scene;
+        in[j].p = J.params;
+        in[j].dFilm = dFilm;
+        in[j].iterFirst = J.params.firstIteration;
+        in[j].iterEnd = std::max(J.params.firstIteration, J.params.totalSpp);
+        if (J.camera) {
+            in[j].hasCam = true;
+            in[j].cam = makeCamera(J.camera->worldToCamera, J.camera->verticalFovDegrees, J.params.width, J.params.height);
+        }
+    }
+}
+
+// Copies the staged films of host-memory jobs back.
+static void batchFilmsOut(sst_ctx* ctx, const SstRenderJob* jobs, int numJobs, const std::vector<JobIn>& in) {
+    for (int j = 0; j < numJobs; ++j) {
+        if (jobs[j].memory != SST_MEM_DEVICE) {
+            size_t filmBytes = size_t(jobs[j].params.width) * jobs[j].params.height * 3 * sizeof(float);
+            CUDA_CHECK(cudaMemcpyAsync(jobs[j].film, in[j].dFilm, filmBytes, cudaMemcpyDeviceToHost, ctx->stream));
+        }
+    }
+    CUDA_CHECK(cudaStreamSynchronize(ctx->stream));
+}
+
+static SstRenderStats emptyStats() {
+    SstRenderStats t{};
+    for (int k = 0; k < 4; ++k) { t.nanPixel[k] = -1; t.nanIteration[k] = -1; }
+    return t;
+}
+
 int sst_render_batch(sst_ctx* ctx, const SstRenderJob* jobs, int32_t numJobs, SstRenderStats* stats) {
     return guarded([&] {
-        if (!ctx || (numJobs > 0 && !jobs) || numJobs < 0) fail(SST_ERR_INVALID_ARGUMENT, "invalid batch");
+        if (!ctx) fail(SST_ERR_INVALID_ARGUMENT, "invalid batch");
         CUDA_CHECK(cudaSetDevice(ctx->device));
-        SstRenderStats total{};
-        for (int k = 0; k < 4; ++k) { total.nanPixel[k] = -1; total.nanIteration[k] = -1; }
-        std::vector<JobIn> in(numJobs);
-        std::vector<std::unique_ptr<DevBuf>> hostFilms(numJobs);
+        SstRenderStats total = emptyStats();
+        std::vector<JobIn> in;
+        std::vector<std::unique_ptr<DevBuf>> staged;
         auto t0 = std::chrono::steady_clock::now();
-        for (int j = 0; j < numJobs; ++j) {
-            const SstRenderJob& J = jobs[j];
-            if (!J.scene || !J.film) fail(SST_ERR_INVALID_ARGUMENT, "job " + std::to_string(j) + ": NULL scene or film");
-            if (J.scene->ctx != ctx) fail(SST_ERR_INVALID_ARGUMENT, "job " + std::to_string(j) + ": scene belongs to another context");
-            checkParams(J.scene, &J.params);
-            size_t filmBytes = size_t(J.params.width) * J.params.height * 3 * sizeof(float);
-            float* dFilm = J.film;
-            if (J.memory != SST_MEM_DEVICE) {
-                hostFilms[j].reset(new DevBuf());
-                hostFilms[j]->ensure(filmBytes);
-                dFilm = hostFilms[j]->as<float>();
-                if (J.params.firstIteration > 0) CUDA_CHECK(cudaMemcpyAsync(dFilm, J.film, filmBytes, cudaMemcpyHostToDevice, ctx->stream));
-                else CUDA_CHECK(cudaMemsetAsync(dFilm, 0, filmBytes, ctx->stream));
-            } else if (J.params.firstIteration == 0) {
-                CUDA_CHECK(cudaMemsetAsync(dFilm, 0, filmBytes, ctx->stream));
-            }
-            in[j].s = J.scene;
-            in[j].p = J.params;
-            in[j].dFilm = dFilm;
-            in[j].iterFirst = J.params.firstIteration;
-            in[j].iterEnd = std::max(J.params.firstIteration, J.params.totalSpp);
-        }
+        batchJobs(ctx, jobs, numJobs, in, staged, false);
         CUDA_CHECK(cudaStreamSynchronize(ctx->stream));
         double fbMs = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
         renderJobs(ctx, in, &total);
         auto t1 = std::chrono::steady_clock::now();
-        for (int j = 0; j < numJobs; ++j) {
-            if (jobs[j].memory != SST_MEM_DEVICE) {
-                size_t filmBytes = size_t(jobs[j].params.width) * jobs[j].params.height * 3 * sizeof(float);
-                CUDA_CHECK(cudaMemcpyAsync(jobs[j].film, in[j].dFilm, filmBytes, cudaMemcpyDeviceToHost, ctx->stream));
-            }
-        }
-        CUDA_CHECK(cudaStreamSynchronize(ctx->stream));
+        batchFilmsOut(ctx, jobs, numJobs, in);
         fbMs += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t1).count();
         total.frameBufferTimeMs = fbMs;
         int it = 0;
         for (auto& j : in) it += j.done;
         total.numIterations = it;
+        if (stats) *stats = total;
+    });
+}
+
+static bool sameJob(const BatchSig& a, const SstRenderJob& J) {
+    const SstPathTracerParams &r = a.params, *p = &J.params;
+    if (a.scene != J.scene || r.width != p->width || r.height != p->height || r.totalSpp != p->totalSpp || r.maxDepth != p->maxDepth ||
+        r.minDepth != p->minDepth || r.baseSeed != p->baseSeed || r.numShadowRays != p->numShadowRays || r.enableBsdfDI != p->enableBsdfDI)
+        return false;
+    if (a.hasCam != (J.camera != nullptr)) return false;
+    return !a.hasCam || std::memcmp(&a.cam, J.camera, sizeof(SstCamera)) == 0;
+}
+
+int sst_forward_batch(sst_ctx* ctx, const SstRenderJob* jobs, int32_t numJobs, SstRenderStats* stats) {
+    return guarded([&] {
+        if (!ctx) fail(SST_ERR_INVALID_ARGUMENT, "invalid batch");
+        CUDA_CHECK(cudaSetDevice(ctx->device));
+        ctx->batchSig.clear();
+        std::vector<JobIn> in;
+        std::vector<std::unique_ptr<DevBuf>> staged;
+        batchJobs(ctx, jobs, numJobs, in, staged, true);
+        if ((int)ctx->batchRecord.size() < numJobs) ctx->batchRecord.resize(numJobs);
+        for (int j = 0; j < numJobs; ++j) {
+            size_t P = size_t(jobs[j].params.width) * jobs[j].params.height;
+            if (!ctx->batchRecord[j]) ctx->batchRecord[j].reset(new DevBuf());
+            ctx->batchRecord[j]->ensure(std::max<size_t>(1, P * size_t(jobs[j].params.totalSpp) * 12));
+            in[j].adj.record = ctx->batchRecord[j]->as<float>();
+        }
+        SstRenderStats total = emptyStats();
+        renderJobs(ctx, in, &total);
+        batchFilmsOut(ctx, jobs, numJobs, in);
+        for (int j = 0; j < numJobs; ++j) {
+            BatchSig sig{};
+            sig.scene = jobs[j].scene;
+            sig.params = jobs[j].params;
+            sig.hasCam = jobs[j].camera != nullptr;
+            if (sig.hasCam) sig.cam = *jobs[j].camera;
+            ctx->batchSig.push_back(sig);
+        }
+        int it = 0;
+        for (auto& j : in) it += j.done;
+        total.numIterations = it;
+        if (stats) *stats = total;
+    });
+}
+
+int sst_backward_batch(sst_ctx* ctx, const SstRenderJob* jobs, int32_t numJobs, const float* const* dLdI, int32_t memory, SstGradients* grads,
+                       SstRenderStats* stats) {
+    return guarded([&] {
+        if (!ctx || !jobs || numJobs <= 0 || !dLdI || !grads) fail(SST_ERR_INVALID_ARGUMENT, "invalid batch");
+        if ((int)ctx->batchSig.size() != numJobs) fail(SST_ERR_INVALID_ARGUMENT, "sst_backward_batch needs a preceding sst_forward_batch with the same jobs");
+        for (int j = 0; j < numJobs; ++j)
+            if (!sameJob(ctx->batchSig[j], jobs[j]) || !dLdI[j])
+                fail(SST_ERR_INVALID_ARGUMENT, "job " + std::to_string(j) + " differs from the last sst_forward_batch (or has no dLoss/dImage)");
+        CUDA_CHECK(cudaSetDevice(ctx->device));
+        cudaStream_t st = ctx->stream;
+        std::vector<JobIn> in;
+        std::vector<std::unique_ptr<DevBuf>> staged;
+        batchJobs(ctx, jobs, numJobs, in, staged, true);
+        if ((int)ctx->batchDLdI.size() < numJobs) ctx->batchDLdI.resize(numJobs);
+        // gradient buffers of each distinct scene, zeroed once
+        std::vector<sst_scene*> scenes;
+        std::vector<int> firstJob;
+        for (int j = 0; j < numJobs; ++j) {
+            sst_scene* s = jobs[j].scene;
+            if (std::find(scenes.begin(), scenes.end(), s) != scenes.end()) continue;
+            scenes.push_back(s);
+            firstJob.push_back(j);
+            size_t nTex = texPoolFloats(s), nMat = s->materials.size(), nEm = s->emitters.size();
+            s->gTex.ensure(std::max<size_t>(1, nTex * 4));
+            s->gMatBase.ensure(std::max<size_t>(1, nMat * 12));
+            s->gMatRough.ensure(std::max<size_t>(1, nMat * 4));
+            s->gEmitter.ensure(std::max<size_t>(1, nEm * 12));
+            CUDA_CHECK(cudaMemsetAsync(s->gTex.p, 0, std::max<size_t>(1, nTex * 4), st));
+            CUDA_CHECK(cudaMemsetAsync(s->gMatBase.p, 0, std::max<size_t>(1, nMat * 12), st));
+            CUDA_CHECK(cudaMemsetAsync(s->gMatRough.p, 0, std::max<size_t>(1, nMat * 4), st));
+            CUDA_CHECK(cudaMemsetAsync(s->gEmitter.p, 0, std::max<size_t>(1, nEm * 12), st));
+        }
+        for (int j = 0; j < numJobs; ++j) {
+            sst_scene* s = jobs[j].scene;
+            size_t P = size_t(jobs[j].params.width) * jobs[j].params.height;
+            if (!ctx->batchDLdI[j]) ctx->batchDLdI[j].reset(new DevBuf());
+            in[j].dFilm = nullptr;
+            DevAdj& a = in[j].adj;
+            a.record = ctx->batchRecord[j]->as<float>();
+            a.dLdI = toDevice(ctx, *ctx->batchDLdI[j], dLdI[j], P * 3, memory);
+            a.invSpp = 1.0f / float(std::max(1, jobs[j].params.totalSpp));
+            a.gTex = s->gTex.as<float>();
+            a.gMatBase = s->gMatBase.as<float>();
+            a.gMatRough = s->gMatRough.as<float>();
+            a.gEmitter = s->gEmitter.as<float>();
+        }
+        SstRenderStats total = emptyStats();
+        renderJobs(ctx, in, &total, true);
+        for (size_t k = 0; k < scenes.size(); ++k) {
+            sst_scene* s = scenes[k];
+            SstGradients& g = grads[firstJob[k]];
+            size_t nTex = texPoolFloats(s), nMat = s->materials.size(), nEm = s->emitters.size();
+            auto out = [&](float* dst, const DevBuf& src, size_t n) {
+                if (!dst || n == 0) return;
+                CUDA_CHECK(cudaMemcpyAsync(dst, src.p, n * 4, g.memory == SST_MEM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, st));
+            };
+            out(g.textures, s->gTex, nTex);
+            out(g.materialBaseColor, s->gMatBase, nMat * 3);
+            out(g.materialRoughness, s->gMatRough, nMat);
+            out(g.emitterRadiance, s->gEmitter, nEm * 3);
+        }
+        CUDA_CHECK(cudaStreamSynchronize(st));
         if (stats) *stats = total;
     });
 }
@@ -1516,11 +1692,6 @@ int sst_scene_update_texture(sst_scene* s, int32_t texture, const float* data) {
     });
 }
 
-static size_t texPoolFloats(const sst_scene* s) {
-    size_t n = 0;
-    for (auto& t : s->textures) n += t.data.size();
-    return n;
-}
 
 int sst_forward(sst_scene* s, const SstPathTracerParams* p, float* film, int32_t memory, SstRenderStats* stats) {
     return guarded([&] {

@@ -13,6 +13,7 @@
 //      child boxes in the parent, 64-byte nodes); a collapsed subtree becomes one leaf reference
 //      to its contiguous range of sorted triangles.
 #include <cub/cub.cuh>
+#include <algorithm>
 #include <cuda_runtime.h>
 
 #include "sst_bvh.h"
@@ -353,5 +354,110 @@ void launch_leaf_gather(const int* order, int n, const float4* trivG, const floa
                         float4* triN, int4* aux, int4* vtx, cudaStream_t st) {
     if (n <= 0) return;
     k_leaf_gather<<<(n + 255) / 256, 256, 0, st>>>(order, n, trivG, triNG, auxG, vtxG, triv, triN, aux, vtx);
+}
+}  // namespace sst
+
+// =============================================================================================
+// 4-wide BVH from the binary one.  Each 4-wide node is made from a binary inner node by opening
+// its inner children with the largest surface area until it has four children (or only leaves
+// remain); leaves are shared unchanged.  Level-synchronous: one launch per level of the 4-wide
+// tree, the frontier holds (binary node, 4-wide slot) pairs.
+// Node layout (8 float4, 128 bytes): lo.x[4], hi.x[4], lo.y[4], hi.y[4], lo.z[4], hi.z[4],
+// child references[4] (a 4-wide node index or a leaf reference), (number of children, -, -, -).
+// =============================================================================================
+namespace sst {
+namespace {
+struct Child4 {
+    uint32_t ref;
+    float lo[3], hi[3];
+};
+__device__ float halfArea(const Child4& c) {
+    float dx = c.hi[0] - c.lo[0], dy = c.hi[1] - c.lo[1], dz = c.hi[2] - c.lo[2];
+    return dx * dy + dy * dz + dz * dx;
+}
+__device__ void readChildren(const float4* nodes2, uint32_t b, Child4& c0, Child4& c1) {
+    const float4* nd = nodes2 + 4 * (size_t)b;
+    float4 n0 = nd[0], n1 = nd[1], n2 = nd[2], n3 = nd[3];
+    c0.lo[0] = n0.x; c0.hi[0] = n0.y; c0.lo[1] = n0.z; c0.hi[1] = n0.w; c0.lo[2] = n2.x; c0.hi[2] = n2.y;
+    c1.lo[0] = n1.x; c1.hi[0] = n1.y; c1.lo[1] = n1.z; c1.hi[1] = n1.w; c1.lo[2] = n2.z; c1.hi[2] = n2.w;
+    c0.ref = __float_as_uint(n3.x);
+    c1.ref = __float_as_uint(n3.y);
+}
+__global__ void k_collapse4(const float4* nodes2, const int2* frontier, const int* nFront, float4* nodes4, int* nodeCounter, int2* next,
+                            int* nNext) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= *nFront) return;
+    int2 item = frontier[i];
+    Child4 c[4];
+    int cnt = 2;
+    readChildren(nodes2, (uint32_t)item.x, c[0], c[1]);
+    while (cnt < 4) {
+        int best = -1;
+        float bestA = -1.0f;
+        for (int k = 0; k < cnt; ++k)
+            if (!(c[k].ref & kLeafFlag)) {
+                float a = halfArea(c[k]);
+                if (a > bestA) { bestA = a; best = k; }
+            }
+        if (best < 0) break;
+        Child4 a, b;
+        readChildren(nodes2, c[best].ref, a, b);
+        c[best] = a;
+        c[cnt++] = b;
+    }
+    float4* out = nodes4 + 8 * (size_t)item.y;
+    float v[6][4];
+    uint32_t refs[4];
+    for (int k = 0; k < 4; ++k) {
+        if (k < cnt) {
+            for (int a = 0; a < 3; ++a) { v[2 * a][k] = c[k].lo[a]; v[2 * a + 1][k] = c[k].hi[a]; }
+            uint32_t r = c[k].ref;
+            if (!(r & kLeafFlag)) {
+                int slot = atomicAdd(nodeCounter, 1);
+                next[atomicAdd(nNext, 1)] = make_int2((int)r, slot);
+                r = (uint32_t)slot;
+            }
+            refs[k] = r;
+        } else {
+            for (int a = 0; a < 6; ++a) v[a][k] = 0.0f;
+            refs[k] = 0u;
+        }
+    }
+    for (int a = 0; a < 6; ++a) out[a] = make_float4(v[a][0], v[a][1], v[a][2], v[a][3]);
+    out[6] = make_float4(__uint_as_float(refs[0]), __uint_as_float(refs[1]), __uint_as_float(refs[2]), __uint_as_float(refs[3]));
+    out[7] = make_float4(__int_as_float(cnt), 0.0f, 0.0f, 0.0f);
+}
+__global__ void k_collapse_root(int2* frontier, int* nFront, int* nodeCounter) {
+    frontier[0] = make_int2(0, 0);
+    *nFront = 1;
+    *nodeCounter = 1;
+}
+}  // namespace
+
+size_t bvh4ScratchBytes(int nNodes2) { return 2 * sizeof(int2) * (size_t)std::max(1, nNodes2) + 1024; }
+
+int buildBvh4(const float4* nodes2, int nNodes2, float4* nodes4, void* scratch, int* hostNodeCount, int* hostDepth, cudaStream_t st) {
+    *hostNodeCount = 0;
+    *hostDepth = 0;
+    if (nNodes2 <= 0) return 0;
+    char* p = static_cast<char*>(scratch);
+    int* counters = reinterpret_cast<int*>(p);  // [0] node counter, [1], [2] frontier sizes
+    int2* fr[2] = {reinterpret_cast<int2*>(p + 256), reinterpret_cast<int2*>(p + 256) + nNodes2};
+    k_collapse_root<<<1, 1, 0, st>>>(fr[0], counters + 1, counters);
+    int cur = 0, depth = 0, n = 1;
+    int hostCnt = 0;
+    while (n > 0) {
+        if (++depth > 4 * kMaxBvhDepth) return -2;
+        if (cudaMemsetAsync(counters + 2 - cur, 0, sizeof(int), st) != cudaSuccess) return -1;
+        k_collapse4<<<(n + 127) / 128, 128, 0, st>>>(nodes2, fr[cur], counters + 1 + cur, nodes4, counters, fr[1 - cur], counters + 2 - cur);
+        if (cudaMemcpyAsync(&n, counters + 2 - cur, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess) return -1;
+        if (cudaStreamSynchronize(st) != cudaSuccess) return -1;
+        cur = 1 - cur;
+    }
+    if (cudaMemcpyAsync(&hostCnt, counters, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess) return -1;
+    if (cudaStreamSynchronize(st) != cudaSuccess) return -1;
+    *hostNodeCount = hostCnt;
+    *hostDepth = depth;
+    return 0;
 }
 }  // namespace sst

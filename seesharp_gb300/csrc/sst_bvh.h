@@ -16,6 +16,12 @@ size_t lbvhScratchBytes(int n);
 int buildLbvh(const float4* tri, int n, float4* nodesOut, int* orderOut, void* scratch, size_t scratchBytes, int* hostNodeCount, int* hostMaxDepth,
               cudaStream_t st);
 
+// 4-wide BVH collapsed from the binary one (nNodes2 binary inner nodes in the layout above):
+// at most nNodes2 nodes of 8 float4 each are written to nodes4.  Returns 0 on success with the
+// node count and the number of levels through the host pointers.
+size_t bvh4ScratchBytes(int nNodes2);
+int buildBvh4(const float4* nodes2, int nNodes2, float4* nodes4, void* scratch, int* hostNodeCount, int* hostDepth, cudaStream_t st);
+
 // Gathers per-triangle records into leaf order: out[t] = in[order[t]] (triv also stamps the
 // global id into v0.w).
 void launch_leaf_gather(const int* order, int n, const float4* trivG, const float4* triNG, const int4* auxG, const int4* vtxG, float4* triv,

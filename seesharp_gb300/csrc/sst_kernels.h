@@ -12,11 +12,13 @@ void launch_camera(const DevJob* jobs, const WaveChunk* chunks, const WaveDesc* 
 void launch_film_fold(const DevJob* jobs, const WaveChunk* chunks, const WaveDesc* waves, int* curWave, const float* samples, DevStats* st,
                       int maxFold, int advance, cudaStream_t s);
 // Traversal launch configuration (sst_trace.cu): threads per block (64, 128 or 256), stack
-// entries per thread kept in shared memory (16, 24 or 32), resident blocks per SM (0: as many as fit).
+// entries per thread kept in shared memory (16, 24 or 32), resident blocks per SM (0: as many as
+// fit), BVH width (2 or 4; a scene without a 4-wide BVH is traversed binary).
 struct TraceTuning {
     int block = kTraceBlock;
     int smemStack = kSmemStack;
     int blocksPerSM = 0;
+    int width = 2;  // BVH width: 2 (binary) or 4
 };
 bool traceTuningValid(const TraceTuning& t);
 int traceGrid(const TraceTuning& t);

@@ -143,9 +143,106 @@ SST_D TraceResult traverse(const Bvh sc, float3 org, float3 dir, float tmin, flo
     return r;
 }
 
+// 4-wide traversal over the same leaves.  Per node: the four slab tests, the hit children
+// ordered by entry distance (a 5-comparator network), the nearest one visited next and the others
+// pushed farthest first.  SSTACK entries per thread in shared memory, the rest in local memory
+// (kMaxStack4 bounds three pending children per level).
+struct Bvh4 {
+    const float4* nodes4;
+    const float4* triv;
+    int nNodes4;
+};
+SST_D Bvh4 bvh4Of(const DevScene& sc) { return Bvh4{sc.nodes4, sc.triv, sc.nNodes4}; }
+
+SST_D void cswap(float& ka, uint32_t& ra, float& kb, uint32_t& rb) {
+    bool s = kb < ka;
+    float k = s ? kb : ka;
+    kb = s ? ka : kb;
+    ka = k;
+    uint32_t r = s ? rb : ra;
+    rb = s ? ra : rb;
+    ra = r;
+}
+
+template <bool ANY, int BLOCK, int SSTACK>
+SST_D TraceResult traverse4(const Bvh4 sc, float3 org, float3 dir, float tmin, float tmax, int* sstack, int* errFlags) {
+    TraceResult r{tmax, 0.f, 0.f, -1};
+    if (sc.nNodes4 == 0 || !(tmax > tmin)) return r;
+    int bestGid = 0x7FFFFFFF;
+    RayPre pre = rayPre(dir);
+    float3 inv = mk(1.0f / dir.x, 1.0f / dir.y, 1.0f / dir.z);
+    float3 oi = mk(-org.x * inv.x, -org.y * inv.y, -org.z * inv.z);
+    int lstack[kMaxStack4 - SSTACK];
+    int sp = 0;
+    uint32_t ref = 0;  // root
+    const int tid = threadIdx.x;
+    for (;;) {
+        if (!(ref & kLeafFlag)) {
+            const float4* nd = sc.nodes4 + 8 * (size_t)ref;
+            float4 lx = __ldg(nd), hx = __ldg(nd + 1), ly = __ldg(nd + 2), hy = __ldg(nd + 3), lz = __ldg(nd + 4), hz = __ldg(nd + 5);
+            float4 rf = __ldg(nd + 6), meta = __ldg(nd + 7);
+            const int cnt = __float_as_int(meta.x);
+            const float hitT = r.t * 1.0000004f;
+            float key[4];
+            uint32_t cr[4];
+            const float* LX = &lx.x; const float* HX = &hx.x; const float* LY = &ly.x; const float* HY = &hy.x;
+            const float* LZ = &lz.x; const float* HZ = &hz.x; const float* RF = &rf.x;
+            int nh = 0;
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+                float a = fmaf(LX[k], inv.x, oi.x), b = fmaf(HX[k], inv.x, oi.x);
+                float c = fmaf(LY[k], inv.y, oi.y), d = fmaf(HY[k], inv.y, oi.y);
+                float e = fmaf(LZ[k], inv.z, oi.z), f = fmaf(HZ[k], inv.z, oi.z);
+                float tn = fmaxf(fmaxf(fminf(a, b), fminf(c, d)), fmaxf(fminf(e, f), tmin));
+                float tf = fminf(fminf(fmaxf(a, b), fmaxf(c, d)), fminf(fmaxf(e, f), hitT));
+                bool hit = k < cnt && tn <= tf * 1.0000004f;
+                key[k] = hit ? tn : CUDART_INF_F;
+                cr[k] = __float_as_uint(RF[k]);
+                nh += hit ? 1 : 0;
+            }
+            if (nh > 0) {
+                // ascending by entry distance; children that were not hit sort last (key = inf)
+                cswap(key[0], cr[0], key[1], cr[1]);
+                cswap(key[2], cr[2], key[3], cr[3]);
+                cswap(key[0], cr[0], key[2], cr[2]);
+                cswap(key[1], cr[1], key[3], cr[3]);
+                cswap(key[1], cr[1], key[2], cr[2]);
+                // push the farther hit children, farthest first
+                for (int k = nh - 1; k >= 1; --k) {
+                    uint32_t pr = k == 3 ? cr[3] : (k == 2 ? cr[2] : cr[1]);
+                    if (sp < SSTACK) sstack[sp * BLOCK + tid] = (int)pr;
+                    else if (sp < kMaxStack4) lstack[sp - SSTACK] = (int)pr;
+                    else { atomicOr(errFlags, 1); return r; }
+                    ++sp;
+                }
+                ref = cr[0];
+                continue;
+            }
+        } else {
+            int first = (int)(ref & kLeafFirstMask);
+            int cnt = (int)((ref >> kLeafCountShift) & 0xF) + 1;
+            for (int k = 0; k < cnt; ++k) {
+                int ti = first + k;
+                float4 a = __ldg(&sc.triv[3 * (size_t)ti]), b = __ldg(&sc.triv[3 * (size_t)ti + 1]), c = __ldg(&sc.triv[3 * (size_t)ti + 2]);
+                float t, u, v;
+                float lim = ANY ? r.t : __uint_as_float(__float_as_uint(r.t) + (r.t < CUDART_INF_F ? 1u : 0u));
+                if (isectTri(org, pre, f3(a), f3(b), f3(c), tmin, lim, t, u, v)) {
+                    int gid = __float_as_int(a.w);
+                    if (ANY) { r.t = t; r.u = u; r.v = v; r.tri = ti; return r; }
+                    if (t < r.t || (t == r.t && gid < bestGid)) { r.t = t; r.u = u; r.v = v; r.tri = ti; bestGid = gid; }
+                }
+            }
+        }
+        if (sp == 0) break;
+        --sp;
+        ref = (uint32_t)(sp < SSTACK ? sstack[sp * BLOCK + tid] : lstack[sp - SSTACK]);
+    }
+    return r;
+}
+
 // mode 0: closest hit -> hits[i]; mode 1: shadow rays, zero nee[tgt[i]] when occluded;
 // mode 2: any hit -> occl[i] = 1/0.
-template <int MODE, int BLOCK, int SSTACK>
+template <int MODE, int BLOCK, int SSTACK, bool WIDE>
 __global__ void __launch_bounds__(BLOCK) k_trace(const DevJob* __restrict__ jobs, const uint32_t* __restrict__ rayJob, const float4* ro,
                                                  const float4* rd, const int* count, int* work, float4* hits, const int* tgt, float4* nee,
                                                  int* occl, DevStats* stats, int countRays) {
@@ -164,7 +261,10 @@ __global__ void __launch_bounds__(BLOCK) k_trace(const DevJob* __restrict__ jobs
         if (i < n) {
             float4 o = ro[i], d = rd[i];
             uint32_t jb = rayJob ? rayJob[i] : 0u;
-            TraceResult h = traverse<MODE != 0, BLOCK, SSTACK>(bvhOf(jobs[jb].sc), f3(o), f3(d), o.w, d.w, sstack, &stats->errorFlags);
+            const DevScene& sc = jobs[jb].sc;
+            TraceResult h = (WIDE && sc.nNodes4 > 0)
+                                ? traverse4<MODE != 0, BLOCK, SSTACK>(bvh4Of(sc), f3(o), f3(d), o.w, d.w, sstack, &stats->errorFlags)
+                                : traverse<MODE != 0, BLOCK, SSTACK>(bvhOf(sc), f3(o), f3(d), o.w, d.w, sstack, &stats->errorFlags);
             if (MODE == 0) {
                 hits[i] = make_float4(h.t, h.u, h.v, __int_as_float(h.tri));
             } else if (MODE == 1) {
@@ -177,34 +277,18 @@ __global__ void __launch_bounds__(BLOCK) k_trace(const DevJob* __restrict__ jobs
 }
 
 // ---------------------------------------------------------------------------------------------
-// Variant table: block size x shared stack entries, for each of the three modes.
+// Variant table: BVH width x block size x shared stack entries, for each of the three modes.
 // ---------------------------------------------------------------------------------------------
 using TraceKernel = void (*)(const DevJob*, const uint32_t*, const float4*, const float4*, const int*, int*, float4*, const int*, float4*, int*,
                              DevStats*, int);
 
-template <int BLOCK, int SSTACK>
+template <int BLOCK, int SSTACK, bool WIDE>
 struct TraceVariant {
-    static constexpr TraceKernel k[3] = {k_trace<0, BLOCK, SSTACK>, k_trace<1, BLOCK, SSTACK>, k_trace<2, BLOCK, SSTACK>};
+    static constexpr TraceKernel k[3] = {k_trace<0, BLOCK, SSTACK, WIDE>, k_trace<1, BLOCK, SSTACK, WIDE>, k_trace<2, BLOCK, SSTACK, WIDE>};
 };
 
 static const int kBlocks[3] = {64, 128, 256};
 static const int kStacks[3] = {16, 24, 32};
-
-static TraceKernel traceKernel(int mode, int bi, int si) {
-#define SST_TV(B, S) TraceVariant<B, S>::k[mode]
-    switch (bi * 3 + si) {
-        case 0: return SST_TV(64, 16);
-        case 1: return SST_TV(64, 24);
-        case 2: return SST_TV(64, 32);
-        case 3: return SST_TV(128, 16);
-        case 4: return SST_TV(128, 24);
-        case 5: return SST_TV(128, 32);
-        case 6: return SST_TV(256, 16);
-        case 7: return SST_TV(256, 24);
-        default: return SST_TV(256, 32);
-    }
-#undef SST_TV
-}
 
 static int indexOf(const int* a, int v) {
     for (int k = 0; k < 3; ++k)
@@ -212,22 +296,54 @@ static int indexOf(const int* a, int v) {
     return -1;
 }
 
-bool traceTuningValid(const TraceTuning& t) { return indexOf(kBlocks, t.block) >= 0 && indexOf(kStacks, t.smemStack) >= 0 && t.blocksPerSM >= 0; }
+// Variant index: (width 2 or 4) x block x stack, 18 in all.
+static int variantOf(const TraceTuning& t) {
+    int bi = indexOf(kBlocks, t.block), si = indexOf(kStacks, t.smemStack);
+    if (bi < 0 || si < 0 || (t.width != 2 && t.width != 4)) return -1;
+    return (t.width == 4 ? 9 : 0) + bi * 3 + si;
+}
+
+static TraceKernel traceKernel(int mode, int variant) {
+#define SST_TV(B, S, W) TraceVariant<B, S, W>::k[mode]
+    switch (variant) {
+        case 0: return SST_TV(64, 16, false);
+        case 1: return SST_TV(64, 24, false);
+        case 2: return SST_TV(64, 32, false);
+        case 3: return SST_TV(128, 16, false);
+        case 4: return SST_TV(128, 24, false);
+        case 5: return SST_TV(128, 32, false);
+        case 6: return SST_TV(256, 16, false);
+        case 7: return SST_TV(256, 24, false);
+        case 8: return SST_TV(256, 32, false);
+        case 9: return SST_TV(64, 16, true);
+        case 10: return SST_TV(64, 24, true);
+        case 11: return SST_TV(64, 32, true);
+        case 12: return SST_TV(128, 16, true);
+        case 13: return SST_TV(128, 24, true);
+        case 14: return SST_TV(128, 32, true);
+        case 15: return SST_TV(256, 16, true);
+        case 16: return SST_TV(256, 24, true);
+        default: return SST_TV(256, 32, true);
+    }
+#undef SST_TV
+}
+
+bool traceTuningValid(const TraceTuning& t) { return variantOf(t) >= 0 && t.blocksPerSM >= 0; }
 
 // Resident blocks per SM of a variant (occupancy), computed once per variant for the device that
 // first asks (the devices of one machine are identical).
-static int maxBlocksPerSM(int bi, int si) {
-    static int cache[9] = {};
-    int& c = cache[bi * 3 + si];
+static int maxBlocksPerSM(int variant) {
+    static int cache[18] = {};
+    int& c = cache[variant];
     if (c == 0) {
         int bps = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, traceKernel(0, bi, si), kBlocks[bi], 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, traceKernel(0, variant), kBlocks[(variant % 9) / 3], 0);
         c = bps > 0 ? bps : 1;
     }
     return c;
 }
 
-int traceGrid(const TraceTuning& t) {
+static int numSMs() {
     static int sms = 0;
     if (sms == 0) {
         int dev = 0;
@@ -235,20 +351,27 @@ int traceGrid(const TraceTuning& t) {
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         if (sms <= 0) sms = 1;
     }
-    int bi = indexOf(kBlocks, t.block), si = indexOf(kStacks, t.smemStack);
-    int m = maxBlocksPerSM(bi, si);
-    int b = t.blocksPerSM > 0 ? std::min(t.blocksPerSM, m) : m;
-    return sms * b;
+    return sms;
 }
 
-int traceMaxBlocksPerSM(const TraceTuning& t) { return maxBlocksPerSM(indexOf(kBlocks, t.block), indexOf(kStacks, t.smemStack)); }
+int traceGrid(const TraceTuning& t) {
+    int v = variantOf(t);
+    if (v < 0) v = 4;
+    int m = maxBlocksPerSM(v);
+    int b = t.blocksPerSM > 0 ? std::min(t.blocksPerSM, m) : m;
+    return numSMs() * b;
+}
+
+int traceMaxBlocksPerSM(const TraceTuning& t) {
+    int v = variantOf(t);
+    return maxBlocksPerSM(v < 0 ? 4 : v);
+}
 
 static void launch(const TraceTuning& t, int mode, const DevJob* jobs, const uint32_t* rayJob, const float4* ro, const float4* rd, const int* count,
                    int* work, float4* hits, const int* tgt, float4* nee, int* occl, DevStats* stats, int countRays, cudaStream_t s) {
-    int bi = indexOf(kBlocks, t.block), si = indexOf(kStacks, t.smemStack);
-    if (bi < 0 || si < 0) { bi = 1; si = 1; }
-    traceKernel(mode, bi, si)<<<traceGrid(TraceTuning{kBlocks[bi], kStacks[si], t.blocksPerSM}), kBlocks[bi], 0, s>>>(
-        jobs, rayJob, ro, rd, count, work, hits, tgt, nee, occl, stats, countRays);
+    int v = variantOf(t);
+    if (v < 0) v = 4;  // 128 threads, 24 shared entries, binary
+    traceKernel(mode, v)<<<traceGrid(t), kBlocks[(v % 9) / 3], 0, s>>>(jobs, rayJob, ro, rd, count, work, hits, tgt, nee, occl, stats, countRays);
 }
 
 void launch_trace_closest(const TraceTuning& t, const DevJob* jobs, const uint32_t* rayJob, const float4* ro, const float4* rd, const int* count,

@@ -9,6 +9,7 @@ constexpr int kMaxShadowRays = 4;     // NumShadowRays supported per vertex
 constexpr int kTraceBlock = 128;      // threads per block of the traversal kernels
 constexpr int kSmemStack = 24;        // traversal stack entries kept in shared memory per thread
 constexpr int kMaxStack = 64;         // total stack entries (the BVH builder caps the depth below this)
+constexpr int kMaxStack4 = 192;       // 4-wide traversal: at most 3 pending children per level of at most 60 levels
 constexpr int kMaxBvhDepth = 60;
 constexpr int kMaxLeafSize = 8;
 
@@ -61,7 +62,8 @@ struct DevCamera {
 };
 
 struct DevScene {
-    const float4* nodes;   // 4 float4 per node
+    const float4* nodes;   // binary BVH: 4 float4 per node
+    const float4* nodes4;  // 4-wide BVH over the same leaves: 8 float4 per node
     const float4* triv;    // 3 float4 per leaf-ordered triangle: v1 (w = global tri id), v2, v3
     const float4* triN;    // per leaf-ordered triangle: face normal, w = emitter index (int bits, -1)
     const int4* triAux;    // (material, mesh, local face, attribute flags: 1 normals, 2 uvs)
@@ -75,6 +77,7 @@ struct DevScene {
     int nEmitters;
     int nTri;
     int nNodes;
+    int nNodes4;
     int hasEnv;
     DevEnv env;
     DevCamera cam;

@@ -221,6 +221,90 @@ def sphere_field(num_spheres=200, width=1024, height=1024, seed=11, level=4, num
     return sc
 
 
+def _terrain(n, x0, z0, size, seed):
+    """Heightfield of n x n quads over [x0, x0 + size] x [z0, z0 + size]: vertices (n+1)^2, UVs
+    spanning [0, 1]^2, heights a seeded sum of sines around y = -1.5."""
+    rng = np.random.default_rng(seed)
+    g = np.linspace(0.0, 1.0, n + 1)
+    U, Vv = np.meshgrid(g, g, indexing="xy")
+    h = np.zeros_like(U)
+    for _ in range(6):
+        f = rng.uniform(2, 12, size=2)
+        a = rng.uniform(0.1, 0.6)
+        h += a * np.sin(2 * math.pi * (f[0] * U + rng.uniform())) * np.cos(2 * math.pi * (f[1] * Vv + rng.uniform()))
+    V = np.stack([x0 + size * U, -1.5 + h, z0 + size * Vv], -1).reshape(-1, 3).astype(np.float32)
+    uv = np.stack([U, 1.0 - Vv], -1).reshape(-1, 2).astype(np.float32)
+    i = np.arange(n)
+    a = (i[None, :] + (n + 1) * i[:, None]).reshape(-1)
+    b, c, d = a + 1, a + n + 2, a + n + 1
+    I = np.stack([a, c, b, a, d, c], -1).reshape(-1).astype(np.int32)  # faces point up (+y)
+    return V, I, uv
+
+
+def large_combined(width=1920, height=1080, seed=21, num_spheres=2000, terrain_quads=1024, tex_res=1024, num_lights=1000, views=8, level=4):
+    """The large combined workload: num_spheres seeded displaced icospheres (5120 triangles each
+    at subdivision 4) with one GenericMaterial each (its roughness is a parameter), a heightfield
+    terrain of terrain_quads^2 quads whose GenericMaterial base colour is a tex_res^2 RGB texture
+    (a parameter), num_lights emissive triangles, a procedural sky and `views` camera views
+    around the field.  2000 spheres + 1024^2 quads give 12.3M triangles.
+    Returns (scene, terrain texture, sphere materials, [(worldToCamera, fov)] views)."""
+    rng = np.random.default_rng(seed)
+    base_v, base_i = icosphere(level)
+    nv = base_v.shape[0]
+    sc = Scene()
+    extent = 100.0
+    tv, ti, tuv = _terrain(terrain_quads, -10.0, -10.0, extent, seed + 1)
+    yy, xx = np.meshgrid(np.linspace(0, 1, tex_res), np.linspace(0, 1, tex_res), indexing="ij")
+    tex_img = np.stack([0.3 + 0.2 * np.sin(23 * xx) * np.cos(17 * yy), 0.45 + 0.2 * np.cos(31 * yy + 1.0), 0.25 + 0.15 * np.sin(13 * (xx + yy))], -1)
+    tex_img = np.clip(tex_img + 0.05 * rng.standard_normal(tex_img.shape), 0.02, 0.98).astype(np.float32)
+    tex = TextureRgb(RgbImage(tex_img))
+    terrain = Mesh(tv, ti, textureCoordinates=tuv)
+    terrain.Material = GenericMaterial(GenericMaterial.Parameters(BaseColor=tex, Roughness=TextureMono(0.7), SpecularTintStrength=0.0))
+    sc.Meshes.append(terrain)
+    freq = rng.uniform(2, 6, size=(num_spheres, 3, 3))
+    phase = rng.uniform(0, 2 * math.pi, size=(num_spheres, 3))
+    mats = []
+    for k in range(num_spheres):
+        center = np.array([rng.uniform(0, 80), rng.uniform(0.0, 6.0), rng.uniform(0, 80)])
+        radius = rng.uniform(0.5, 1.3)
+        disp = np.zeros(nv)
+        for j in range(3):
+            disp += 0.04 * np.sin(base_v @ freq[k, j] + phase[k, j])
+        V = base_v * (radius * (1.0 + disp))[:, None] + center
+        N = _vertex_normals(V, base_i)
+        m = Mesh(V.astype(np.float32), base_i, shadingNormals=N.astype(np.float32))
+        mat = GenericMaterial(GenericMaterial.Parameters(BaseColor=TextureRgb(RgbColor(*rng.uniform(0.05, 0.95, size=3))),
+                                                         Roughness=TextureMono(rng.uniform(0.1, 0.9)), Metallic=float(rng.random() < 0.3)))
+        m.Material = mat
+        mats.append(mat)
+        sc.Meshes.append(m)
+    lv = []
+    for k in range(num_lights):
+        c = np.array([rng.uniform(-5, 85), rng.uniform(25, 30), rng.uniform(-5, 85)])
+        sz = rng.uniform(0.5, 1.2)
+        a = rng.uniform(0, 2 * math.pi)
+        p0 = c + sz * np.array([math.cos(a), 0, math.sin(a)])
+        p1 = c + sz * np.array([math.cos(a + 2.1), 0, math.sin(a + 2.1)])
+        p2 = c + sz * np.array([math.cos(a + 4.2), 0, math.sin(a + 4.2)])
+        if np.cross(p1 - p0, p2 - p0)[1] > 0:
+            p1, p2 = p2, p1
+        lv += [p0, p1, p2]
+    lights = Mesh(np.array(lv, np.float32), np.arange(3 * num_lights, dtype=np.int32))
+    lights.Material = DiffuseMaterial(DiffuseMaterial.Parameters(BaseColor=TextureRgb(RgbColor.Black)))
+    sc.Meshes.append(lights)
+    for k in range(num_lights):
+        sc.Emitters.append(DiffuseEmitter(Triangle(lights, k), RgbColor(*rng.uniform(5, 40, size=3))))
+    sc.Background = EnvironmentMap(RgbImage(procedural_sky(seed=seed + 2)))
+    cams = []
+    for v in range(views):
+        a = 2 * math.pi * v / views + 0.3
+        eye = [40 + 55 * math.cos(a), rng.uniform(12, 22), 40 + 55 * math.sin(a)]
+        cams.append((Matrix4x4.CreateLookAt(eye, [40, 0, 40], [0, 1, 0]), 50.0))
+    sc.Camera = PerspectiveCamera(cams[0][0], cams[0][1])
+    sc.FrameBuffer = FrameBuffer(width, height)
+    return sc, tex, mats, cams
+
+
 def sphere_field_for_triangles(num_triangles, **kw):
     return sphere_field(num_spheres=max(1, int(round(num_triangles / 5120))), **kw)
 

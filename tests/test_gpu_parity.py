@@ -219,8 +219,18 @@ def triangle_soup(rng, n):
     return sc
 
 
+@pytest.fixture(params=[2, 4], ids=["bvh2", "bvh4"])
+def bvh_width(request):
+    """Runs a test under each traversal width (the other launch settings at their defaults)."""
+    ctx = _native.default_context()
+    base = _native.get_tuning(ctx)
+    _native.set_tuning(ctx, traceBvhWidth=request.param)
+    yield request.param
+    _native.set_tuning(ctx, **base)
+
+
 @pytest.mark.parametrize("seed,ntri", [(1, 300), (2, 3000)])
-def test_intersection_against_fp64(seed, ntri):
+def test_intersection_against_fp64(seed, ntri, bvh_width):
     """Closest hit: primitive id exact and t to a relative 1e-5 on non-degenerate rays, against an
     FP64 brute-force watertight intersector."""
     rng = np.random.default_rng(seed)
@@ -259,7 +269,7 @@ def test_intersection_against_fp64(seed, ntri):
     assert checked > n // 4
 
 
-def test_occlusion_queries():
+def test_occlusion_queries(bvh_width):
     rng = np.random.default_rng(9)
     sc = triangle_soup(rng, 500)
     sc.Prepare()
@@ -358,7 +368,7 @@ def test_relmse_ratio_sphere_field_1m_triangles():
     assert er > 0 and 1 / 1.05 <= ratio <= 1.05, ratio
 
 
-def test_sphere_field_paths_match():
+def test_sphere_field_paths_match(bvh_width):
     sc = workloads.sphere_field(12, 80, 80, level=3)
     sc.Prepare()
     g, st = render_gpu(sc, 1, 8)
@@ -501,9 +511,10 @@ def test_tuning_and_autotune_leave_images_and_queries_unchanged():
         ref, st0 = render_gpu(sc, 4, 6)
         hits0, occ0 = sc.native.trace(rays), sc.native.occluded(rays)
         assert st0.numKernelLaunches > 0
-        for t in [dict(traceBlock=64, traceStackShared=16, traceBlocksPerSM=1, waveCapacity=4096),
-                  dict(traceBlock=256, traceStackShared=32, traceBlocksPerSM=0, waveCapacity=0),
-                  dict(traceBlock=128, traceStackShared=24, traceBlocksPerSM=2, waveCapacity=1 << 20)]:
+        for t in [dict(traceBlock=64, traceStackShared=16, traceBlocksPerSM=1, waveCapacity=4096, traceBvhWidth=2),
+                  dict(traceBlock=256, traceStackShared=32, traceBlocksPerSM=0, waveCapacity=0, traceBvhWidth=4),
+                  dict(traceBlock=64, traceStackShared=16, traceBlocksPerSM=3, waveCapacity=8192, traceBvhWidth=4),
+                  dict(traceBlock=128, traceStackShared=24, traceBlocksPerSM=2, waveCapacity=1 << 20, traceBvhWidth=2)]:
             _native.set_tuning(ctx, **t)
             assert _native.get_tuning(ctx) == t
             img, _ = render_gpu(sc, 4, 6)
@@ -517,9 +528,31 @@ def test_tuning_and_autotune_leave_images_and_queries_unchanged():
         assert chosen == _native.get_tuning(ctx) and ms > 0
         img, _ = render_gpu(sc, 4, 6)
         assert np.array_equal(img, ref)
-        for bad in (dict(traceBlock=96), dict(traceStackShared=20), dict(waveCapacity=100), dict(traceBlocksPerSM=-1)):
+        for bad in (dict(traceBlock=96), dict(traceStackShared=20), dict(waveCapacity=100), dict(traceBlocksPerSM=-1), dict(traceBvhWidth=8)):
             with pytest.raises(_native.SstError):
                 _native.set_tuning(ctx, **bad)
             assert _native.get_tuning(ctx) == chosen
     finally:
         _native.set_tuning(ctx, **base)
+
+
+def test_camera_views_in_a_batch_equal_scenes_with_those_cameras():
+    """SstRenderJob.camera: views of one scene in one batch render exactly like scenes that carry
+    those cameras."""
+    views = [(Matrix4x4.CreateLookAt([10, 9, -16], [10, 8, 10], [0, 1, 0]), 45.0),
+             (Matrix4x4.CreateLookAt([-6, 5, 4], [10, 2, 10], [0, 1, 0]), 60.0)]
+    scenes = []
+    for m, f in views:
+        sc = workloads.sphere_field(12, 64, 48, level=3)
+        sc.Camera = PerspectiveCamera(m, f)
+        sc.Prepare()
+        scenes.append(sc)
+    singles = [render_gpu(sc, 3, 5)[0] for sc in scenes]
+    base = scenes[0]
+    films = [np.zeros((48, 64, 3), np.float32) for _ in views]
+    base.FrameBuffer.Reset()
+    p = PathTracer(TotalSpp=3, MaxDepth=5).params(base)
+    jobs = [(base.native, p, f.ctypes.data, _native.SST_MEM_HOST, _native.make_camera(m, fov)) for f, (m, fov) in zip(films, views)]
+    _native.render_batch(base.native.ctx, jobs)
+    for f, s1 in zip(films, singles):
+        assert np.array_equal(f, s1)
