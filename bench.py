@@ -85,9 +85,13 @@ def run_batch(args, cfg):
         sequential()
     with ClockSampler(0) as clk:
         nlaunch[0] = 0
+        w0 = time.perf_counter()
         tb = [batched() for _ in range(args.steps)]
+        wall_b = (time.perf_counter() - w0) / args.steps
         batched_launches = nlaunch[0]
+        w0 = time.perf_counter()
         ts = [sequential() for _ in range(args.steps)]
+        wall_s = (time.perf_counter() - w0) / args.steps
     vb = samples / (np.mean(tb) / 1000) / 1e6
     vs = samples / (np.mean(ts) / 1000) / 1e6
     # e2e: wall clock through the public API with host films
@@ -101,6 +105,8 @@ def run_batch(args, cfg):
                        "triangles_total": int(sum(tris))},
             "sequential": {"value": round(vs, 3), "ms_per_step": round(float(np.mean(ts)), 3)},
             "batched_over_sequential": round(vb / vs, 3),
+            "wall_clock": {"batched_s": round(wall_b, 3), "sequential_s": round(wall_s, 3), "batched_over_sequential": round(wall_s / wall_b, 3),
+                           "note": "host time per step through the public API, films read back to the host"},
             "gpu_launches": int(batched_launches),
             "e2e": {"value": round(e2e_b, 3), "unit": "Msamples/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": int(sum(sc.FrameBuffer.Image.data.nbytes for sc, _ in pairs))},

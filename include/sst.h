@@ -172,10 +172,10 @@ int sst_occluded(sst_scene* scene, const SstRay* rays, int32_t n, int32_t* occlu
  * a result: films and query results are bitwise the same under every valid setting. */
 typedef struct SstTuning {
     int32_t waveCapacity;     /* paths in flight per wave; 0 = the default (2^21) */
-    int32_t traceBlock;       /* threads per traversal block: 64, 128 or 256 */
-    int32_t traceStackShared; /* traversal stack entries per thread kept in shared memory: 16, 24 or 32 */
+    int32_t traceBlock;       /* threads per traversal block: 64, 128 (the default) or 256 */
+    int32_t traceStackShared; /* traversal stack entries per thread kept in shared memory: 16, 24 (the default) or 32 */
     int32_t traceBlocksPerSM; /* resident traversal blocks per SM; 0 = as many as fit */
-    int32_t traceBvhWidth;    /* BVH traversed: 2 (binary) or 4 (4-wide, same leaves) */
+    int32_t traceBvhWidth;    /* BVH traversed: 2 (binary) or 4 (4-wide, same leaves; the default) */
 } SstTuning;
 int sst_get_tuning(sst_ctx* ctx, SstTuning* out);
 /* Invalid values return SST_ERR_INVALID_ARGUMENT and leave the setting unchanged. */

@@ -14,9 +14,15 @@
 
 namespace cg = cooperative_groups;
 
-// Minimum resident blocks per SM requested for the shade kernel (register budget).
+// Minimum resident 128-thread blocks per SM the shade kernel is compiled for (its register
+// budget).  The kernel is latency-bound: on GB300, 8 blocks (64 registers, some spilled to L1)
+// shade 18% faster than the unconstrained 131-register build on the 1M-triangle scene and are
+// the fastest cap on the Cornell box; the adjoint variant is fastest at 16 blocks (32 registers).
 #ifndef SST_SHADE_MIN_BLOCKS
-#define SST_SHADE_MIN_BLOCKS 1
+#define SST_SHADE_MIN_BLOCKS 8
+#endif
+#ifndef SST_SHADE_ADJ_MIN_BLOCKS
+#define SST_SHADE_ADJ_MIN_BLOCKS 16
 #endif
 
 namespace sst {
@@ -202,7 +208,7 @@ SST_D int aggAppend(int* counter) {
 //     (applied at the next vertex, after that vertex has resolved vertex k's NEE).
 // Every term is weighted by dLoss/dSample of the path's pixel.
 template <int NS, bool ADJ>
-__global__ void __launch_bounds__(128, SST_SHADE_MIN_BLOCKS) k_shade(const DevJob* __restrict__ jobs, PathBuf A, PathBuf B,
+__global__ void __launch_bounds__(128, ADJ ? SST_SHADE_ADJ_MIN_BLOCKS : SST_SHADE_MIN_BLOCKS) k_shade(const DevJob* __restrict__ jobs, PathBuf A, PathBuf B,
                                                                    const float4* __restrict__ hits, float4* nee, float4* neeG, int cap,
                                                                    float4* shRo, float4* shRd, int* shTgt, uint32_t* shJob, const int* nIn,
                                                                    int* nOut, int* nSh, float* samples, DevStats* stats) {

@@ -18,7 +18,7 @@ struct TraceTuning {
     int block = kTraceBlock;
     int smemStack = kSmemStack;
     int blocksPerSM = 0;
-    int width = 2;  // BVH width: 2 (binary) or 4
+    int width = 4;  // BVH width: 2 (binary) or 4
 };
 bool traceTuningValid(const TraceTuning& t);
 int traceGrid(const TraceTuning& t);

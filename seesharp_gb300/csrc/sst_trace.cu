@@ -242,8 +242,12 @@ SST_D TraceResult traverse4(const Bvh4 sc, float3 org, float3 dir, float tmin, f
 
 // mode 0: closest hit -> hits[i]; mode 1: shadow rays, zero nee[tgt[i]] when occluded;
 // mode 2: any hit -> occl[i] = 1/0.
+// Resident threads per SM the traversal kernels are compiled for (register budget); 0: no bound.
+#ifndef SST_TRACE_MIN_THREADS
+#define SST_TRACE_MIN_THREADS 0
+#endif
 template <int MODE, int BLOCK, int SSTACK, bool WIDE>
-__global__ void __launch_bounds__(BLOCK) k_trace(const DevJob* __restrict__ jobs, const uint32_t* __restrict__ rayJob, const float4* ro,
+__global__ void __launch_bounds__(BLOCK, SST_TRACE_MIN_THREADS > 0 ? SST_TRACE_MIN_THREADS / BLOCK : 1) k_trace(const DevJob* __restrict__ jobs, const uint32_t* __restrict__ rayJob, const float4* ro,
                                                  const float4* rd, const int* count, int* work, float4* hits, const int* tgt, float4* nee,
                                                  int* occl, DevStats* stats, int countRays) {
     __shared__ int sstack[SSTACK * BLOCK];

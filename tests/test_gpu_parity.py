@@ -556,3 +556,30 @@ def test_camera_views_in_a_batch_equal_scenes_with_those_cameras():
     _native.render_batch(base.native.ctx, jobs)
     for f, s1 in zip(films, singles):
         assert np.array_equal(f, s1)
+
+
+def test_single_triangle_scene_and_empty_queries(bvh_width):
+    """Edge cases of the BVH builders and the query entry points: a one-triangle scene (the
+    single-leaf tree), an empty ray batch, and rays with tmax <= tmin (always a miss)."""
+    sc = Scene()
+    m = Mesh([[-1, -1, 0], [1, -1, 0], [0, 1, 0]], [0, 1, 2])
+    m.Material = DiffuseMaterial(DiffuseMaterial.Parameters(BaseColor=TextureRgb(RgbColor(0.6, 0.5, 0.4))))
+    sc.Meshes.append(m)
+    e = Mesh([[-1, -1, 4], [1, -1, 4], [0, 1, 4]], [0, 2, 1])
+    e.Material = DiffuseMaterial()
+    sc.Meshes.append(e)
+    sc.Emitters.extend(DiffuseEmitter.MakeFromMesh(e, RgbColor(3, 3, 3)))
+    sc.Camera = PerspectiveCamera(Matrix4x4.CreateLookAt([0, 0, 3], [0, 0, 0], [0, 1, 0]), 40)
+    sc.FrameBuffer = FrameBuffer(32, 24)
+    sc.Prepare()
+    g, st = render_gpu(sc, 4, 4)
+    r, rays, _ = render_oracle(sc, 4, 4)
+    assert st.numRays == rays
+    assert per_path_agreement(g, r, 1e-3, 1e-4) >= 0.99
+    empty = np.zeros((0, 8), np.float32)
+    assert sc.native.trace(empty).shape == (0, 12) and sc.native.occluded(empty).shape == (0,)
+    q = np.array([[0, 0, 2, 0, 0, 0, -1, np.inf], [0, 0, 2, 5, 0, 0, -1, 1], [0, 0, 2, 0, 0, 0, -1, 0]], np.float32)
+    hits = sc.native.trace(q)
+    assert hits[0].view(np.int32)[3] == 0 and abs(hits[0, 0] - 2.0) < 1e-5
+    assert np.all(hits[1:].view(np.int32)[:, 3] == -1)
+    assert list(sc.native.occluded(q)) == [1, 0, 0]
