@@ -33,7 +33,10 @@ CONFIGS = {
     2: dict(name="batch_64jobs_10k-1Mtri_128-1024px_4-64spp_depth3-10", builder="batch", jobs=64, seed=2024),
     3: dict(name="cornell_adjoint_tex256_512x512_32spp_depth5", builder="adjoint", W=512, H=512, spp=32, depth=5, tex=256),
     4: dict(name="large_12.3Mtri_8views_1920x1080_256spp_depth10_adjoint_tex1024_rough2000", builder="large", W=1920, H=1080, spp=256, depth=10),
+    5: dict(name="reference_scene_CornellBox.json_512x512_512spp_depth5", builder="scenefile", path="CornellBox/CornellBox.json", W=512, H=512,
+            spp=512, depth=5, seed=571298512, recorded="CornellBox/References/MaxDepth5-Width512-Height512.json"),
 }
+SCENE_DIR = os.path.join(ROOT, "tests", "golden", "scenes")
 
 
 def batch_jobs(cfg, seed_offset=0):
@@ -224,9 +227,14 @@ def run_large(args, cfg):
 
 
 def make_scene(cfg):
-    from seesharp_gb300 import workloads
+    from seesharp_gb300 import FrameBuffer, workloads
     if cfg["builder"] == "cornell":
         return workloads.cornell_box(cfg["W"], cfg["H"])
+    if cfg["builder"] == "scenefile":
+        from seesharp_gb300 import sceneio
+        sc = sceneio.load_json_scene(os.path.join(SCENE_DIR, cfg["path"]))
+        sc.FrameBuffer = FrameBuffer(cfg["W"], cfg["H"])
+        return sc
     return workloads.sphere_field(cfg["spheres"], cfg["W"], cfg["H"])
 
 
@@ -353,7 +361,7 @@ def cpu_sample(cfg, seconds_target=15.0, min_paths=4096, nthreads=None, scene=No
     from oracle import pyoracle as O
     sc = scene if scene is not None else make_scene(cfg)
     o = O.OracleScene.from_scene(sc)
-    p = o.params(cfg["W"], cfg["H"], cfg["spp"], cfg["depth"])
+    p = o.params(cfg["W"], cfg["H"], cfg["spp"], cfg["depth"], baseSeed=cfg.get("seed", 0xC030114))
     nthreads = nthreads or os.cpu_count() or 1
     npix = cfg["W"] * cfg["H"]
     # calibrate on a small sample, then size the sample for ~seconds_target
@@ -421,7 +429,7 @@ def run_ours(args, cfg):
     samples = W * H * spp
     film = torch.zeros((H, W, 3), dtype=torch.float32, device=f"cuda:{local}")
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")
-    params = _native.make_params(W, H, spp, depth)
+    params = _native.make_params(W, H, spp, depth, baseSeed=cfg.get("seed", 0xC030114))
 
     def step():
         return sc.native.render(params, film.data_ptr(), _native.SST_MEM_DEVICE)
@@ -472,7 +480,7 @@ def run_ours(args, cfg):
     for _ in range(e2e_steps):
         sc.FrameBuffer = FrameBuffer(W, H)
         sc.Prepare()
-        PathTracer(TotalSpp=spp, MaxDepth=depth).Render(sc)
+        PathTracer(TotalSpp=spp, MaxDepth=depth, BaseSeed=cfg.get("seed", 0xC030114)).Render(sc)
     e2e_s = max_over_ranks(ws, (time.perf_counter() - t0) / max(e2e_steps, 1))
     e2e_val = samples * ws / e2e_s / 1e6 if e2e_steps else None
     if e2e_steps:
@@ -506,7 +514,8 @@ def run_ours(args, cfg):
         line = {
             "metric": "Msamples/s PathTracer", "value": round(value, 3), "unit": "Msamples/s", "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": round(ms_per_step, 3), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f32", "data": "synthetic (seeded scene generator)",
+            "dtype": "f32",
+            "data": "the reference's own scene file (tests/golden/scenes)" if cfg["builder"] == "scenefile" else "synthetic (seeded scene generator)",
             "config": {"workload": cfg["name"], "triangles": info["triangles"], "emitters": info["emitters"], "bvh_nodes": info["bvh_nodes"],
                        "width": W, "height": H, "spp": spp, "max_depth": depth, "l2": "256 MB buffer written between timed steps",
                        "parallelism": f"replicas x{ws}"},
@@ -522,6 +531,12 @@ def run_ours(args, cfg):
             "clocks": clocks,
             "cpu_baseline": cpu,
         }
+        if cfg.get("recorded"):
+            with open(os.path.join(SCENE_DIR, cfg["recorded"])) as f:
+                rec_ms = float(json.load(f)["RenderTime"])
+            line["reference_recorded"] = {"render_time_ms": rec_ms, "Msamples_per_s": round(samples / rec_ms / 1e3, 4),
+                                          "source": "the reference's stored reference-image metadata for this scene and configuration "
+                                                    "(Data/Scenes/" + cfg["recorded"] + "), measured by its authors on their CPU"}
         print(json.dumps(line), flush=True)
     if ws > 1:
         import torch.distributed as dist

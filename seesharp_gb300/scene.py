@@ -81,6 +81,37 @@ class Matrix4x4:
         sz = sx if sz is None else sz
         return np.diag(np.array([sx, sy, sz, 1], np.float32))
 
+    @staticmethod
+    def CreateFromYawPitchRoll(yaw, pitch, roll):
+        """Rotation by roll about z, then pitch about x, then yaw about y (row vectors), built
+        through the unit quaternion of the three half-angle rotations."""
+        sr, cr = math.sin(roll * 0.5), math.cos(roll * 0.5)
+        sp, cp = math.sin(pitch * 0.5), math.cos(pitch * 0.5)
+        sy, cy = math.sin(yaw * 0.5), math.cos(yaw * 0.5)
+        x = cy * sp * cr + sy * cp * sr
+        y = sy * cp * cr - cy * sp * sr
+        z = cy * cp * sr - sy * sp * cr
+        w = cy * cp * cr + sy * sp * sr
+        m = np.eye(4, dtype=np.float64)
+        m[0, 0] = 1 - 2 * (y * y + z * z)
+        m[0, 1] = 2 * (x * y + z * w)
+        m[0, 2] = 2 * (x * z - y * w)
+        m[1, 0] = 2 * (x * y - z * w)
+        m[1, 1] = 1 - 2 * (z * z + x * x)
+        m[1, 2] = 2 * (y * z + x * w)
+        m[2, 0] = 2 * (x * z + y * w)
+        m[2, 1] = 2 * (y * z - x * w)
+        m[2, 2] = 1 - 2 * (y * y + x * x)
+        return m.astype(np.float32)
+
+    @staticmethod
+    def Invert(m):
+        """(True, inverse) or (False, NaN matrix) like Matrix4x4.Invert."""
+        m = np.asarray(m, np.float64)
+        if abs(np.linalg.det(m)) < 1e-30:
+            return False, np.full((4, 4), np.nan, np.float32)
+        return True, np.linalg.inv(m).astype(np.float32)
+
 
 # ---------------------------------------------------------------------------------------------
 # Geometry
