@@ -224,6 +224,34 @@ typedef struct SstCamera {
     int32_t reserved;
 } SstCamera;
 
+/* ---- frame-buffer layers ------------------------------------------------------------------------
+ * Computed on the device while the film is folded:
+ *  - the VarianceLayer (FrameBuffer.Flags.EstimatePixelVariance, Images/VarianceLayer.cs:10-84);
+ *  - the per-iteration error metrics against FrameBuffer.ReferenceImage (FrameBuffer.cs:276-277,
+ *    378-383): the mean over pixels and channels of (x - r)^2 and of (x - r)^2 / (r^2 + 0.01) (the
+ *    outlier-rejecting RelMSE of SimpleImageIO is not computed);
+ *  - the denoiser's feature layers (DenoiseBuffers.LogPrimaryHit, Integrators/Util/DenoiseBuffers.cs:20-23,
+ *    logged at the primary hit as in PathTracer.cs:336-339): running means of the material's scatter
+ *    strength and of the shading normal.
+ * The running means resume like the film: when firstIteration > 0 the state arrays hold the layers
+ * after iteration firstIteration and are read, and they are always written back. */
+typedef struct SstFilmLayers {
+    float* variance;        /* out: width*height VarianceLayer image, or NULL */
+    float* varianceAverage; /* out: 1 float, VarianceLayer.Average, or NULL */
+    float* varianceState;   /* in/out: 2*width*height running means of the iteration's value and of its
+                               square (required with variance or varianceAverage) */
+    const float* reference; /* in: width*height*3 reference image, or NULL */
+    double* errors;         /* out: 2 per iteration of this call (MSE, RelMSE after it; zero for iterations that a
+                               time limit skipped), or NULL */
+    float* albedo;          /* in/out: width*height*3 "albedo" layer, or NULL */
+    float* normal;          /* in/out: width*height*3 "normal" layer, or NULL */
+    int32_t memory;         /* SST_MEM_HOST / SST_MEM_DEVICE for the arrays above */
+    int32_t reserved;
+} SstFilmLayers;
+/* sst_render that also fills the requested layers. */
+int sst_render_layers(sst_scene* scene, const SstPathTracerParams* params, float* film, int32_t memory, const SstFilmLayers* layers,
+                      SstRenderStats* stats);
+
 /* One render job of a batch. */
 typedef struct SstRenderJob {
     sst_scene* scene;

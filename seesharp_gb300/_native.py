@@ -77,6 +77,12 @@ class SstTuning(ctypes.Structure):
         return {k: int(getattr(self, k)) for k, _ in self._fields_}
 
 
+class SstFilmLayers(ctypes.Structure):
+    _fields_ = [("variance", ctypes.c_void_p), ("varianceAverage", ctypes.c_void_p), ("varianceState", ctypes.c_void_p), ("reference", ctypes.c_void_p),
+                ("errors", ctypes.c_void_p), ("albedo", ctypes.c_void_p), ("normal", ctypes.c_void_p), ("memory", ctypes.c_int32),
+                ("reserved", ctypes.c_int32)]
+
+
 class SstCamera(ctypes.Structure):
     _fields_ = [("worldToCamera", ctypes.c_float * 16), ("verticalFovDegrees", ctypes.c_float), ("reserved", ctypes.c_int32)]
 
@@ -118,6 +124,7 @@ SIGNATURES = {
     "sst_render_batch": [_vp, _P(SstRenderJob), _i32, _P(SstRenderStats)],
     "sst_scene_update_texture": [_vp, _i32, _vp],
     "sst_forward_batch": [_vp, _vp, _i32, _P(SstRenderStats)],
+    "sst_render_layers": [_vp, _P(SstPathTracerParams), _vp, _i32, _P(SstFilmLayers), _P(SstRenderStats)],
     "sst_backward_batch": [_vp, _vp, _i32, _vp, _i32, _vp, _P(SstRenderStats)],
     "sst_forward": [_vp, _P(SstPathTracerParams), _vp, _i32, _P(SstRenderStats)],
     "sst_backward": [_vp, _P(SstPathTracerParams), _vp, _i32, _P(SstGradients), _P(SstRenderStats)],
@@ -375,6 +382,27 @@ class SceneHandle:
         occ = np.zeros(rays.shape[0], np.int32)
         check(self.lib.sst_occluded_noalloc(self.handle, ptr(rays), rays.shape[0], ptr(occ), SST_MEM_HOST))
         return occ
+
+    def render_layers(self, params, film, variance_state=None, reference=None, albedo=None, normal=None):
+        """sst_render_layers into a host film.  variance_state: (2, H, W) float32 running means (in/out)
+        or None; albedo / normal: (H, W, 3) float32 layers (in/out) or None.  Returns (stats,
+        variance image or None, variance average or None, (iterations of this call, 2) array of
+        (MSE, RelMSE) or None)."""
+        W, H = params.width, params.height
+        L = SstFilmLayers()
+        var = np.zeros((H, W), np.float32) if variance_state is not None else None
+        avg = np.zeros(1, np.float32) if variance_state is not None else None
+        ref = None if reference is None else np.ascontiguousarray(reference, np.float32)
+        err = np.zeros((max(0, params.totalSpp - params.firstIteration), 2), np.float64) if reference is not None else None
+        for name, arr in (("variance", var), ("varianceAverage", avg), ("varianceState", variance_state), ("reference", ref), ("errors", err),
+                          ("albedo", albedo), ("normal", normal)):
+            if arr is not None:
+                assert arr.flags["C_CONTIGUOUS"]
+                setattr(L, name, arr.ctypes.data)
+        L.memory = SST_MEM_HOST
+        stats = SstRenderStats()
+        check(self.lib.sst_render_layers(self.handle, ctypes.byref(params), ctypes.c_void_p(film), SST_MEM_HOST, ctypes.byref(L), ctypes.byref(stats)))
+        return stats, var, None if avg is None else float(avg[0]), err
 
     def update_texture(self, tex_id, data):
         d = np.ascontiguousarray(data, np.float32)

@@ -114,6 +114,8 @@ struct sst_ctx {
     DevBuf scratchIn, scratchOut, scratchOut2;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     int* pinnedCount = nullptr;
+    // frame-buffer layers (sst_render_layers)
+    DevBuf layMean, layRef, layErr, layVar, laySum, layAlb, layNrm, aovSamples;
     // batched adjoint: the jobs of the last sst_forward_batch, their path radiance, dLoss/dImage
     std::vector<BatchSig> batchSig;
     std::vector<std::unique_ptr<DevBuf>> batchRecord, batchDLdI;
@@ -734,6 +736,7 @@ struct JobIn {
     DevAdj adj{};  // adjoint buffers (forward record or replay)
     bool hasCam = false;  // a camera view that replaces the scene's camera for this job
     DevCamera cam{};
+    DevLayers lay{};      // frame-buffer layers
 };
 
 // Splits the (job, iteration, pixel) paths into waves of at most `cap` paths.  A job whose
@@ -816,12 +819,18 @@ static void renderJobs(sst_ctx* c, std::vector<JobIn>& jobs, SstRenderStats* out
         w.wb.b.adjL = c->adjB[0].as<float4>(); w.wb.b.adjD = c->adjB[1].as<float4>(); w.wb.b.adjP = c->adjB[2].as<float4>();
         w.wb.neeG = c->neeG.as<float4>();
     }
+    // per-item samples of the denoiser feature layers (written by the first shade, read by the fold)
+    bool anyAov = false;
+    for (auto& j : jobs) anyAov |= j.lay.aovAlbedo != nullptr;
+    if (anyAov) c->aovSamples.ensure(size_t(w.wb.cap) * 24);
     // job table
     std::vector<DevJob> hj(jobs.size());
     for (size_t k = 0; k < jobs.size(); ++k) {
         const SstPathTracerParams* P = &jobs[k].p;
         hj[k].sc = jobs[k].s->dev;
         if (jobs[k].hasCam) hj[k].sc.cam = jobs[k].cam;
+        hj[k].lay = jobs[k].lay;
+        if (hj[k].lay.aovAlbedo) hj[k].lay.aovSamples = c->aovSamples.as<float>();
         hj[k].cfg = PTConfig{P->width, P->height, P->maxDepth, P->minDepth, P->baseSeed, P->numShadowRays, P->enableBsdfDI, P->ignoreNanAndInf};
         hj[k].adj = jobs[k].adj;
     }
@@ -1544,6 +1553,96 @@ static SstRenderStats emptyStats() {
     SstRenderStats t{};
     for (int k = 0; k < 4; ++k) { t.nanPixel[k] = -1; t.nanIteration[k] = -1; }
     return t;
+}
+
+int sst_render_layers(sst_scene* s, const SstPathTracerParams* p, float* film, int32_t memory, const SstFilmLayers* L, SstRenderStats* stats) {
+    return guarded([&] {
+        if (!s || !p || !film || !L) fail(SST_ERR_INVALID_ARGUMENT, "NULL argument");
+        checkParams(s, p);
+        const bool wantVar = L->variance || L->varianceAverage;
+        if (wantVar && !L->varianceState) fail(SST_ERR_INVALID_ARGUMENT, "the variance layer needs its state array");
+        if (L->errors && !L->reference) fail(SST_ERR_INVALID_ARGUMENT, "error metrics need a reference image");
+        if ((L->albedo == nullptr) != (L->normal == nullptr)) fail(SST_ERR_INVALID_ARGUMENT, "albedo and normal layers come together");
+        sst_ctx* c = s->ctx;
+        cudaStream_t st = c->stream;
+        CUDA_CHECK(cudaSetDevice(c->device));
+        const size_t P = size_t(p->width) * p->height;
+        const int first = p->firstIteration, S = p->totalSpp;
+        const bool resume = first > 0;
+        const cudaMemcpyKind in = L->memory == SST_MEM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+        const cudaMemcpyKind out = L->memory == SST_MEM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+        SstRenderStats local = emptyStats();
+        float* dFilm = film;
+        if (memory != SST_MEM_DEVICE) {
+            c->film.ensure(P * 12);
+            dFilm = c->film.as<float>();
+            if (resume) CUDA_CHECK(cudaMemcpyAsync(dFilm, film, P * 12, cudaMemcpyHostToDevice, st));
+        }
+        if (!resume) CUDA_CHECK(cudaMemsetAsync(dFilm, 0, P * 12, st));
+        std::vector<JobIn> jobs(1);
+        jobs[0].s = s;
+        jobs[0].p = *p;
+        jobs[0].dFilm = dFilm;
+        jobs[0].iterFirst = first;
+        jobs[0].iterEnd = std::max(first, S);
+        DevLayers& lay = jobs[0].lay;
+        // layer state: read back in when resuming, zero otherwise
+        auto state = [&](DevBuf& b, size_t bytes, const float* src) {
+            b.ensure(bytes);
+            if (resume) CUDA_CHECK(cudaMemcpyAsync(b.p, src, bytes, in, st));
+            else CUDA_CHECK(cudaMemsetAsync(b.p, 0, bytes, st));
+            return b.as<float>();
+        };
+        if (wantVar) {
+            lay.varMean = state(c->layMean, P * 8, L->varianceState);  // mean plane, then moment plane
+            lay.varMoment = lay.varMean + P;
+        }
+        if (L->albedo) {
+            lay.aovAlbedo = state(c->layAlb, P * 12, L->albedo);
+            lay.aovNormal = state(c->layNrm, P * 12, L->normal);
+        }
+        if (L->reference) {
+            lay.ref = toDevice(c, c->layRef, L->reference, P * 3, L->memory);
+            c->layErr.ensure(std::max<size_t>(1, size_t(S) * 16));
+            CUDA_CHECK(cudaMemsetAsync(c->layErr.p, 0, std::max<size_t>(1, size_t(S) * 16), st));
+            lay.errSum = c->layErr.as<double>();
+        }
+        if (first < S) renderJobs(c, jobs, &local);
+        if (wantVar) {
+            CUDA_CHECK(cudaMemcpyAsync(L->varianceState, lay.varMean, P * 8, out, st));
+            c->layVar.ensure(P * 4);
+            c->laySum.ensure(8);
+            CUDA_CHECK(cudaMemsetAsync(c->laySum.p, 0, 8, st));
+            launch_variance_finish(lay.varMean, lay.varMoment, p->width, p->height, c->layVar.as<float>(), c->laySum.as<double>(), st);
+            CUDA_CHECK(cudaGetLastError());
+            if (L->variance) CUDA_CHECK(cudaMemcpyAsync(L->variance, c->layVar.p, P * 4, out, st));
+            if (L->varianceAverage) {
+                double sum = 0.0;
+                CUDA_CHECK(cudaMemcpyAsync(&sum, c->laySum.p, 8, cudaMemcpyDeviceToHost, st));
+                CUDA_CHECK(cudaStreamSynchronize(st));
+                float avg = float(sum / double(P));
+                if (L->memory == SST_MEM_DEVICE) CUDA_CHECK(cudaMemcpy(L->varianceAverage, &avg, 4, cudaMemcpyHostToDevice));
+                else *L->varianceAverage = avg;
+            }
+        }
+        if (L->albedo) {
+            CUDA_CHECK(cudaMemcpyAsync(L->albedo, lay.aovAlbedo, P * 12, out, st));
+            CUDA_CHECK(cudaMemcpyAsync(L->normal, lay.aovNormal, P * 12, out, st));
+        }
+        if (L->errors && first < S) {
+            std::vector<double> e(2 * size_t(S));
+            CUDA_CHECK(cudaMemcpyAsync(e.data(), c->layErr.p, e.size() * 8, cudaMemcpyDeviceToHost, st));
+            CUDA_CHECK(cudaStreamSynchronize(st));
+            for (auto& x : e) x /= double(3 * P);
+            const double* src = e.data() + 2 * size_t(first);
+            size_t n = 2 * size_t(S - first);
+            if (L->memory == SST_MEM_DEVICE) CUDA_CHECK(cudaMemcpy(L->errors, src, n * 8, cudaMemcpyHostToDevice));
+            else std::copy(src, src + n, L->errors);
+        }
+        if (memory != SST_MEM_DEVICE) CUDA_CHECK(cudaMemcpyAsync(film, dFilm, P * 12, cudaMemcpyDeviceToHost, st));
+        CUDA_CHECK(cudaStreamSynchronize(st));
+        if (stats) *stats = local;
+    });
 }
 
 int sst_render_batch(sst_ctx* ctx, const SstRenderJob* jobs, int32_t numJobs, SstRenderStats* stats) {

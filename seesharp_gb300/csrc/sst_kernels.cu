@@ -6,6 +6,7 @@
 //   k_shade       -> one bounce of EstimateIncidentRadiance (PathTracer.cs:318-378), with queue
 //                    compaction and the FrameBuffer.Splat running mean (Images/FrameBuffer.cs:166-191)
 #include <cooperative_groups.h>
+#include <cooperative_groups/reduce.h>
 #include <cuda_runtime.h>
 
 #include "sst_adjoint.cuh"
@@ -140,6 +141,14 @@ __global__ void k_film_fold(const DevJob* __restrict__ jobs, const WaveChunk* __
         size_t pix = (size_t)(ck.pixStart + p);
         float* f = ck.film + 3 * pix;
         float3 cur = mk(f[0], f[1], f[2]);
+        const DevLayers& lay = jobs[ck.job].lay;
+        float vMean = lay.varMean ? lay.varMean[pix] : 0.0f, vMoment = lay.varMoment ? lay.varMoment[pix] : 0.0f;
+        float3 ref = lay.ref ? mk(lay.ref[3 * pix], lay.ref[3 * pix + 1], lay.ref[3 * pix + 2]) : mk(0, 0, 0);
+        float3 alb = mk(0, 0, 0), nrm = mk(0, 0, 0);
+        if (lay.aovAlbedo) {
+            alb = mk(lay.aovAlbedo[3 * pix], lay.aovAlbedo[3 * pix + 1], lay.aovAlbedo[3 * pix + 2]);
+            nrm = mk(lay.aovNormal[3 * pix], lay.aovNormal[3 * pix + 1], lay.aovNormal[3 * pix + 2]);
+        }
         for (int m = 0; m < ck.nIter; ++m) {
             uint32_t iter = (uint32_t)(ck.iterBase + m);
             const float* s = samples + 3 * ((size_t)ck.itemOffset + (size_t)m * ck.pixCount + p);
@@ -157,9 +166,56 @@ __global__ void k_film_fold(const DevJob* __restrict__ jobs, const WaveChunk* __
                 unsigned long long k = atomicAdd(&st->nanCount, 1ull);
                 if (k < 4) { st->nanPixel[k] = (int)pix; st->nanIter[k] = (int)iter + 1; }
             }
-            if (finite || !cfg.ignoreNan) cur = cur + v / kf;
+            bool used = finite || !cfg.ignoreNan;
+            if (used) cur = cur + v / kf;
+            if (lay.aovAlbedo) {
+                // RgbLayer running means (Images/Layer.cs:33-37, RgbLayer.cs:17-18)
+                const float* a6 = lay.aovSamples + 6 * ((size_t)ck.itemOffset + (size_t)m * ck.pixCount + p);
+                if (iter > 0) {
+                    alb = alb * ((kf - 1.0f) / kf);
+                    nrm = nrm * ((kf - 1.0f) / kf);
+                }
+                alb = alb + mk(a6[0], a6[1], a6[2]) / kf;
+                nrm = nrm + mk(a6[3], a6[4], a6[5]) / kf;
+            }
+            if (lay.varMean) {
+                // VarianceLayer (Images/VarianceLayer.cs:41-65): both images are running means of the
+                // iteration's splatted value (the sample's channel average, 0 if it was skipped)
+                float val = used ? a : 0.0f;
+                if (iter > 0) {
+                    vMoment = vMoment * ((kf - 1.0f) / kf);
+                    vMean = vMean * ((kf - 1.0f) / kf);
+                }
+                vMoment = vMoment + val * val / kf;
+                vMean = vMean + val / kf;
+            }
+            if (lay.ref) {
+                // FrameBuffer error metrics after iteration iter + 1 (FrameBuffer.cs:276-277, 378-383)
+                float3 d = cur - ref;
+                double e1 = (double)d.x * d.x + (double)d.y * d.y + (double)d.z * d.z;
+                double e2 = (double)d.x * d.x / ((double)ref.x * ref.x + 0.01) + (double)d.y * d.y / ((double)ref.y * ref.y + 0.01) +
+                            (double)d.z * d.z / ((double)ref.z * ref.z + 0.01);
+                cg::coalesced_group act = cg::coalesced_threads();
+                cg::coalesced_group grp = cg::labeled_partition(act, (int)iter);
+                e1 = cg::reduce(grp, e1, cg::plus<double>());
+                e2 = cg::reduce(grp, e2, cg::plus<double>());
+                if (grp.thread_rank() == 0) {
+                    atomicAdd(lay.errSum + 2 * (size_t)iter, e1);
+                    atomicAdd(lay.errSum + 2 * (size_t)iter + 1, e2);
+                }
+            }
         }
         f[0] = cur.x; f[1] = cur.y; f[2] = cur.z;
+        if (lay.varMean) {
+            lay.varMean[pix] = vMean;
+            lay.varMoment[pix] = vMoment;
+        }
+        if (lay.aovAlbedo) {
+            float* A = lay.aovAlbedo + 3 * pix;
+            float* N = lay.aovNormal + 3 * pix;
+            A[0] = alb.x; A[1] = alb.y; A[2] = alb.z;
+            N[0] = nrm.x; N[1] = nrm.y; N[2] = nrm.z;
+        }
     }
     // the last block to finish advances the wave counter (one CUDA graph serves every wave)
     if (advance) {
@@ -174,6 +230,38 @@ __global__ void k_film_fold(const DevJob* __restrict__ jobs, const WaveChunk* __
             }
         }
     }
+}
+
+// VarianceLayer.OnEndIteration (Images/VarianceLayer.cs:57-84): both images blurred by a 3x3 box
+// (the mean of the window's pixels inside the image), variance = (moment - mean^2) / (mean^2 +
+// 0.001), and the image average (summed in double).
+__global__ void k_variance_finish(const float* mean, const float* moment, int W, int H, float* out, double* sum) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    double v = 0.0;
+    if (i < W * H) {
+        int x = i % W, y = i / W;
+        float sm = 0.0f, so = 0.0f;
+        int n = 0;
+        for (int dy = -1; dy <= 1; ++dy)
+            for (int dx = -1; dx <= 1; ++dx) {
+                int xx = x + dx, yy = y + dy;
+                if (xx < 0 || yy < 0 || xx >= W || yy >= H) continue;
+                sm += mean[yy * W + xx];
+                so += moment[yy * W + xx];
+                ++n;
+            }
+        float bm = sm / (float)n, bo = so / (float)n;
+        float var = (bo - bm * bm) / (bm * bm + 0.001f);
+        out[i] = var;
+        v = var;
+    }
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0) atomicAdd(sum, v);
+}
+
+void launch_variance_finish(const float* mean, const float* moment, int W, int H, float* out, double* sum, cudaStream_t s) {
+    int n = W * H;
+    k_variance_finish<<<(n + 255) / 256, 256, 0, s>>>(mean, moment, W, H, out, sum);
 }
 
 void launch_film_fold(const DevJob* jobs, const WaveChunk* chunks, const WaveDesc* waves, int* curWave, const float* samples, DevStats* st,
@@ -294,6 +382,11 @@ __global__ void __launch_bounds__(128, ADJ ? SST_SHADE_ADJ_MIN_BLOCKS : SST_SHAD
             float3 rdir = f3(rd4);
             float4 h = hits[i];
             int ti = __float_as_int(h.w);
+            float* aov = (!ADJ && depth == 1) ? jobs[job].lay.aovSamples : nullptr;
+            if (aov && ti < 0) {  // no primary hit: nothing is logged this iteration
+                float* a6 = aov + 6 * (size_t)pix;
+                a6[0] = a6[1] = a6[2] = a6[3] = a6[4] = a6[5] = 0.0f;
+            }
             if (ti < 0) {
                 // OnBackgroundHit (PathTracer.cs:384-400)
                 if ((int)depth >= cfg.minDepth && sc.hasEnv && cfg.enableBsdfDI) {
@@ -335,6 +428,15 @@ __global__ void __launch_bounds__(128, ADJ ? SST_SHADE_ADJ_MIN_BLOCKS : SST_SHAD
                     s.uv = make_float2(u, v);
                 }
                 hitPos = s.pos;
+                if (aov) {
+                    // DenoiseBuffers.LogPrimaryHit (PathTracer.cs:336-339): GetScatterStrength is the base
+                    // colour at the hit for both materials (DiffuseMaterial.cs:37-38, GenericMaterial.cs:65)
+                    const DevMaterial& mm = sc.mats[s.mat];
+                    float3 alb = lookupRgb(sc, mm.baseTex, mm.base, s.uv);
+                    float* a6 = aov + 6 * (size_t)pix;
+                    a6[0] = alb.x; a6[1] = alb.y; a6[2] = alb.z;
+                    a6[3] = s.sn.x; a6[4] = s.sn.y; a6[5] = s.sn.z;
+                }
                 // SurfaceShader / ShadingContext (PathTracer.cs:334)
                 Ctx c;
                 c.f.n = s.sn;

@@ -9,6 +9,7 @@ namespace sst {
 void launch_env_build(const float4* img, int w, int h, float* colCdf, float* rowMarg, int* hasCol, float* rowCdf, cudaStream_t s);
 void launch_camera(const DevJob* jobs, const WaveChunk* chunks, const WaveDesc* waves, const int* curWave, const PathBuf& A, int* qCount,
                    int maxItems, cudaStream_t s);
+void launch_variance_finish(const float* mean, const float* moment, int W, int H, float* out, double* sum, cudaStream_t s);
 void launch_film_fold(const DevJob* jobs, const WaveChunk* chunks, const WaveDesc* waves, int* curWave, const float* samples, DevStats* st,
                       int maxFold, int advance, cudaStream_t s);
 // Traversal launch configuration (sst_trace.cu): threads per block (64, 128 or 256), stack

@@ -103,12 +103,24 @@ struct DevAdj {
     float* gEmitter;      // 3 per emitter: radiance
 };
 
+// Frame-buffer layers of a job (all NULL unless requested).
+struct DevLayers {
+    float* varMean;     // per pixel: running mean of the iteration's pixel value (VarianceLayer meanImage)
+    float* varMoment;   // per pixel: running mean of its square (VarianceLayer momentImage)
+    const float* ref;   // W*H*3 reference image for the per-iteration error metrics
+    double* errSum;     // 2 per iteration: sums of squared and of relative squared errors
+    float* aovAlbedo;   // W*H*3 running mean of the primary hit's scatter strength
+    float* aovNormal;   // W*H*3 running mean of the primary hit's shading normal
+    float* aovSamples;  // 6 per wave item: this iteration's (albedo, normal), written by the first shade
+};
+
 // One render job: its scene and path-tracer settings (the kernels index this table by the job
 // id every path carries).
 struct DevJob {
     DevScene sc;
     PTConfig cfg;
     DevAdj adj;
+    DevLayers lay;
 };
 
 // A chunk of a wave: nIter consecutive iterations of the pixel range [pixStart, pixStart +

@@ -164,6 +164,38 @@ class TextureMono(ImageTexture):
             self.constColor = float(np.float32(value))
 
 
+class Layer:
+    """Images/Layer.cs: an auxiliary frame-buffer image, a running mean over the iterations."""
+
+    def __init__(self):
+        self.Image = None
+
+    def Init(self, width, height):
+        raise NotImplementedError
+
+
+class RgbLayer(Layer):
+    """Images/RgbLayer.cs: an RGB running mean (the denoiser's "albedo" and "normal" features)."""
+
+    def Init(self, width, height):
+        self.Image = RgbImage(width, height)
+
+
+class VarianceLayer(Layer):
+    """Images/VarianceLayer.cs: the relative pixel variance image (MonochromeImage) and its
+    average, filled by the GPU film fold when the frame buffer has EstimatePixelVariance.  The
+    running means of the iteration values and of their squares are kept for resumed renders."""
+
+    def __init__(self):
+        super().__init__()
+        self.Average = 0.0
+        self.state = None
+
+    def Init(self, width, height):
+        self.Image = MonochromeImage(width, height)
+        self.state = np.zeros((2, height, width), np.float32)
+
+
 class FrameBuffer:
     """Progressive film with a running mean over iterations (Images/FrameBuffer.cs).
 
@@ -172,14 +204,14 @@ class FrameBuffer:
     """
 
     class Flags(enum.IntFlag):
-        # Images/FrameBuffer.cs:101-133
+        # Images/FrameBuffer.cs:100-133
         None_ = 0
         WriteIntermediate = 1
         WriteContinously = 2
-        WriteExponentially = 4
-        SendToTev = 8
+        SendToTev = 4
+        EstimatePixelVariance = 8
         IgnoreNanAndInf = 16
-        EstimatePixelVariance = 32
+        WriteExponentially = 32
         Recommended = 16
 
     def __init__(self, width, height, filename="", flags=None):
@@ -191,15 +223,35 @@ class FrameBuffer:
         self.CurIteration = 0
         self.MetaData = {}
         self.NaNWarnings = []
+        self.ReferenceImage = None   # RgbImage: per-iteration error metrics are recorded in Errors
+        self.Errors = []             # (TimeMS, MSE, RelMSE, RelMSE_Outlier) per iteration
+        self.layers = {}
+        self.PixelVariance = None
+        if self.flags & FrameBuffer.Flags.EstimatePixelVariance:
+            self.PixelVariance = VarianceLayer()
+            self.AddLayer("variance", self.PixelVariance)
+
+    def AddLayer(self, name, layer):
+        """FrameBuffer.AddLayer (FrameBuffer.cs:60): the layer is initialised to the buffer's size."""
+        layer.Init(self.Width, self.Height)
+        self.layers[name] = layer
+
+    def GetLayer(self, name):
+        return self.layers[name]
 
     @property
     def IgnoreNanAndInf(self):
         return bool(self.flags & FrameBuffer.Flags.IgnoreNanAndInf)
 
     def Reset(self):
-        """FrameBuffer.Reset (FrameBuffer.cs:296-299) plus clearing the image."""
+        """FrameBuffer.Reset (FrameBuffer.cs:296-299) plus clearing the image and the layers."""
         self.CurIteration = 0
         self.Image = RgbImage(self.Width, self.Height)
+        self.Errors = []
+        for layer in self.layers.values():
+            layer.Init(self.Width, self.Height)
+            if isinstance(layer, VarianceLayer):
+                layer.Average = 0.0
 
     def WriteToFile(self, filename=None):
         """Writes the image as a PFM (little endian, bottom row first) and the metadata as JSON.

@@ -11,6 +11,7 @@ from __future__ import annotations
 import numpy as np
 
 from . import _native
+from .images import MonochromeImage, RgbLayer
 
 
 class Integrator:
@@ -39,8 +40,9 @@ class PathTracer(Integrator):
         self.NumShadowRays = 1
         self.EnableBsdfDI = True
         self.RenderTechniquePyramid = False
-        # The reference denoises the last iteration with Open Image Denoise by default; denoising
-        # is outside this library, so the flag is accepted and has no effect.
+        # The reference logs the denoiser's albedo / normal layers and denoises the last iteration
+        # with Open Image Denoise by default; the layers are computed on the GPU, the denoiser is
+        # outside this library.
         self.EnableDenoiser = True
         for k, v in kw.items():
             if not hasattr(self, k):
@@ -76,7 +78,28 @@ class PathTracer(Integrator):
             return
         film = fb.Image.data
         assert film.dtype == np.float32 and film.flags["C_CONTIGUOUS"]
-        stats = scene.native.render(p, film.ctypes.data)
+        if self.EnableDenoiser:
+            # DenoiseBuffers (Integrators/Util/DenoiseBuffers.cs:10-15): the feature layers; the
+            # denoiser itself (Open Image Denoise) is outside this library
+            for name in ("albedo", "normal"):
+                if name not in fb.layers:
+                    fb.AddLayer(name, RgbLayer())
+        albedo = fb.layers["albedo"].Image.data if "albedo" in fb.layers else None
+        normal = fb.layers["normal"].Image.data if "normal" in fb.layers else None
+        var = fb.PixelVariance
+        if var is not None or fb.ReferenceImage is not None or albedo is not None:
+            ref = None if fb.ReferenceImage is None else fb.ReferenceImage.data
+            stats, vimg, avg, err = scene.native.render_layers(p, film.ctypes.data, variance_state=None if var is None else var.state,
+                                                               reference=ref, albedo=albedo, normal=normal)
+            if var is not None:
+                var.Image = MonochromeImage(vimg)
+                var.Average = avg
+            if err is not None:
+                # per-iteration times are not separable in the wavefront: the render time is prorated
+                n = int(stats.numIterations)
+                fb.Errors += [(int(round(stats.renderTimeMs * (k + 1) / max(n, 1))), float(err[k, 0]), float(err[k, 1]), None) for k in range(n)]
+        else:
+            stats = scene.native.render(p, film.ctypes.data)
         fb.CurIteration = fb.CurIteration + stats.numIterations
         fb.MetaData["NumIterations"] = fb.CurIteration
         fb.MetaData["RenderTime"] = stats.renderTimeMs
