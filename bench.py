@@ -527,7 +527,7 @@ def run_ours(args, cfg):
             "kernel_ms": {k: round(v["ms"], 3) for k, v in ktimes.items()},
             "kernel_ms_note": "one extra render with per-kernel CUDA events after the timed region",
             "tuning": tuning, "autotune_s": round(tune_s, 3),
-            "prepare_s": round(prep_s, 3), "bvh": os.environ.get("SST_BVH", "lbvh"),
+            "prepare_s": round(prep_s, 3), "bvh": os.environ.get("SST_BVH", "ploc"),
             "clocks": clocks,
             "cpu_baseline": cpu,
         }
@@ -563,7 +563,7 @@ def main():
         if a is not None:
             cfg[k] = a
             cfg["name"] = cfg["name"] + f"_{k}{a}"
-    os.environ.setdefault("SST_BVH", "lbvh")
+    os.environ.setdefault("SST_BVH", "ploc")
     if args.impl == "reference" and cfg["builder"] in ("adjoint", "large"):
         if dist_info()[1] == 0:
             print(json.dumps({"impl": "reference", "unavailable": "the reference PathTracer has no adjoint (differentiation is new in this library)"}))

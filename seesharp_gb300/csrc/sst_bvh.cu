@@ -13,7 +13,9 @@
 //      child boxes in the parent, 64-byte nodes); a collapsed subtree becomes one leaf reference
 //      to its contiguous range of sorted triangles.
 #include <cub/cub.cuh>
+#include <math_constants.h>
 #include <algorithm>
+#include <cstdlib>
 #include <cuda_runtime.h>
 
 #include "sst_bvh.h"
@@ -190,6 +192,159 @@ __global__ void k_kept(const int* parentInner, const int* collapse, int n, int* 
     if (k) atomicMax(maxDepth, depth);
 }
 
+// ---------------------------------------------------------------------------------------------
+// PLOC topology (Meister and Bittner, "Parallel Locally-Ordered Clustering for Bounding Volume
+// Hierarchy Construction", 2018): the clusters start as the Morton-sorted leaves; in each round
+// every cluster finds the cluster within a radius of positions whose union box has the smallest
+// surface area, mutual nearest neighbours merge into a new inner node, and the cluster list is
+// compacted in order.  The resulting tree is then given a depth-first leaf order so that every
+// subtree covers a contiguous range, and the LBVH's refit / collapse / emit stages finish it.
+// ---------------------------------------------------------------------------------------------
+
+__device__ __forceinline__ float unionArea(const float* a, const float* b) {
+    float lo[3], hi[3];
+    for (int k = 0; k < 3; ++k) { lo[k] = fminf(a[k], b[k]); hi[k] = fmaxf(a[3 + k], b[3 + k]); }
+    return areaOf(lo, hi);
+}
+
+// clusters = sorted leaves ~i with their triangle boxes
+__global__ void k_ploc_init(const float4* tri, const int* order, int n, int* clus, float* cbox) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    int t = order[i];
+    float4 a = tri[3 * (size_t)t], b = tri[3 * (size_t)t + 1], d = tri[3 * (size_t)t + 2];
+    float* o = cbox + 6 * (size_t)i;
+    o[0] = fminf(a.x, fminf(b.x, d.x)); o[3] = fmaxf(a.x, fmaxf(b.x, d.x));
+    o[1] = fminf(a.y, fminf(b.y, d.y)); o[4] = fmaxf(a.y, fmaxf(b.y, d.y));
+    o[2] = fminf(a.z, fminf(b.z, d.z)); o[5] = fmaxf(a.z, fmaxf(b.z, d.z));
+    clus[i] = ~i;
+}
+
+// nearest neighbour within `radius` positions (ties: the smaller index)
+__global__ void k_ploc_nn(const float* cbox, const int* nc, int radius, int* nn) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    int n = *nc;
+    if (i >= n) return;
+    float me[6];
+    for (int k = 0; k < 6; ++k) me[k] = cbox[6 * (size_t)i + k];
+    float best = CUDART_INF_F;
+    int bj = -1;
+    int j0 = max(0, i - radius), j1 = min(n - 1, i + radius);
+    for (int j = j0; j <= j1; ++j) {
+        if (j == i) continue;
+        float a = unionArea(me, cbox + 6 * (size_t)j);
+        if (a < best) { best = a; bj = j; }
+    }
+    nn[i] = bj;
+}
+
+// flags: create[i] = i merges with its mutual neighbour (i the lower index); keep[i] = cluster i
+// (possibly merged) stays in the list
+__global__ void k_ploc_flags(const int* nn, const int* nc, int* create, int* keep) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    int n = *nc;
+    if (i >= n) return;
+    int j = nn[i];
+    bool mutual = j >= 0 && nn[j] == i;
+    create[i] = (mutual && i < j) ? 1 : 0;
+    keep[i] = (!mutual || i < j) ? 1 : 0;
+}
+
+// merged clusters become inner nodes numbered base + createIdx[i] in creation order
+__global__ void k_ploc_compact(const int* clus, const float* cbox, const int* nn, const int* nc, const int* create, const int* createIdx,
+                               const int* keep, const int* newPos, int base, int* clusOut, float* cboxOut, int2* child, float* ibox) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    int n = *nc;
+    if (i >= n || !keep[i]) return;
+    int out = newPos[i];
+    if (create[i]) {
+        int j = nn[i];
+        int id = base + createIdx[i];
+        child[id] = make_int2(clus[i], clus[j]);
+        float* b = cboxOut + 6 * (size_t)out;
+        for (int k = 0; k < 3; ++k) {
+            b[k] = fminf(cbox[6 * (size_t)i + k], cbox[6 * (size_t)j + k]);
+            b[3 + k] = fmaxf(cbox[6 * (size_t)i + 3 + k], cbox[6 * (size_t)j + 3 + k]);
+        }
+        for (int k = 0; k < 6; ++k) ibox[6 * (size_t)id + k] = b[k];
+        clusOut[out] = id;
+    } else {
+        clusOut[out] = clus[i];
+        for (int k = 0; k < 6; ++k) cboxOut[6 * (size_t)out + k] = cbox[6 * (size_t)i + k];
+    }
+}
+
+// creation ids -> final ids (root = 0: reversed creation order); parent pointers
+__global__ void k_ploc_renumber(const int2* childC, int n, int2* child, int* parentInner, int* parentLeaf) {
+    int id = blockIdx.x * blockDim.x + threadIdx.x;
+    if (id >= n - 1) return;
+    int nid = (n - 2) - id;
+    int2 c = childC[id];
+    int a = c.x >= 0 ? (n - 2) - c.x : c.x;
+    int b = c.y >= 0 ? (n - 2) - c.y : c.y;
+    child[nid] = make_int2(a, b);
+    if (a < 0) parentLeaf[~a] = nid; else parentInner[a] = nid;
+    if (b < 0) parentLeaf[~b] = nid; else parentInner[b] = nid;
+}
+
+// subtree leaf counts, bottom-up from every leaf (the second child to arrive continues)
+__global__ void k_ploc_sizes(const int2* child, const int* parentLeaf, const int* parentInner, int n, int* visits, int* size) {
+    int li = blockIdx.x * blockDim.x + threadIdx.x;
+    if (li >= n) return;
+    int node = parentLeaf[li];
+    while (node >= 0) {
+        __threadfence();
+        if (atomicAdd(&visits[node], 1) == 0) return;
+        __threadfence();
+        int2 c = child[node];
+        int sa = c.x < 0 ? 1 : ((const volatile int*)size)[c.x];
+        int sb = c.y < 0 ? 1 : ((const volatile int*)size)[c.y];
+        size[node] = sa + sb;
+        node = parentInner[node];
+    }
+}
+
+// depth-first offsets: a node's first leaf is the number of leaves left of it, summed over the
+// ancestors of which it lies in the right subtree.  Inner nodes get their leaf range; leaves their
+// position in the new order.
+__global__ void k_ploc_offsets(const int2* child, const int* parentInner, const int* parentLeaf, const int* size, int n, int2* range,
+                               int* leafPos) {
+    int x = blockIdx.x * blockDim.x + threadIdx.x;
+    if (x >= 2 * n - 1) return;
+    bool leaf = x >= n - 1;
+    int self = leaf ? ~(x - (n - 1)) : x;
+    int p = leaf ? parentLeaf[x - (n - 1)] : parentInner[x];
+    int off = 0, cur = self;
+    for (int guard = 0; p >= 0 && guard < 1 << 20; ++guard) {
+        int2 c = child[p];
+        if (c.y == cur) off += c.x < 0 ? 1 : size[c.x];
+        cur = p;
+        p = parentInner[p];
+    }
+    if (leaf) leafPos[x - (n - 1)] = off;
+    else range[x] = make_int2(off, off + size[x] - 1);
+}
+
+__global__ void k_ploc_leaf_parents(const int2* child, int n, int* parentLeaf) {
+    int x = blockIdx.x * blockDim.x + threadIdx.x;
+    if (x >= n - 1) return;
+    int2 c = child[x];
+    if (c.x < 0) parentLeaf[~c.x] = x;
+    if (c.y < 0) parentLeaf[~c.y] = x;
+}
+
+// leaves re-encoded by their depth-first position; the triangle order follows
+__global__ void k_ploc_reorder(int2* child, const int* leafPos, const int* sortedOrder, int n, int* order) {
+    int x = blockIdx.x * blockDim.x + threadIdx.x;
+    if (x < n) order[leafPos[x]] = sortedOrder[x];
+    if (x < n - 1) {
+        int2 c = child[x];
+        if (c.x < 0) c.x = ~leafPos[~c.x];
+        if (c.y < 0) c.y = ~leafPos[~c.y];
+        child[x] = c;
+    }
+}
+
 __device__ __forceinline__ uint32_t leafRef(int first, int count) {
     return kLeafFlag | ((uint32_t)(count - 1) << kLeafCountShift) | (uint32_t)first;
 }
@@ -267,12 +422,13 @@ size_t lbvhScratchBytes(int n) {
     s += sizeof(int) * n * 2;                                        // parents
     s += sizeof(int) * n * 4;                                        // visits, collapse, kept, newIdx
     s += sizeof(float) * n * 7;                                      // boxes, cost
+    s += sizeof(int) * n * 11 + sizeof(float) * n * 18 + sizeof(int2) * n + 4096;  // PLOC clusters, boxes, flags, sizes
     s += tmp + 64 * 256 + 64;
     return s;
 }
 
 int buildLbvh(const float4* tri, int n, float4* nodesOut, int* orderOut, void* scratch, size_t scratchBytes, int* hostNodeCount, int* hostMaxDepth,
-              cudaStream_t st) {
+              cudaStream_t st, int method) {
     if (n <= 0) { *hostNodeCount = 0; *hostMaxDepth = 0; return 0; }
     if (n == 1) {
         k_emit_single<<<1, 1, 0, st>>>(tri, nodesOut);
@@ -310,8 +466,69 @@ int buildLbvh(const float4* tri, int n, float4* nodesOut, int* orderOut, void* s
     cub::DeviceRadixSort::SortPairs(tmp, tmpBytes, keysA, keysB, valsA, valsB, n, 0, 63, st);
     cudaMemsetAsync(parentInner, 0xFF, sizeof(int) * n, st);
     cudaMemsetAsync(visits, 0, sizeof(int) * n, st);
-    k_karras<<<grid, 256, 0, st>>>(keysB, n, range, child, parentInner, parentLeaf);
-    k_refit<<<grid, 256, 0, st>>>(tri, valsB, n, range, child, parentInner, parentLeaf, visits, boxes, cost, collapse);
+    const int* order = valsB;
+    if (method == 1 && n > 2) {
+        // PLOC topology in place of the radix tree
+        const char* re = getenv("SST_PLOC_RADIUS");
+        const int plocRadius = re ? std::max(1, std::min(256, atoi(re))) : 16;
+        int* clus = carve<int>(p, n);
+        int* clus2 = carve<int>(p, n);
+        float* cbox = carve<float>(p, 6 * size_t(n));
+        float* cbox2 = carve<float>(p, 6 * size_t(n));
+        float* ibox = carve<float>(p, 6 * size_t(n));
+        int* nn = carve<int>(p, n);
+        int* create = carve<int>(p, n);
+        int* keep = carve<int>(p, n);
+        int* createIdx = carve<int>(p, n);
+        int* newPos = carve<int>(p, n);
+        int* nc = carve<int>(p, 4);
+        int2* childC = carve<int2>(p, n);
+        int* size = carve<int>(p, n);
+        int* leafPos = carve<int>(p, n);
+        int* order2 = carve<int>(p, n);
+        if (size_t(p - static_cast<char*>(scratch)) > scratchBytes) return -2;
+        k_ploc_init<<<grid, 256, 0, st>>>(tri, valsB, n, clus, cbox);
+        int ncH = n, base = 0;
+        cudaMemcpyAsync(nc, &ncH, sizeof(int), cudaMemcpyHostToDevice, st);
+        size_t scanBytes = 0;
+        cub::DeviceScan::ExclusiveSum(nullptr, scanBytes, create, createIdx, n, st);
+        if (scanBytes > tmpBytes) return -2;
+        for (int round = 0; ncH > 1; ++round) {
+            if (round > n) return -3;  // each round merges at least the globally closest pair
+            int g = (ncH + 255) / 256;
+            k_ploc_nn<<<g, 256, 0, st>>>(cbox, nc, plocRadius, nn);
+            k_ploc_flags<<<g, 256, 0, st>>>(nn, nc, create, keep);
+            cub::DeviceScan::ExclusiveSum(tmp, scanBytes, create, createIdx, ncH, st);
+            cub::DeviceScan::ExclusiveSum(tmp, scanBytes, keep, newPos, ncH, st);
+            k_ploc_compact<<<g, 256, 0, st>>>(clus, cbox, nn, nc, create, createIdx, keep, newPos, base, clus2, cbox2, childC, ibox);
+            int h4[4];
+            cudaMemcpyAsync(&h4[0], createIdx + (ncH - 1), sizeof(int), cudaMemcpyDeviceToHost, st);
+            cudaMemcpyAsync(&h4[1], create + (ncH - 1), sizeof(int), cudaMemcpyDeviceToHost, st);
+            cudaMemcpyAsync(&h4[2], newPos + (ncH - 1), sizeof(int), cudaMemcpyDeviceToHost, st);
+            cudaMemcpyAsync(&h4[3], keep + (ncH - 1), sizeof(int), cudaMemcpyDeviceToHost, st);
+            if (cudaStreamSynchronize(st) != cudaSuccess) return -1;
+            if (h4[0] + h4[1] == 0) return -3;  // no mutual pair: degenerate boxes
+            base += h4[0] + h4[1];
+            ncH = h4[2] + h4[3];
+            cudaMemcpyAsync(nc, &ncH, sizeof(int), cudaMemcpyHostToDevice, st);
+            std::swap(clus, clus2);
+            std::swap(cbox, cbox2);
+        }
+        if (base != n - 1) return -4;
+        k_ploc_renumber<<<grid, 256, 0, st>>>(childC, n, child, parentInner, parentLeaf);
+        cudaMemsetAsync(size, 0, sizeof(int) * n, st);
+        k_ploc_sizes<<<grid, 256, 0, st>>>(child, parentLeaf, parentInner, n, visits, size);
+        cudaMemsetAsync(visits, 0, sizeof(int) * n, st);
+        k_ploc_offsets<<<(2 * n - 1 + 255) / 256, 256, 0, st>>>(child, parentInner, parentLeaf, size, n, range, leafPos);
+        k_ploc_reorder<<<grid, 256, 0, st>>>(child, leafPos, valsB, n, order2);
+        // the leaves' parents in the new order
+        cudaMemsetAsync(parentLeaf, 0xFF, sizeof(int) * n, st);
+        k_ploc_leaf_parents<<<grid, 256, 0, st>>>(child, n, parentLeaf);
+        order = order2;
+    } else {
+        k_karras<<<grid, 256, 0, st>>>(keysB, n, range, child, parentInner, parentLeaf);
+    }
+    k_refit<<<grid, 256, 0, st>>>(tri, order, n, range, child, parentInner, parentLeaf, visits, boxes, cost, collapse);
     k_kept<<<grid, 256, 0, st>>>(parentInner, collapse, n, kept, small + 6);
     size_t scanBytes = 0;
     cub::DeviceScan::ExclusiveSum(nullptr, scanBytes, kept, newIdx, n - 1, st);
@@ -325,8 +542,8 @@ int buildLbvh(const float4* tri, int n, float4* nodesOut, int* orderOut, void* s
     if (cudaStreamSynchronize(st) != cudaSuccess) return -1;
     *hostNodeCount = hs[0] + hs[1];
     *hostMaxDepth = md;
-    k_emit<<<grid, 256, 0, st>>>(tri, valsB, n, range, child, collapse, kept, newIdx, boxes, nodesOut);
-    cudaMemcpyAsync(orderOut, valsB, sizeof(int) * n, cudaMemcpyDeviceToDevice, st);
+    k_emit<<<grid, 256, 0, st>>>(tri, order, n, range, child, collapse, kept, newIdx, boxes, nodesOut);
+    cudaMemcpyAsync(orderOut, order, sizeof(int) * n, cudaMemcpyDeviceToDevice, st);
     return cudaStreamSynchronize(st) == cudaSuccess ? 0 : -1;
 }
 

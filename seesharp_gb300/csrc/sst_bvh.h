@@ -13,8 +13,10 @@ size_t lbvhScratchBytes(int n);
 // n - 1 nodes (4 float4 each) to nodesOut and the leaf order (sorted position -> global triangle)
 // to orderOut.  Returns 0 on success; the node count and the maximum inner-node depth are
 // returned through the host pointers.
+// method 0: the radix tree of the Morton codes (Karras 2012); 1: PLOC clustering (Meister and
+// Bittner 2018) over the same sorted leaves.  Both finish with the SAH refit and leaf collapse.
 int buildLbvh(const float4* tri, int n, float4* nodesOut, int* orderOut, void* scratch, size_t scratchBytes, int* hostNodeCount, int* hostMaxDepth,
-              cudaStream_t st);
+              cudaStream_t st, int method);
 
 // 4-wide BVH collapsed from the binary one (nNodes2 binary inner nodes in the layout above):
 // at most nNodes2 nodes of 8 float4 each are written to nodes4.  Returns 0 on success with the

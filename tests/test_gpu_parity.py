@@ -219,6 +219,13 @@ def triangle_soup(rng, n):
     return sc
 
 
+@pytest.fixture(params=["lbvh", "ploc"])
+def bvh_builder(request, monkeypatch):
+    """Builds the scenes of a test with each GPU BVH builder (SST_BVH is read at Scene.Prepare)."""
+    monkeypatch.setenv("SST_BVH", request.param)
+    return request.param
+
+
 @pytest.fixture(params=[2, 4], ids=["bvh2", "bvh4"])
 def bvh_width(request):
     """Runs a test under each traversal width (the other launch settings at their defaults)."""
@@ -230,7 +237,7 @@ def bvh_width(request):
 
 
 @pytest.mark.parametrize("seed,ntri", [(1, 300), (2, 3000)])
-def test_intersection_against_fp64(seed, ntri, bvh_width):
+def test_intersection_against_fp64(seed, ntri, bvh_width, bvh_builder):
     """Closest hit: primitive id exact and t to a relative 1e-5 on non-degenerate rays, against an
     FP64 brute-force watertight intersector."""
     rng = np.random.default_rng(seed)
@@ -368,7 +375,7 @@ def test_relmse_ratio_sphere_field_1m_triangles():
     assert er > 0 and 1 / 1.05 <= ratio <= 1.05, ratio
 
 
-def test_sphere_field_paths_match(bvh_width):
+def test_sphere_field_paths_match(bvh_width, bvh_builder):
     sc = workloads.sphere_field(12, 80, 80, level=3)
     sc.Prepare()
     g, st = render_gpu(sc, 1, 8)
@@ -558,7 +565,7 @@ def test_camera_views_in_a_batch_equal_scenes_with_those_cameras():
         assert np.array_equal(f, s1)
 
 
-def test_single_triangle_scene_and_empty_queries(bvh_width):
+def test_single_triangle_scene_and_empty_queries(bvh_width, bvh_builder):
     """Edge cases of the BVH builders and the query entry points: a one-triangle scene (the
     single-leaf tree), an empty ray batch, and rays with tmax <= tmin (always a miss)."""
     sc = Scene()
