@@ -36,6 +36,7 @@ CONFIGS = {
     5: dict(name="reference_scene_CornellBox.json_512x512_512spp_depth5", builder="scenefile", path="CornellBox/CornellBox.json", W=512, H=512,
             spp=512, depth=5, seed=571298512, recorded="CornellBox/References/MaxDepth5-Width512-Height512.json"),
 }
+CONFIGS[6] = dict(name="light_paths_sphere_field_1Mtri_262144paths_depth8", builder="lightpaths", spheres=200, W=1024, H=1024, paths=262144, depth=8)
 SCENE_DIR = os.path.join(ROOT, "tests", "golden", "scenes")
 
 
@@ -222,6 +223,43 @@ def run_large(args, cfg):
             "e2e": {"value": round(samples / wall / 1e6, 3), "unit": "Msamples/s (forward samples per forward+loss+backward second)",
                     "h2d_bytes_per_step": int(len(views) * W * H * 12), "d2h_bytes_per_step": int(len(views) * W * H * 12 + 4 * (tex0.size + len(mats)))},
             "setup_s": {"generate": round(gen_s, 2), "prepare": round(prep_s, 2), "autotune": round(tune_s, 2)}, "tuning": tuning,
+            "clocks": clk.summary()}
+    print(json.dumps(line), flush=True)
+
+
+def run_lightpaths(args, cfg):
+    """Light-path tracing for the bidirectional integrators (LightPathCache.TraceAllPaths) on the
+    1M-triangle scene: Mpaths/s on the device (CUDA events), end to end with the vertices read
+    back to the host, and the oracle's single-threaded restatement on a sample of the paths."""
+    from oracle import pyoracle as O
+    from seesharp_gb300 import workloads
+    sc = workloads.sphere_field(cfg["spheres"], cfg["W"], cfg["H"])
+    sc.Prepare()
+    n, depth = cfg["paths"], cfg["depth"]
+    for k in range(args.warmup):
+        sc.native.trace_light_paths(99, k, n, depth)
+    ms, verts = [], 0
+    with ClockSampler(0) as clk:
+        t0 = time.perf_counter()
+        for k in range(args.steps):
+            _, _, lengths, st = sc.native.trace_light_paths(1234, k, n, depth)
+            ms.append(st.renderTimeMs)
+            verts += int(lengths.sum())
+        wall = (time.perf_counter() - t0) / args.steps
+    dev_ms = float(np.mean(ms))
+    o = O.OracleScene.from_scene(sc)
+    m = 4096
+    t0 = time.perf_counter()
+    o.light_paths(1234, 0, depth, m)
+    cpu = m / (time.perf_counter() - t0) / 1e6
+    stride_bytes = (depth + 1) * 88
+    line = {"metric": "Mpaths/s light-path tracing (LightPathCache.TraceAllPaths)", "value": round(n / dev_ms / 1e3, 3), "unit": "Mpaths/s",
+            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(dev_ms, 3), "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scene generator)",
+            "config": {"workload": cfg["name"], "paths": n, "max_depth": depth, "vertices_per_step": verts // max(args.steps, 1)},
+            "e2e": {"value": round(n / wall / 1e6, 3), "unit": "Mpaths/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": n * (stride_bytes + 4)},
+            "cpu_baseline": {"value": round(cpu, 5), "unit": "Mpaths/s", "cores": 1, "kind": "port",
+                             "sample": f"{m} paths of the same job, oracle restatement, one thread"},
             "clocks": clk.summary()}
     print(json.dumps(line), flush=True)
 
@@ -564,9 +602,9 @@ def main():
             cfg[k] = a
             cfg["name"] = cfg["name"] + f"_{k}{a}"
     os.environ.setdefault("SST_BVH", "ploc")
-    if args.impl == "reference" and cfg["builder"] in ("adjoint", "large"):
+    if args.impl == "reference" and cfg["builder"] in ("adjoint", "large", "lightpaths"):
         if dist_info()[1] == 0:
-            print(json.dumps({"impl": "reference", "unavailable": "the reference PathTracer has no adjoint (differentiation is new in this library)"}))
+            print(json.dumps({"impl": "reference", "unavailable": "this workload has no counterpart in the reference PathTracer's CPU path"}))
     elif args.impl == "reference":
         run_reference(args, cfg)
     elif cfg["builder"] == "batch":
@@ -575,6 +613,8 @@ def main():
         run_adjoint(args, cfg)
     elif cfg["builder"] == "large":
         run_large(args, cfg)
+    elif cfg["builder"] == "lightpaths":
+        run_lightpaths(args, cfg)
     else:
         run_ours(args, cfg)
 

@@ -224,6 +224,31 @@ typedef struct SstCamera {
     int32_t reserved;
 } SstCamera;
 
+/* ---- light paths: no counterpart in the reference's PathTracer -----------------------------------
+ * LightPathCache.TraceAllPaths (Integrators/Bidir/LightPathCache.cs:126-260) for the bidirectional
+ * integrators: numPaths random walks from the emitters and the background with the LightPathWalk
+ * vertices (Integrators/Common/PathVertex.cs), path i seeded RNG(seed, i, iteration).  The next-
+ * event pdf callback is not evaluated (pdfNextEventAncestor = 0). */
+typedef struct SstPathVertex {
+    float position[3];
+    float normal[3];           /* face normal; 0 for the first vertex of a background path */
+    float shadingNormal[3];
+    float pdfFromAncestor;     /* surface-area pdf of this vertex from its ancestor */
+    float pdfReverseAncestor;  /* surface-area pdf of the ancestor's ancestor from the ancestor */
+    float pdfNextEventAncestor;
+    float weight[3];           /* Monte Carlo weight of the subpath up to this vertex */
+    float maximumRoughness;
+    int32_t meshId;            /* -1 for the first vertex of a background path */
+    int32_t primId;
+    int32_t depth;             /* edges along the path */
+    int32_t pathId;
+    int32_t fromBackground;
+    int32_t reserved;
+} SstPathVertex;
+/* vertices: numPaths * (maxDepth + 1) entries, path i at i * (maxDepth + 1); lengths: numPaths. */
+int sst_trace_light_paths(sst_scene* scene, uint32_t seed, uint32_t iteration, int32_t numPaths, int32_t maxDepth, SstPathVertex* vertices,
+                          int32_t* lengths, int32_t memory, SstRenderStats* stats);
+
 /* ---- frame-buffer layers ------------------------------------------------------------------------
  * Computed on the device while the film is folded:
  *  - the VarianceLayer (FrameBuffer.Flags.EstimatePixelVariance, Images/VarianceLayer.cs:10-84);

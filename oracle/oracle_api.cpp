@@ -354,6 +354,38 @@ int ora_material_sample(void* p, int mat, const float* pt, const float* outDir, 
 // outputs (double): gTex (all textures' texels concatenated), gMatBase (3 per material),
 // gMatRough (1 per material), gEmitter (3 per emitter).  Each path's total radiance comes from an
 // FP64 render of the same path; non-finite paths are skipped as the frame buffer skips them.
+// Light paths of LightPathCache.TraceAllPaths for paths [0, n): per vertex 16 floats
+// (position 3, normal 3, shading normal 3, pdfFromAncestor, pdfReverseAncestor, weight 3,
+// maxRoughness, fromBackground) and 4 ints (mesh, prim, depth, pathId); stride = maxDepth + 1
+// vertices per path; lengths[n].
+int ora_light_paths(void* p, uint32_t seed, uint32_t iter, int maxDepth, int n, float* vf, int* vi, int* lengths) {
+    Handle* H = static_cast<Handle*>(p);
+    const int stride = maxDepth + 1;
+    auto emit = [&](auto& sc) {
+        using T = decltype(sc.emitters[0].invArea);
+        V3<T> c; T r;
+        SceneBounds(sc, c, r);
+        LightPathParams<T> P{seed, iter, maxDepth};
+        for (int i = 0; i < n; ++i) {
+            std::vector<LightVertex<T>> path = TraceLightPath(sc, P, i, c, r);
+            lengths[i] = int(path.size());
+            for (int k = 0; k < int(path.size()) && k < stride; ++k) {
+                const LightVertex<T>& v = path[k];
+                float* f = vf + 16 * (size_t(i) * stride + k);
+                int* q = vi + 4 * (size_t(i) * stride + k);
+                const V3<T>* vs[3] = {&v.point.position, &v.point.normal, &v.point.shadingNormal};
+                for (int a = 0; a < 3; ++a) { f[3 * a] = float(vs[a]->x); f[3 * a + 1] = float(vs[a]->y); f[3 * a + 2] = float(vs[a]->z); }
+                f[9] = float(v.pdfFromAncestor); f[10] = float(v.pdfReverseAncestor);
+                f[11] = float(v.weight.r); f[12] = float(v.weight.g); f[13] = float(v.weight.b);
+                f[14] = float(v.maxRoughness); f[15] = v.fromBackground ? 1.0f : 0.0f;
+                q[0] = v.point.mesh; q[1] = v.point.prim; q[2] = v.depth; q[3] = v.pathId;
+            }
+        }
+    };
+    if (H->fp64) emit(H->s64); else emit(H->s32);
+    return 0;
+}
+
 int ora_adjoint(void* p, const PTParams* P, const float* dLdI, double* gTex, double* gMatBase, double* gMatRough, double* gEmitter, int nthreads) {
     Handle* H = static_cast<Handle*>(p);
     if (!H->fp64) return -1;

@@ -587,7 +587,8 @@ template <class T> struct Scene {
 template <class T> struct ShadingContext {
     SurfacePoint<T> point;
     V3<T> normal, tangent, binormal, outDir, outDirWorld;
-    ShadingContext(const SurfacePoint<T>& p, V3<T> outW) : point(p) {
+    bool onLight = false;  // ShadingContext.IsOnLightSubpath
+    ShadingContext(const SurfacePoint<T>& p, V3<T> outW, bool onLightSubpath = false) : point(p), onLight(onLightSubpath) {
         normal = p.shadingNormal;
         ComputeBasisVectors(normal, tangent, binormal);
         outDir = WorldToShading(normal, tangent, binormal, outW);
@@ -686,7 +687,7 @@ template <class T> struct MaterialEval {
             T sqrtDenom = cOut + eta * cIn;
             if (!SameHemisphere(o, inDir) && cOut * cIn < T(0)) {
                 Rgb<T> F(FresnelDielectric(cOut, T(1), mat.ior));
-                T factor = T(1);  // the camera subpath is never on a light subpath
+                T factor = c.onLight ? T(1) / eta : T(1);  // GenericMaterial.cs:255
                 V3<T> wh = (!SameHemisphere(o, ht)) ? -ht : ht;
                 T num = ndf.D(wh) * ndf.G(o, inDir);
                 num *= eta * eta * std::max(T(0), dot(inDir, -wh)) * std::max(T(0), dot(o, wh));
@@ -1177,6 +1178,193 @@ template <class T> void AdjointPixel(const Scene<T>& sc, const PTParams& P, uint
         prevPdf = bs.Pdf * surv;
     }
     applyPending();
+}
+
+// ---------------------------------------------------------------------------------------------
+// Light paths: LightPathCache.TraceAllPaths / TraceLightPath (Integrators/Bidir/LightPathCache.cs:
+// 126-260) with the LightPathWalk modifier (:271-341) over RandomWalk (Integrators/Common/
+// RandomWalk.cs:76-216).  No next-event pdf callback (PdfNextEventAncestor stays 0).
+// ---------------------------------------------------------------------------------------------
+template <class T> struct LightVertex {
+    SurfacePoint<T> point;
+    T pdfFromAncestor = 0, pdfReverseAncestor = 0, pdfNextEventAncestor = 0;
+    Rgb<T> weight;
+    int pathId = 0, depth = 0;
+    T maxRoughness = 0;
+    bool fromBackground = false;
+};
+
+// Scene.Prepare (Scene.cs:115-136): center = mean of all vertices, radius = distance to the
+// furthest vertex
+template <class T> void SceneBounds(const Scene<T>& sc, V3<T>& center, T& radius) {
+    V3<T> c(0, 0, 0);
+    double n = 0;
+    for (const auto& m : sc.meshes)
+        for (size_t v = 0; v < m.V.size(); ++v) { c = c + m.V[v]; n += 1; }
+    center = c / T(n);
+    T r = 0;
+    for (const auto& m : sc.meshes)
+        for (size_t v = 0; v < m.V.size(); ++v) r = std::max(r, lengthSq(m.V[v] - center));
+    radius = std::sqrt(r);
+}
+
+template <class T> struct EmitterRaySample { SurfacePoint<T> point; V3<T> dir; T pdf = 0; Rgb<T> weight; };
+
+// DiffuseEmitter.SampleRay (DiffuseEmitter.cs:44-64), GlossyEmitter.SampleRay (GlossyEmitter.cs:47-71)
+template <class T> EmitterRaySample<T> EmitterSampleRay(const Scene<T>& sc, const Emitter<T>& e, V2<T> primaryPos, V2<T> primaryDir) {
+    EmitterRaySample<T> r;
+    r.point = SampleEmitterArea(sc, e, primaryPos);
+    T posPdf = e.invArea;
+    V3<T> n = r.point.shadingNormal, t, b;
+    ComputeBasisVectors(n, t, b);
+    if (!e.glossy()) {
+        DirectionSample<T> local = ToCosHemisphere(primaryDir);
+        r.dir = n * local.Direction.z + t * local.Direction.x + b * local.Direction.y;
+        r.pdf = local.Pdf * posPdf;
+        r.weight = e.radiance / posPdf * PI<T>();
+    } else {
+        DirectionSample<T> local = ToCosineLobe(e.exponent + T(1), primaryDir);
+        r.dir = n * local.Direction.z + t * local.Direction.x + b * local.Direction.y;
+        T cosine = local.Direction.z;
+        Rgb<T> w = e.radiance * std::pow(cosine, e.exponent + T(1)) * e.normalization;
+        r.pdf = local.Pdf * posPdf;
+        r.weight = w / posPdf / local.Pdf;
+    }
+    return r;
+}
+
+template <class T> struct LightPathParams { uint32_t seed, iter; int maxDepth; };
+
+// GetRoughness (DiffuseMaterial.cs:31, GenericMaterial.cs:64)
+template <class T> T MaterialRoughness(const Scene<T>& sc, const SurfacePoint<T>& p) {
+    const Material<T>& m = sc.materials[sc.meshes[p.mesh].material];
+    return m.type == MAT_GENERIC ? sc.TexLookupMono(m.roughness, p.uv) : T(1);
+}
+
+template <class T> std::vector<LightVertex<T>> TraceLightPath(const Scene<T>& sc, const LightPathParams<T>& P, int idx, V3<T> center, T radius) {
+    std::vector<LightVertex<T>> out;
+    Rng rng(P.seed, uint32_t(idx), P.iter);
+    const int nEm = int(sc.emitters.size());
+    // SelectLight (:33-40)
+    T bgProb = sc.env ? T(1) / (T(1) + T(nEm)) : T(0);
+    bool background = false;
+    const Emitter<T>* em = nullptr;
+    T prob;
+    if (bgProb > T(0) && T(rng.NextFloat()) <= bgProb) {
+        background = true;
+        prob = bgProb;
+    } else {
+        em = &sc.emitters[rng.NextInt(uint32_t(nEm))];
+        prob = (T(1) - bgProb) / T(nEm);
+    }
+    Rgb<T> approx = Rgb<T>::White();
+    T nextReversePdf = 0, maxRough = 0;
+    Ray<T> ray;
+    SurfacePoint<T> prev;
+    T pdfDirection;
+    Rgb<T> prefix;
+    int depth;
+    auto survival = [&](int d) { return d > 4 ? std::clamp(approx.Average(), T(0.05f), T(0.95f)) : T(1); };
+    auto addVertex = [&](const SurfacePoint<T>& p, T pdfFrom, const Rgb<T>& w, int d) {
+        LightVertex<T> v;
+        v.point = p;
+        v.pdfFromAncestor = pdfFrom;
+        v.pdfReverseAncestor = nextReversePdf;
+        v.pathId = idx;
+        v.weight = w;
+        v.depth = d;
+        // LightPathWalk.OnHit takes the maximum with Payload.maxRoughness, which stays 0 (:323-337)
+        v.maxRoughness = std::max(MaterialRoughness(sc, p), maxRough);
+        v.fromBackground = background;
+        out.push_back(v);
+    };
+    if (!background) {
+        // TraceEmitterPath (:211-224)
+        V2<float> pp = rng.NextFloat2D(), pd = rng.NextFloat2D();
+        EmitterRaySample<T> es = EmitterSampleRay(sc, *em, V2<T>(T(pp.x), T(pp.y)), V2<T>(T(pd.x), T(pd.y)));
+        es.pdf *= prob;
+        if (es.pdf == T(0) || es.weight.IsBlack()) return out;
+        LightVertex<T> v0;
+        v0.point = es.point;
+        v0.pathId = idx;
+        out.push_back(v0);  // OnStartEmitter (:295-306)
+        ray = Scene<T>::SpawnRay(es.point, es.dir);
+        prev = es.point;
+        pdfDirection = es.pdf;
+        prefix = es.weight / prob;
+        depth = 1;
+    } else {
+        // TraceBackgroundPath (:226-241), EnvironmentMap.SampleRay (EnvironmentMap.cs:87-111)
+        V2<float> pp = rng.NextFloat2D(), pd = rng.NextFloat2D();
+        BackgroundSample<T> ds = sc.env->SampleDirection(V2<T>(T(pd.x), T(pd.y)));
+        V2<T> disc = ToConcentricDisc(V2<T>(T(pp.x), T(pp.y)));
+        V3<T> t, b;
+        ComputeBasisVectors(ds.Direction, t, b);
+        V3<T> pos = center + (ds.Direction + t * disc.x + b * disc.y) * radius;
+        T posPdf = (T(1) / PI<T>()) / (radius * radius);
+        Rgb<T> weight = ds.Weight / posPdf;
+        T pdf = posPdf * ds.Pdf;
+        pdf *= prob;
+        weight = weight / prob;
+        if (pdf == T(0) || weight.IsBlack()) return out;
+        LightVertex<T> v0;
+        v0.point.position = pos;
+        v0.pathId = idx;
+        v0.fromBackground = true;
+        out.push_back(v0);  // OnStartBackground (:308-319)
+        // StartFromBackground (RandomWalk.cs:86-124)
+        Ray<T> r0;
+        r0.org = pos;
+        r0.dir = -ds.Direction;
+        r0.tmin = 0;
+        SurfacePoint<T> hit = sc.Trace(r0);
+        if (!hit.valid) return out;
+        ShadingContext<T> ctx(hit, -r0.dir, true);
+        MaterialEval<T> me{sc, sc.materials[sc.meshes[hit.mesh].material]};
+        // SampleBsdf (RandomWalk.cs:126-135): Sample(rng.NextFloat(), rng.NextFloat2D())
+        float uc = rng.NextFloat();
+        V2<float> up = rng.NextFloat2D();
+        BsdfSample<T> bs = me.Sample(ctx, T(uc), V2<T>(T(up.x), T(up.y)));
+        approx = approx * bs.Weight;
+        addVertex(hit, pdf, weight, 1);
+        nextReversePdf = bs.PdfReverse;
+        if (P.maxDepth <= 1) return out;
+        if (bs.Pdf == T(0) || bs.Weight.IsBlack()) return out;
+        ray = Scene<T>::SpawnRay(hit, bs.Direction);
+        prev = hit;
+        pdfDirection = bs.Pdf;
+        prefix = weight * bs.Weight;
+        depth = 2;
+    }
+    // ContinueWalk (RandomWalk.cs:145-216)
+    while (depth < P.maxDepth) {
+        SurfacePoint<T> hit = sc.Trace(ray);
+        if (!hit.valid) break;
+        ShadingContext<T> ctx(hit, -ray.dir, true);
+        T pdfFromAncestor = pdfDirection * SurfaceAreaToSolidAngle(prev, hit);
+        if (pdfFromAncestor == T(0)) break;
+        addVertex(hit, pdfFromAncestor, prefix, depth);
+        if (depth + 1 >= P.maxDepth) break;
+        T surv = survival(depth);
+        if (T(rng.NextFloat()) > surv) break;
+        MaterialEval<T> me{sc, sc.materials[sc.meshes[hit.mesh].material]};
+        float uc = rng.NextFloat();
+        V2<float> up = rng.NextFloat2D();
+        BsdfSample<T> bs = me.Sample(ctx, T(uc), V2<T>(T(up.x), T(up.y)));
+        approx = approx * (bs.Weight / surv);
+        T pdfToAncestor = bs.PdfReverse * SurfaceAreaToSolidAngle(hit, prev);
+        nextReversePdf = pdfToAncestor;  // OnContinue
+        if (bs.Pdf == T(0) || bs.Weight.IsBlack()) break;
+        Rgb<T> w = bs.Weight;
+        w = w * (std::fabs(dot(hit.normal, bs.Direction)) / std::fabs(dot(hit.shadingNormal, bs.Direction)));
+        w = w * (std::fabs(dot(hit.shadingNormal, -ray.dir)) / std::fabs(dot(hit.normal, -ray.dir)));
+        prefix = prefix * (w / surv);
+        ++depth;
+        pdfDirection = bs.Pdf;
+        prev = hit;
+        ray = Scene<T>::SpawnRay(hit, bs.Direction);
+    }
+    return out;
 }
 
 }  // namespace ora

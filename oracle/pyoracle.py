@@ -74,6 +74,7 @@ def lib():
         L.ora_emitter_radiance.argtypes = [vp, i, vp, vp, vp]
         L.ora_query_emitter.argtypes = [vp, i, i]
         L.ora_adjoint.argtypes = [vp, ctypes.POINTER(PTParams), vp, vp, vp, vp, vp, i]
+        L.ora_light_paths.argtypes = [vp, u32, u32, i, i, vp, vp, vp]
         _lib = L
     return _lib
 
@@ -282,6 +283,16 @@ class OracleScene:
         out["materialRoughness"] = out["materialRoughness"][:n_mat]
         out["emitterRadiance"] = out["emitterRadiance"][:3 * n_em].reshape(-1, 3)
         return out
+
+    def light_paths(self, seed, iteration, max_depth, n):
+        """LightPathCache.TraceAllPaths for paths [0, n): (floats (n, maxDepth+1, 16), ints
+        (n, maxDepth+1, 4), lengths (n,)) in the layout of sst_trace_light_paths."""
+        stride = max_depth + 1
+        vf = np.zeros((n, stride, 16), np.float32)
+        vi = np.full((n, stride, 4), -1, np.int32)
+        lengths = np.zeros(n, np.int32)
+        self.L.ora_light_paths(self.h, seed & 0xFFFFFFFF, iteration & 0xFFFFFFFF, int(max_depth), int(n), _p(vf), _p(vi), _p(lengths))
+        return vf, vi, lengths
 
     def num_emitters(self):
         return int(self.L.ora_num_emitters(self.h))

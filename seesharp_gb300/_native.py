@@ -124,6 +124,7 @@ SIGNATURES = {
     "sst_render_batch": [_vp, _P(SstRenderJob), _i32, _P(SstRenderStats)],
     "sst_scene_update_texture": [_vp, _i32, _vp],
     "sst_forward_batch": [_vp, _vp, _i32, _P(SstRenderStats)],
+    "sst_trace_light_paths": [_vp, ctypes.c_uint32, ctypes.c_uint32, _i32, _i32, _vp, _vp, _i32, _P(SstRenderStats)],
     "sst_render_layers": [_vp, _P(SstPathTracerParams), _vp, _i32, _P(SstFilmLayers), _P(SstRenderStats)],
     "sst_backward_batch": [_vp, _vp, _i32, _vp, _i32, _vp, _P(SstRenderStats)],
     "sst_forward": [_vp, _P(SstPathTracerParams), _vp, _i32, _P(SstRenderStats)],
@@ -403,6 +404,17 @@ class SceneHandle:
         stats = SstRenderStats()
         check(self.lib.sst_render_layers(self.handle, ctypes.byref(params), ctypes.c_void_p(film), SST_MEM_HOST, ctypes.byref(L), ctypes.byref(stats)))
         return stats, var, None if avg is None else float(avg[0]), err
+
+    def trace_light_paths(self, seed, iteration, num_paths, max_depth):
+        """sst_trace_light_paths: (floats (n, maxDepth+1, 16), ints (n, maxDepth+1, 6), lengths (n,),
+        stats) in the layout of SstPathVertex."""
+        stride = max_depth + 1
+        raw = np.zeros((num_paths, stride, 22), np.float32)
+        lengths = np.zeros(num_paths, np.int32)
+        stats = SstRenderStats()
+        check(self.lib.sst_trace_light_paths(self.handle, seed & 0xFFFFFFFF, iteration & 0xFFFFFFFF, int(num_paths), int(max_depth), ptr(raw),
+                                              ptr(lengths), SST_MEM_HOST, ctypes.byref(stats)))
+        return raw[..., :16].copy(), raw[..., 16:].copy().view(np.int32), lengths, stats
 
     def update_texture(self, tex_id, data):
         d = np.ascontiguousarray(data, np.float32)

@@ -114,6 +114,8 @@ struct sst_ctx {
     DevBuf scratchIn, scratchOut, scratchOut2;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     int* pinnedCount = nullptr;
+    // light paths (sst_trace_light_paths)
+    DevBuf lightA[9], lightB[9], lightHits, lightVerts, lightLengths, lightCnt;
     // frame-buffer layers (sst_render_layers)
     DevBuf layMean, layRef, layErr, layVar, laySum, layAlb, layNrm, aovSamples;
     // batched adjoint: the jobs of the last sst_forward_batch, their path radiance, dLoss/dImage
@@ -602,6 +604,8 @@ static void commitScene(sst_scene* s, int W, int H) {
         d.rad = make_float4(he.rad[0], he.rad[1], he.rad[2], he.exponent);
         d.norm = (he.exponent + 1.0f) / (2.0f * 3.14159265f);  // GlossyEmitter.cs:14
         d.globalTri = s->meshTriOffset[he.mesh] + f;
+        d.mesh = he.mesh;
+        d.face = f;
     }
     // textures
     std::vector<DevTexture> texs;
@@ -636,6 +640,26 @@ static void commitScene(sst_scene* s, int W, int H) {
     d.nNodes = s->nNodes;
     d.nodes4 = s->nNodes4 > 0 ? s->nodes4.as<float4>() : nullptr;
     d.nNodes4 = s->nNodes4;
+    {
+        // Scene.Prepare (Scene.cs:115-136): the mean of all vertices and the distance to the
+        // furthest one, summed in single precision in mesh and vertex order
+        float cx = 0.f, cy = 0.f, cz = 0.f;
+        unsigned long long total = 0;
+        for (auto& m : s->meshes) {
+            for (size_t v = 0; v + 2 < m.V.size(); v += 3) { cx += m.V[v]; cy += m.V[v + 1]; cz += m.V[v + 2]; }
+            total += m.V.size() / 3;
+        }
+        float tf = float(std::max<unsigned long long>(total, 1));
+        cx /= tf; cy /= tf; cz /= tf;
+        float r2 = 0.f;
+        for (auto& m : s->meshes)
+            for (size_t v = 0; v + 2 < m.V.size(); v += 3) {
+                float dx = m.V[v] - cx, dy = m.V[v + 1] - cy, dz = m.V[v + 2] - cz;
+                r2 = std::max(dx * dx + dy * dy + dz * dz, r2);
+            }
+        d.sceneCenter = make_float3(cx, cy, cz);
+        d.sceneRadius = std::sqrt(r2);
+    }
     // environment map (EnvironmentMap.cs:139-156)
     d.hasEnv = s->envW > 0;
     if (d.hasEnv) {
@@ -1644,6 +1668,88 @@ int sst_render_layers(sst_scene* s, const SstPathTracerParams* p, float* film, i
         }
         if (memory != SST_MEM_DEVICE) CUDA_CHECK(cudaMemcpyAsync(film, dFilm, P * 12, cudaMemcpyDeviceToHost, st));
         CUDA_CHECK(cudaStreamSynchronize(st));
+        if (stats) *stats = local;
+    });
+}
+
+static LightPathBuf bindLight(DevBuf* b, size_t cap) {
+    const size_t sz[9] = {4, 4, 4, 16, 16, 16, 16, 16, 16};
+    for (int k = 0; k < 9; ++k) b[k].ensure(cap * sz[k]);
+    LightPathBuf l;
+    l.path = b[0].as<uint32_t>();
+    l.rng = b[1].as<uint32_t>();
+    l.depth = b[2].as<uint32_t>();
+    l.prefix = b[3].as<float4>();
+    l.approx = b[4].as<float4>();
+    l.prevP = b[5].as<float4>();
+    l.prevN = b[6].as<float4>();
+    l.ro = b[7].as<float4>();
+    l.rd = b[8].as<float4>();
+    return l;
+}
+
+int sst_trace_light_paths(sst_scene* s, uint32_t seed, uint32_t iteration, int32_t numPaths, int32_t maxDepth, SstPathVertex* vertices,
+                          int32_t* lengths, int32_t memory, SstRenderStats* stats) {
+    static_assert(sizeof(SstPathVertex) == sizeof(SstPathVertexDev), "path vertex layout");
+    return guarded([&] {
+        if (!s || numPaths < 0 || numPaths > (1 << 24) || maxDepth < 1 || maxDepth > kMaxPathDepth || (numPaths > 0 && (!vertices || !lengths)))
+            fail(SST_ERR_INVALID_ARGUMENT, "invalid light-path query");
+        if (!s->committed) fail(SST_ERR_NOT_COMMITTED, "scene is not committed");
+        SstRenderStats local = emptyStats();
+        if (numPaths == 0) { if (stats) *stats = local; return; }
+        sst_ctx* c = s->ctx;
+        cudaStream_t st = c->stream;
+        CUDA_CHECK(cudaSetDevice(c->device));
+        const size_t n = size_t(numPaths), stride = size_t(maxDepth) + 1;
+        LightPathBuf A = bindLight(c->lightA, n), B = bindLight(c->lightB, n);
+        c->lightHits.ensure(n * 16);
+        SstPathVertexDev* dv = reinterpret_cast<SstPathVertexDev*>(vertices);
+        int* dl = lengths;
+        if (memory != SST_MEM_DEVICE) {
+            c->lightVerts.ensure(n * stride * sizeof(SstPathVertexDev));
+            c->lightLengths.ensure(n * 4);
+            dv = c->lightVerts.as<SstPathVertexDev>();
+            dl = c->lightLengths.as<int>();
+        }
+        CUDA_CHECK(cudaMemsetAsync(dv, 0, n * stride * sizeof(SstPathVertexDev), st));
+        c->lightCnt.ensure(sizeof(int) * 2 * (size_t(maxDepth) + 3));
+        int* cnt = c->lightCnt.as<int>();
+        CUDA_CHECK(cudaMemsetAsync(cnt, 0, sizeof(int) * 2 * (size_t(maxDepth) + 3), st));
+        c->stats.ensure(sizeof(DevStats));
+        CUDA_CHECK(cudaMemsetAsync(c->stats.p, 0, sizeof(DevStats), st));
+        const DevJob* job = jobTable(s);
+        LightParams P{numPaths, maxDepth, seed, iteration};
+        CUDA_CHECK(cudaEventRecord(c->ev0, st));
+        launch_light_start(job, P, A, cnt, dv, dl, st);
+        CUDA_CHECK(cudaGetLastError());
+        int items = 0;
+        CUDA_CHECK(cudaMemcpyAsync(&items, cnt, sizeof(int), cudaMemcpyDeviceToHost, st));
+        CUDA_CHECK(cudaStreamSynchronize(st));
+        // each step: closest hit, then one walk step (a path reaches at most maxDepth + 1 hits)
+        for (int d = 0; d <= maxDepth && items > 0; ++d) {
+            int* qIn = cnt + d;
+            int* qOut = cnt + d + 1;
+            int* work = cnt + (maxDepth + 2) + d;
+            launch_trace_closest(c->trace, job, nullptr, A.ro, A.rd, qIn, work, c->lightHits.as<float4>(), c->stats.as<DevStats>(), st);
+            launch_light_walk(job, P, A, B, c->lightHits.as<float4>(), qIn, qOut, dv, dl, items, st);
+            CUDA_CHECK(cudaGetLastError());
+            std::swap(A, B);
+            CUDA_CHECK(cudaMemcpyAsync(&items, qOut, sizeof(int), cudaMemcpyDeviceToHost, st));
+            CUDA_CHECK(cudaStreamSynchronize(st));
+        }
+        CUDA_CHECK(cudaEventRecord(c->ev1, st));
+        if (memory != SST_MEM_DEVICE) {
+            CUDA_CHECK(cudaMemcpyAsync(vertices, dv, n * stride * sizeof(SstPathVertexDev), cudaMemcpyDeviceToHost, st));
+            CUDA_CHECK(cudaMemcpyAsync(lengths, dl, n * 4, cudaMemcpyDeviceToHost, st));
+        }
+        DevStats hs;
+        CUDA_CHECK(cudaMemcpyAsync(&hs, c->stats.p, sizeof(DevStats), cudaMemcpyDeviceToHost, st));
+        CUDA_CHECK(cudaStreamSynchronize(st));
+        if (hs.errorFlags & 1) fail(SST_ERR_DEVICE_LIMIT, "BVH traversal stack overflow");
+        float ms = 0.f;
+        CUDA_CHECK(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
+        local.renderTimeMs = ms;
+        local.numRays = hs.rays;
         if (stats) *stats = local;
     });
 }

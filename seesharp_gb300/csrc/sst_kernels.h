@@ -9,6 +9,10 @@ namespace sst {
 void launch_env_build(const float4* img, int w, int h, float* colCdf, float* rowMarg, int* hasCol, float* rowCdf, cudaStream_t s);
 void launch_camera(const DevJob* jobs, const WaveChunk* chunks, const WaveDesc* waves, const int* curWave, const PathBuf& A, int* qCount,
                    int maxItems, cudaStream_t s);
+void launch_light_start(const DevJob* jobs, const LightParams& P, const LightPathBuf& A, int* qCount, SstPathVertexDev* verts, int* lengths,
+                        cudaStream_t s);
+void launch_light_walk(const DevJob* jobs, const LightParams& P, const LightPathBuf& A, const LightPathBuf& B, const float4* hits, const int* nIn,
+                       int* nOut, SstPathVertexDev* verts, int* lengths, int maxItems, cudaStream_t s);
 void launch_variance_finish(const float* mean, const float* moment, int W, int H, float* out, double* sum, cudaStream_t s);
 void launch_film_fold(const DevJob* jobs, const WaveChunk* chunks, const WaveDesc* waves, int* curWave, const float* samples, DevStats* st,
                       int maxFold, int advance, cudaStream_t s);

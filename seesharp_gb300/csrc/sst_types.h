@@ -44,7 +44,7 @@ struct DevEmitter {
     float4 rad;          // radiance rgb, w = glossy exponent (< 0: diffuse)
     float norm;          // (exponent + 1) / (2 pi)
     int globalTri;
-    int pad[2];
+    int mesh, face;      // the emitter's mesh and face
 };
 
 struct DevEnv {
@@ -79,6 +79,8 @@ struct DevScene {
     int nNodes;
     int nNodes4;
     int hasEnv;
+    float3 sceneCenter;  // Scene.Center / Scene.Radius (Scene.cs:115-136)
+    float sceneRadius;
     DevEnv env;
     DevCamera cam;
 };
@@ -101,6 +103,27 @@ struct DevAdj {
     float* gMatBase;      // 3 per material: constant base colour
     float* gMatRough;     // 1 per material: constant roughness
     float* gEmitter;      // 3 per emitter: radiance
+};
+
+// Light paths (sst_light.cu)
+struct LightParams {
+    int numPaths, maxDepth;
+    uint32_t seed, iter;
+};
+struct LightPathBuf {  // structure of arrays of the light paths in flight
+    uint32_t* path;    // path index
+    uint32_t* rng;     // RNG state
+    uint32_t* depth;   // depth | flags
+    float4* prefix;    // prefix weight, w = pdf of the last sampled direction
+    float4* approx;    // approximate throughput, w = reverse pdf for the next vertex
+    float4* prevP;     // previous vertex position
+    float4* prevN;     // previous vertex face normal
+    float4* ro;        // ray origin, w = tmin
+    float4* rd;        // ray direction, w = tmax
+};
+struct SstPathVertexDev {  // the layout of SstPathVertex
+    float p[16];
+    int q[6];
 };
 
 // Frame-buffer layers of a job (all NULL unless requested).
