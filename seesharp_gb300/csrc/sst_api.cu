@@ -846,6 +846,10 @@ static void renderJobs(sst_ctx* c, std::vector<JobIn>& jobs, SstRenderStats* out
         w.wb.b.adjL = c->adjB[0].as<float4>(); w.wb.b.adjD = c->adjB[1].as<float4>(); w.wb.b.adjP = c->adjB[2].as<float4>();
         w.wb.neeG = c->neeG.as<float4>();
     }
+    // any GenericMaterial in the wave's scenes (otherwise the shade kernel without generic code runs)
+    bool generic = false;
+    for (auto& j : jobs)
+        for (auto& m : j.s->materials) generic |= m.type == kGeneric;
     // per-item samples of the denoiser feature layers (written by the first shade, read by the fold)
     bool anyAov = false;
     for (auto& j : jobs) anyAov |= j.lay.aovAlbedo != nullptr;
@@ -898,7 +902,7 @@ static void renderJobs(sst_ctx* c, std::vector<JobIn>& jobs, SstRenderStats* out
             }
             {
                 KTimer kt(c, 2);
-                launch_shade(ns, replay, dj, A, B, w.wb.hits, w.wb.nee, w.wb.neeG, w.wb.cap, w.wb.shRo, w.wb.shRd, w.wb.shTgt, w.wb.shJob,
+                launch_shade(ns, replay, generic, dj, A, B, w.wb.hits, w.wb.nee, w.wb.neeG, w.wb.cap, w.wb.shRo, w.wb.shRd, w.wb.shTgt, w.wb.shJob,
                              cnt + kCntQueue + d, cnt + kCntQueue + d + 1, cnt + kCntShadow + d, c->samples.as<float>(), dstats, maxItems, st);
             }
             {

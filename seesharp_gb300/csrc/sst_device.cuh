@@ -405,8 +405,10 @@ SST_DN float3 diffuseEval(const Ctx& c, float3 base, bool transmitter, float3 in
 }
 
 // Material.EvaluateWithCosine and Material.Pdf for a world direction in one pass.
+// GEN = false compiles the diffuse case only (for waves without GenericMaterials).
+template <bool GEN = true>
 SST_D float3 evalWithCos(const DevScene& sc, const DevMaterial& m, const Lp& lp, float3 diffBase, const Ctx& c, float3 inW, float& pdf) {
-    if (m.type == kGeneric) {
+    if (GEN && m.type == kGeneric) {
         float3 in = c.f.toLocal(inW);
         float3 v = genericEval(c, lp, in, pdf);
         return v * fabsf(in.z);
@@ -416,9 +418,10 @@ SST_D float3 evalWithCos(const DevScene& sc, const DevMaterial& m, const Lp& lp,
 
 // Material.Sample: GenericMaterial.cs:92-150 / DiffuseMaterial.cs:127-164.  Returns false for an
 // invalid sample (pdf 0).
+template <bool GEN = true>
 SST_DN bool sampleMaterial(const DevScene& sc, const DevMaterial& m, const Lp& lp, float3 diffBase, const Ctx& c, float u, float u1, float u2,
                           float3& dirW, float& pdf, float3& weight) {
-    if (m.type == kGeneric) {
+    if (GEN && m.type == kGeneric) {
         if (c.out.z == 0.0f) return false;
         Ggx ndf{lp.ax, lp.ay};
         float eta = c.out.z > 0.0f ? (1.0f / lp.ior) : lp.ior;

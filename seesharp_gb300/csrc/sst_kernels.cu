@@ -295,7 +295,9 @@ SST_D int aggAppend(int* counter) {
 //     which is the forward pass's path radiance minus what has been collected up to vertex k
 //     (applied at the next vertex, after that vertex has resolved vertex k's NEE).
 // Every term is weighted by dLoss/dSample of the path's pixel.
-template <int NS, bool ADJ>
+// GEN = false: a wave without GenericMaterials (the generic code is not compiled in, which keeps
+// the kernel's instruction footprint small).
+template <int NS, bool ADJ, bool GEN>
 __global__ void __launch_bounds__(128, ADJ ? SST_SHADE_ADJ_MIN_BLOCKS : SST_SHADE_MIN_BLOCKS) k_shade(const DevJob* __restrict__ jobs, PathBuf A, PathBuf B,
                                                                    const float4* __restrict__ hits, float4* nee, float4* neeG, int cap,
                                                                    float4* shRo, float4* shRd, int* shTgt, uint32_t* shJob, const int* nIn,
@@ -448,7 +450,7 @@ __global__ void __launch_bounds__(128, ADJ ? SST_SHADE_ADJ_MIN_BLOCKS : SST_SHAD
                 const DevMaterial& m = sc.mats[s.mat];
                 Lp lp = {};
                 float3 diffBase = mk(0, 0, 0);
-                if (m.type == kGeneric) lp = localParams(sc, m, s.uv);
+                if (GEN && m.type == kGeneric) lp = localParams(sc, m, s.uv);
                 else diffBase = lookupRgb(sc, m.baseTex, m.base, s.uv);
 
                 // OnLightHit (PathTracer.cs:402-421)
@@ -492,7 +494,7 @@ __global__ void __launch_bounds__(128, ADJ ? SST_SHADE_ADJ_MIN_BLOCKS : SST_SHAD
                                 float3 ed; float epdf; float3 ew;
                                 envSample(sc.env, e1, e2, ed, epdf, ew);
                                 float pb;
-                                float3 bc = evalWithCos(sc, m, lp, diffBase, c, ed, pb);
+                                float3 bc = evalWithCos<GEN>(sc, m, lp, diffBase, c, ed, pb);
                                 if (!(pb == 0.0f || epdf == 0.0f)) {
                                     float mis = cfg.enableBsdfDI ? 1.0f / (1.0f + pb / (epdf * (float)cfg.numShadowRays)) : 1.0f;
                                     float3 contrib = ew * bc / (float)cfg.numShadowRays;
@@ -539,7 +541,7 @@ __global__ void __launch_bounds__(128, ADJ ? SST_SHADE_ADJ_MIN_BLOCKS : SST_SHAD
                                 float3 emis = emitted(em, lpSn, l2s);
                                 float jac = areaToSolidAngle(s.pos, lpPos, lpN);
                                 float pb;
-                                float3 bc = evalWithCos(sc, m, lp, diffBase, c, -l2s, pb);
+                                float3 bc = evalWithCos<GEN>(sc, m, lp, diffBase, c, -l2s, pb);
                                 float lpPdf = em.faceN.w;
                                 float pne = lpPdf * selProb * (float)cfg.numShadowRays;
                                 float pbA = pb * jac;
@@ -582,7 +584,7 @@ __global__ void __launch_bounds__(128, ADJ ? SST_SHADE_ADJ_MIN_BLOCKS : SST_SHAD
                     float uc = rng.nextFloat();
                     float u1 = rng.nextFloat(), u2 = rng.nextFloat();
                     float3 dirW; float bpdf = 0.f; float3 bw = mk(0, 0, 0);
-                    bool ok = sampleMaterial(sc, m, lp, diffBase, c, uc, u1, u2, dirW, bpdf, bw);
+                    bool ok = sampleMaterial<GEN>(sc, m, lp, diffBase, c, uc, u1, u2, dirW, bpdf, bw);
                     if (!ok || bpdf == 0.0f || isBlack(bw)) {
                         if (pend) { cont = true; outDepth = kDoneFlag; }
                         else terminate = true;
@@ -656,15 +658,19 @@ __global__ void __launch_bounds__(128, ADJ ? SST_SHADE_ADJ_MIN_BLOCKS : SST_SHAD
     }
 }
 
-void launch_shade(int ns, bool adj, const DevJob* jobs, const PathBuf& A, const PathBuf& B, const float4* hits, float4* nee, float4* neeG, int cap,
-                  float4* shRo, float4* shRd, int* shTgt, uint32_t* shJob, const int* nIn, int* nOut, int* nSh, float* samples, DevStats* stats,
-                  int maxItems, cudaStream_t s) {
+void launch_shade(int ns, bool adj, bool generic, const DevJob* jobs, const PathBuf& A, const PathBuf& B, const float4* hits, float4* nee,
+                  float4* neeG, int cap, float4* shRo, float4* shRd, int* shTgt, uint32_t* shJob, const int* nIn, int* nOut, int* nSh, float* samples,
+                  DevStats* stats, int maxItems, cudaStream_t s) {
     int grid = (maxItems + 127) / 128;
     if (grid == 0) return;
+    if (!generic && !adj && ns == 1) {
+        k_shade<1, false, false><<<grid, 128, 0, s>>>(jobs, A, B, hits, nee, neeG, cap, shRo, shRd, shTgt, shJob, nIn, nOut, nSh, samples, stats);
+        return;
+    }
 #define SST_SHADE_CASE(N)                                                                                                                    \
     case N:                                                                                                                                  \
-        if (adj) k_shade<N, true><<<grid, 128, 0, s>>>(jobs, A, B, hits, nee, neeG, cap, shRo, shRd, shTgt, shJob, nIn, nOut, nSh, samples, stats); \
-        else k_shade<N, false><<<grid, 128, 0, s>>>(jobs, A, B, hits, nee, neeG, cap, shRo, shRd, shTgt, shJob, nIn, nOut, nSh, samples, stats); \
+        if (adj) k_shade<N, true, true><<<grid, 128, 0, s>>>(jobs, A, B, hits, nee, neeG, cap, shRo, shRd, shTgt, shJob, nIn, nOut, nSh, samples, stats); \
+        else k_shade<N, false, true><<<grid, 128, 0, s>>>(jobs, A, B, hits, nee, neeG, cap, shRo, shRd, shTgt, shJob, nIn, nOut, nSh, samples, stats); \
         break;
     switch (ns) {
         SST_SHADE_CASE(1)

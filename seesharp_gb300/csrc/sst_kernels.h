@@ -34,9 +34,9 @@ void launch_trace_shadow(const TraceTuning& t, const DevJob* jobs, const uint32_
                          const int* count, int* work, float4* nee, DevStats* stats, cudaStream_t s);
 void launch_trace_query(const TraceTuning& t, const DevJob* jobs, const float4* ro, const float4* rd, const int* count, int* work, float4* hits,
                         int* occl, DevStats* stats, bool anyHit, cudaStream_t s);
-void launch_shade(int ns, bool adj, const DevJob* jobs, const PathBuf& A, const PathBuf& B, const float4* hits, float4* nee, float4* neeG, int cap,
-                  float4* shRo, float4* shRd, int* shTgt, uint32_t* shJob, const int* nIn, int* nOut, int* nSh, float* samples, DevStats* stats,
-                  int maxItems, cudaStream_t s);
+void launch_shade(int ns, bool adj, bool generic, const DevJob* jobs, const PathBuf& A, const PathBuf& B, const float4* hits, float4* nee,
+                  float4* neeG, int cap, float4* shRo, float4* shRd, int* shTgt, uint32_t* shJob, const int* nIn, int* nOut, int* nSh, float* samples,
+                  DevStats* stats, int maxItems, cudaStream_t s);
 void launch_debug_material_eval(const DevScene& sc, int mat, int n, const float* pts, const float* outs, const float* ins, float* vals, float* pdfs,
                                 cudaStream_t s);
 void launch_debug_material_sample(const DevScene& sc, int mat, int n, const float* pts, const float* outs, const float* us, float* dirs, float* pdfs,
