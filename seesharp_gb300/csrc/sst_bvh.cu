@@ -25,7 +25,9 @@ namespace sst {
 
 namespace {
 
-constexpr float kCt = 1.0f;  // traversal cost relative to one triangle test
+// Traversal cost relative to one triangle test.  0.25 keeps most leaves at one triangle: on the
+// 1M-triangle scene it traverses 3.4% faster than 1.0 (and 1.0 17% faster than 3.0).
+constexpr float kCt = 0.25f;
 constexpr float kCi = 1.0f;
 
 __device__ __forceinline__ int floatOrd(float f) {
@@ -132,7 +134,7 @@ __device__ __forceinline__ float areaOf(const float* lo, const float* hi) {
 // Bottom-up refit from every leaf.  boxes: 6 floats per inner node; cost: per inner node;
 // collapse[i] = 1 when the subtree is cheaper as one leaf.
 __global__ void k_refit(const float4* tri, const int* order, int n, const int2* range, const int2* child, const int* parentInner,
-                        const int* parentLeaf, int* visits, float* boxes, float* cost, int* collapse) {
+                        const int* parentLeaf, int* visits, float* boxes, float* cost, int* collapse, float ct, int maxLeaf) {
     int li = blockIdx.x * blockDim.x + threadIdx.x;
     if (li >= n) return;
     int node = parentLeaf[li];
@@ -164,9 +166,9 @@ __global__ void k_refit(const float4* tri, const int* order, int n, const int2* 
         float A = areaOf(lo, hi);
         int2 r = range[node];
         int cnt = r.y - r.x + 1;
-        float split = kCt * A + cs;
+        float split = ct * A + cs;
         float leaf = kCi * cnt * A;
-        bool col = cnt <= kMaxLeafSize && leaf <= split;
+        bool col = cnt <= maxLeaf && leaf <= split;
         float* bo = boxes + 6 * (size_t)node;
         for (int k = 0; k < 3; ++k) { bo[k] = lo[k]; bo[3 + k] = hi[k]; }
         cost[node] = col ? leaf : split;
@@ -528,7 +530,13 @@ int buildLbvh(const float4* tri, int n, float4* nodesOut, int* orderOut, void* s
     } else {
         k_karras<<<grid, 256, 0, st>>>(keysB, n, range, child, parentInner, parentLeaf);
     }
-    k_refit<<<grid, 256, 0, st>>>(tri, order, n, range, child, parentInner, parentLeaf, visits, boxes, cost, collapse);
+    // SAH constants: traversal cost relative to one triangle test and the largest leaf
+    // (SST_BVH_CT / SST_BVH_LEAF override them for experiments)
+    const char* ctEnv = getenv("SST_BVH_CT");
+    const char* leafEnv = getenv("SST_BVH_LEAF");
+    const float ct = ctEnv ? (float)atof(ctEnv) : kCt;
+    const int maxLeaf = leafEnv ? std::max(1, std::min(kMaxLeafSize, atoi(leafEnv))) : kMaxLeafSize;
+    k_refit<<<grid, 256, 0, st>>>(tri, order, n, range, child, parentInner, parentLeaf, visits, boxes, cost, collapse, ct, maxLeaf);
     k_kept<<<grid, 256, 0, st>>>(parentInner, collapse, n, kept, small + 6);
     size_t scanBytes = 0;
     cub::DeviceScan::ExclusiveSum(nullptr, scanBytes, kept, newIdx, n - 1, st);
