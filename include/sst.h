@@ -253,25 +253,32 @@ int sst_trace_light_paths(sst_scene* scene, uint32_t seed, uint32_t iteration, i
  * Computed on the device while the film is folded:
  *  - the VarianceLayer (FrameBuffer.Flags.EstimatePixelVariance, Images/VarianceLayer.cs:10-84);
  *  - the per-iteration error metrics against FrameBuffer.ReferenceImage (FrameBuffer.cs:276-277,
- *    378-383): the mean over pixels and channels of (x - r)^2 and of (x - r)^2 / (r^2 + 0.01) (the
- *    outlier-rejecting RelMSE of SimpleImageIO is not computed);
+ *    378-383): the mean over pixels and channels of (x - r)^2 and of (x - r)^2 / (r^2 + 0.01), and
+ *    the outlier-rejecting RelMSE: each pixel's error is its mean over the channels of
+ *    (x - r)^2 / (r^2 + 0.01), the largest floor(width*height / 1000) of them (0.1%) are dropped and
+ *    the rest averaged.  It needs 4 bytes of device memory per pixel and iteration of the call;
  *  - the denoiser's feature layers (DenoiseBuffers.LogPrimaryHit, Integrators/Util/DenoiseBuffers.cs:20-23,
  *    logged at the primary hit as in PathTracer.cs:336-339): running means of the material's scatter
- *    strength and of the shading normal.
- * The running means resume like the film: when firstIteration > 0 the state arrays hold the layers
- * after iteration firstIteration and are read, and they are always written back. */
+ *    strength and of the shading normal;
+ *  - the OutlierReplayCache (Integrators/Util/OutlierReplayCache.cs:9-35, notified by
+ *    FrameBuffer.Splat, FrameBuffer.cs:187-190): per pixel the numOutliers samples of largest channel
+ *    average with their iteration, in the array order of .NET's 4-ary PriorityQueue min-heap.
+ * The running means and the heaps resume like the film: when firstIteration > 0 the state arrays
+ * hold the layers after iteration firstIteration and are read, and they are always written back. */
 typedef struct SstFilmLayers {
     float* variance;        /* out: width*height VarianceLayer image, or NULL */
     float* varianceAverage; /* out: 1 float, VarianceLayer.Average, or NULL */
     float* varianceState;   /* in/out: 2*width*height running means of the iteration's value and of its
                                square (required with variance or varianceAverage) */
     const float* reference; /* in: width*height*3 reference image, or NULL */
-    double* errors;         /* out: 2 per iteration of this call (MSE, RelMSE after it; zero for iterations that a
-                               time limit skipped), or NULL */
+    double* errors;         /* out: 3 per iteration of this call (MSE, RelMSE, RelMSE_Outlier after it; zero for
+                               iterations that a time limit skipped), or NULL */
     float* albedo;          /* in/out: width*height*3 "albedo" layer, or NULL */
     float* normal;          /* in/out: width*height*3 "normal" layer, or NULL */
     int32_t memory;         /* SST_MEM_HOST / SST_MEM_DEVICE for the arrays above */
-    int32_t reserved;
+    int32_t numOutliers;    /* OutlierReplayCache capacity per pixel, 0..8 (FrameBuffer.NumOutliersToTrack; 0: none) */
+    float* outlierWeight;   /* in/out: width*height*numOutliers heap priorities (the sample's channel average) */
+    int32_t* outlierIteration; /* in/out: width*height*numOutliers heap elements (0-based iteration, -1: empty) */
 } SstFilmLayers;
 /* sst_render that also fills the requested layers. */
 int sst_render_layers(sst_scene* scene, const SstPathTracerParams* params, float* film, int32_t memory, const SstFilmLayers* layers,

@@ -3,13 +3,13 @@
 The Python classes mirror SeeSharp's scene and integrator API; rendering and ray queries run in
 libsst.so (CUDA, C ABI in include/sst.h).
 """
-from .images import (BorderHandling, FrameBuffer, MonochromeImage, RgbColor, RgbImage, TextureMono, TextureRgb, mean_rgb,
-                     rel_mse)
+from .images import (BorderHandling, FrameBuffer, MonochromeImage, OutlierReplayCache, Pixel, RgbColor, RgbImage, TextureMono,
+                     TextureRgb, mean_rgb, rel_mse, rel_mse_outlier_rejection)
 from .integrators import Integrator, PathTracer, autotune, render_batch
 from .scene import (ArgumentException, DiffuseEmitter, DiffuseMaterial, EnvironmentMap, GenericMaterial, GlossyEmitter,
                     InvalidOperationException, Matrix4x4, Mesh, PerspectiveCamera, Scene, Triangle)
 
-__all__ = ["BorderHandling", "FrameBuffer", "MonochromeImage", "RgbColor", "RgbImage", "TextureMono", "TextureRgb", "mean_rgb",
-           "rel_mse", "Integrator", "PathTracer", "autotune", "render_batch", "ArgumentException", "DiffuseEmitter", "DiffuseMaterial", "EnvironmentMap",
+__all__ = ["BorderHandling", "FrameBuffer", "MonochromeImage", "OutlierReplayCache", "Pixel", "RgbColor", "RgbImage", "TextureMono",
+           "TextureRgb", "mean_rgb", "rel_mse", "rel_mse_outlier_rejection", "Integrator", "PathTracer", "autotune", "render_batch", "ArgumentException", "DiffuseEmitter", "DiffuseMaterial", "EnvironmentMap",
            "GenericMaterial", "GlossyEmitter", "InvalidOperationException", "Matrix4x4", "Mesh", "PerspectiveCamera", "Scene",
            "Triangle"]

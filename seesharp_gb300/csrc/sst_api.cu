@@ -117,7 +117,7 @@ struct sst_ctx {
     // light paths (sst_trace_light_paths)
     DevBuf lightA[9], lightB[9], lightHits, lightVerts, lightLengths, lightCnt;
     // frame-buffer layers (sst_render_layers)
-    DevBuf layMean, layRef, layErr, layVar, laySum, layAlb, layNrm, aovSamples;
+    DevBuf layMean, layRef, layErr, layVar, laySum, layAlb, layNrm, aovSamples, layErrPix, layTrim, layOutW, layOutIt;
     // batched adjoint: the jobs of the last sst_forward_batch, their path radiance, dLoss/dImage
     std::vector<BatchSig> batchSig;
     std::vector<std::unique_ptr<DevBuf>> batchRecord, batchDLdI;
@@ -1594,6 +1594,9 @@ int sst_render_layers(sst_scene* s, const SstPathTracerParams* p, float* film, i
         if (wantVar && !L->varianceState) fail(SST_ERR_INVALID_ARGUMENT, "the variance layer needs its state array");
         if (L->errors && !L->reference) fail(SST_ERR_INVALID_ARGUMENT, "error metrics need a reference image");
         if ((L->albedo == nullptr) != (L->normal == nullptr)) fail(SST_ERR_INVALID_ARGUMENT, "albedo and normal layers come together");
+        if (L->numOutliers < 0 || L->numOutliers > kMaxOutliers) fail(SST_ERR_INVALID_ARGUMENT, "numOutliers must be 0..8");
+        if (L->numOutliers > 0 && (!L->outlierWeight || !L->outlierIteration))
+            fail(SST_ERR_INVALID_ARGUMENT, "the outlier cache needs its weight and iteration arrays");
         sst_ctx* c = s->ctx;
         cudaStream_t st = c->stream;
         CUDA_CHECK(cudaSetDevice(c->device));
@@ -1637,8 +1640,47 @@ int sst_render_layers(sst_scene* s, const SstPathTracerParams* p, float* film, i
             c->layErr.ensure(std::max<size_t>(1, size_t(S) * 16));
             CUDA_CHECK(cudaMemsetAsync(c->layErr.p, 0, std::max<size_t>(1, size_t(S) * 16), st));
             lay.errSum = c->layErr.as<double>();
+            if (L->errors && first < S) {
+                // per-pixel errors of every iteration of this call, for the outlier-rejecting RelMSE
+                c->layErrPix.ensure(size_t(S - first) * P * 4);
+                lay.errPix = c->layErrPix.as<float>();
+                lay.errFirst = first;
+            }
+        }
+        const int nOut = L->numOutliers;
+        if (nOut > 0) {
+            // OutlierReplayCache: created empty with the frame buffer's first iteration, kept after that
+            const size_t n = P * size_t(nOut);
+            c->layOutW.ensure(n * 4);
+            c->layOutIt.ensure(n * 4);
+            if (resume) {
+                CUDA_CHECK(cudaMemcpyAsync(c->layOutW.p, L->outlierWeight, n * 4, in, st));
+                CUDA_CHECK(cudaMemcpyAsync(c->layOutIt.p, L->outlierIteration, n * 4, in, st));
+            } else {
+                CUDA_CHECK(cudaMemsetAsync(c->layOutW.p, 0, n * 4, st));
+                CUDA_CHECK(cudaMemsetAsync(c->layOutIt.p, 0xFF, n * 4, st));
+            }
+            lay.nOut = nOut;
+            lay.outW = c->layOutW.as<float>();
+            lay.outIt = c->layOutIt.as<int>();
         }
         if (first < S) renderJobs(c, jobs, &local);
+        if (nOut > 0) {
+            const size_t n = P * size_t(nOut);
+            CUDA_CHECK(cudaMemcpyAsync(L->outlierWeight, lay.outW, n * 4, out, st));
+            CUDA_CHECK(cudaMemcpyAsync(L->outlierIteration, lay.outIt, n * 4, out, st));
+        }
+        std::vector<double> trim;
+        if (lay.errPix) {
+            const int nIt = S - first, done = std::min(nIt, std::max(0, local.numIterations));
+            c->layTrim.ensure(size_t(nIt) * 8);
+            CUDA_CHECK(cudaMemsetAsync(c->layTrim.p, 0, size_t(nIt) * 8, st));
+            // the largest 0.1% of the pixels are dropped (SimpleImageIO's default percentage)
+            launch_error_trim(lay.errPix, int(P), int(P / 1000), done, c->layTrim.as<double>(), st);
+            CUDA_CHECK(cudaGetLastError());
+            trim.resize(nIt);
+            CUDA_CHECK(cudaMemcpyAsync(trim.data(), c->layTrim.p, size_t(nIt) * 8, cudaMemcpyDeviceToHost, st));
+        }
         if (wantVar) {
             CUDA_CHECK(cudaMemcpyAsync(L->varianceState, lay.varMean, P * 8, out, st));
             c->layVar.ensure(P * 4);
@@ -1664,11 +1706,15 @@ int sst_render_layers(sst_scene* s, const SstPathTracerParams* p, float* film, i
             std::vector<double> e(2 * size_t(S));
             CUDA_CHECK(cudaMemcpyAsync(e.data(), c->layErr.p, e.size() * 8, cudaMemcpyDeviceToHost, st));
             CUDA_CHECK(cudaStreamSynchronize(st));
-            for (auto& x : e) x /= double(3 * P);
-            const double* src = e.data() + 2 * size_t(first);
-            size_t n = 2 * size_t(S - first);
-            if (L->memory == SST_MEM_DEVICE) CUDA_CHECK(cudaMemcpy(L->errors, src, n * 8, cudaMemcpyHostToDevice));
-            else std::copy(src, src + n, L->errors);
+            const int nIt = S - first;
+            std::vector<double> res(3 * size_t(nIt));
+            for (int i = 0; i < nIt; ++i) {
+                res[3 * i] = e[2 * size_t(first + i)] / double(3 * P);
+                res[3 * i + 1] = e[2 * size_t(first + i) + 1] / double(3 * P);
+                res[3 * i + 2] = trim[i];
+            }
+            if (L->memory == SST_MEM_DEVICE) CUDA_CHECK(cudaMemcpy(L->errors, res.data(), res.size() * 8, cudaMemcpyHostToDevice));
+            else std::copy(res.begin(), res.end(), L->errors);
         }
         if (memory != SST_MEM_DEVICE) CUDA_CHECK(cudaMemcpyAsync(film, dFilm, P * 12, cudaMemcpyDeviceToHost, st));
         CUDA_CHECK(cudaStreamSynchronize(st));

@@ -119,6 +119,43 @@ __global__ void __launch_bounds__(256) k_camera(const DevJob* __restrict__ jobs,
     }
 }
 
+// OutlierReplayCache.Notify (Integrators/Util/OutlierReplayCache.cs:9-22): the pixel keeps the n
+// samples of largest channel average in a .NET PriorityQueue, a 4-ary min-heap in an array.  While
+// it holds fewer than n, Enqueue appends the sample and moves it up past every parent of strictly
+// larger priority; after that EnqueueDequeue replaces the root only by a strictly larger sample and
+// moves it down, each step to the first child of least priority, while that child is strictly
+// smaller.  A sample that only ties the smallest kept one does not enter, and the array order is
+// the reference's.
+SST_D void outlierNotify(float* w, int* it, int& cnt, int n, float p, int iter) {
+    int k;
+    if (cnt < n) {
+        k = cnt++;
+        while (k > 0) {
+            int par = (k - 1) >> 2;
+            if (!(p < w[par])) break;
+            w[k] = w[par];
+            it[k] = it[par];
+            k = par;
+        }
+    } else {
+        if (cnt == 0 || !(p > w[0])) return;
+        k = 0;
+        for (;;) {
+            int c = 4 * k + 1;
+            if (c >= cnt) break;
+            int m = c, e = min(c + 4, cnt);
+            for (int j = c + 1; j < e; ++j)
+                if (w[j] < w[m]) m = j;
+            if (p <= w[m]) break;
+            w[k] = w[m];
+            it[k] = it[m];
+            k = m;
+        }
+    }
+    w[k] = p;
+    it[k] = iter;
+}
+
 // =============================================================================================
 // K8: fold the per-iteration path estimates of a wave into the film with the frame buffer's
 // running mean: for iteration k (1-based) film = film * (k - 1) / k + v / k, non-finite
@@ -149,6 +186,16 @@ __global__ void k_film_fold(const DevJob* __restrict__ jobs, const WaveChunk* __
             alb = mk(lay.aovAlbedo[3 * pix], lay.aovAlbedo[3 * pix + 1], lay.aovAlbedo[3 * pix + 2]);
             nrm = mk(lay.aovNormal[3 * pix], lay.aovNormal[3 * pix + 1], lay.aovNormal[3 * pix + 2]);
         }
+        // the pixel's outlier heap (slots 0..cnt-1 are occupied, empty ones hold iteration -1)
+        const int nOut = lay.nOut;
+        float hw[kMaxOutliers];
+        int hit[kMaxOutliers];
+        int hcnt = 0;
+        for (int j = 0; j < nOut; ++j) {
+            hw[j] = lay.outW[pix * nOut + j];
+            hit[j] = lay.outIt[pix * nOut + j];
+            hcnt += hit[j] >= 0;
+        }
         for (int m = 0; m < ck.nIter; ++m) {
             uint32_t iter = (uint32_t)(ck.iterBase + m);
             const float* s = samples + 3 * ((size_t)ck.itemOffset + (size_t)m * ck.pixCount + p);
@@ -168,6 +215,7 @@ __global__ void k_film_fold(const DevJob* __restrict__ jobs, const WaveChunk* __
             }
             bool used = finite || !cfg.ignoreNan;
             if (used) cur = cur + v / kf;
+            if (finite && nOut > 0) outlierNotify(hw, hit, hcnt, nOut, a, (int)iter);
             if (lay.aovAlbedo) {
                 // RgbLayer running means (Images/Layer.cs:33-37, RgbLayer.cs:17-18)
                 const float* a6 = lay.aovSamples + 6 * ((size_t)ck.itemOffset + (size_t)m * ck.pixCount + p);
@@ -195,6 +243,7 @@ __global__ void k_film_fold(const DevJob* __restrict__ jobs, const WaveChunk* __
                 double e1 = (double)d.x * d.x + (double)d.y * d.y + (double)d.z * d.z;
                 double e2 = (double)d.x * d.x / ((double)ref.x * ref.x + 0.01) + (double)d.y * d.y / ((double)ref.y * ref.y + 0.01) +
                             (double)d.z * d.z / ((double)ref.z * ref.z + 0.01);
+                if (lay.errPix) lay.errPix[(size_t)((int)iter - lay.errFirst) * cfg.W * cfg.H + pix] = (float)(e2 / 3.0);
                 cg::coalesced_group act = cg::coalesced_threads();
                 cg::coalesced_group grp = cg::labeled_partition(act, (int)iter);
                 e1 = cg::reduce(grp, e1, cg::plus<double>());
@@ -206,6 +255,10 @@ __global__ void k_film_fold(const DevJob* __restrict__ jobs, const WaveChunk* __
             }
         }
         f[0] = cur.x; f[1] = cur.y; f[2] = cur.z;
+        for (int j = 0; j < nOut; ++j) {
+            lay.outW[pix * nOut + j] = hw[j];
+            lay.outIt[pix * nOut + j] = hit[j];
+        }
         if (lay.varMean) {
             lay.varMean[pix] = vMean;
             lay.varMoment[pix] = vMoment;
@@ -257,6 +310,82 @@ __global__ void k_variance_finish(const float* mean, const float* moment, int W,
     }
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
     if ((threadIdx.x & 31) == 0) atomicAdd(sum, v);
+}
+
+// FrameBuffer.ComputeErrorMetric's RelMSE_OutlierRejection (Images/FrameBuffer.cs:378-383, computed
+// by SimpleImageIO's Metrics): the mean of the pixels' relative squared errors after the k largest
+// are dropped.  One block per iteration.  The errors are non-negative, so their bit patterns order
+// like their values (NaN above +inf); a most-significant-digit-first radix select over 8-bit digits
+// finds the bits T of the k-th largest error and how many copies of T are among the k largest.  The
+// kept errors (all below T, and the remaining copies of T) are then summed in double.
+__global__ void __launch_bounds__(1024) k_error_trim(const float* err, int P, int k, double* out) {
+    const uint32_t* e = reinterpret_cast<const uint32_t*>(err) + (size_t)blockIdx.x * P;
+    __shared__ unsigned hist[256];
+    __shared__ uint32_t sPrefix;
+    __shared__ int sNeed;
+    __shared__ double sSum[32];
+    __shared__ unsigned sEq[32];
+    const int tid = threadIdx.x, nt = blockDim.x;
+    uint32_t prefix = 0xFFFFFFFFu, mask = 0;
+    int need = 0;
+    if (k > 0) {
+        prefix = 0;
+        need = k;
+        for (int shift = 24; shift >= 0; shift -= 8) {
+            for (int i = tid; i < 256; i += nt) hist[i] = 0;
+            __syncthreads();
+            for (int i = tid; i < P; i += nt) {
+                uint32_t b = e[i];
+                if ((b & mask) == prefix) atomicAdd(&hist[(b >> shift) & 255u], 1u);
+            }
+            __syncthreads();
+            if (tid == 0) {
+                // the digit d with fewer than `need` candidates above it and at least `need` from it up
+                unsigned acc = 0;
+                int d = 255;
+                for (; d > 0; --d) {
+                    if (acc + hist[d] >= (unsigned)need) break;
+                    acc += hist[d];
+                }
+                sPrefix = prefix | ((uint32_t)d << shift);
+                sNeed = need - (int)acc;
+            }
+            __syncthreads();
+            prefix = sPrefix;
+            need = sNeed;
+            mask |= 255u << shift;
+        }
+    }
+    double sum = 0.0;
+    unsigned eq = 0;
+    for (int i = tid; i < P; i += nt) {
+        uint32_t b = e[i];
+        if (b < prefix) sum += (double)__uint_as_float(b);
+        else if (b == prefix) ++eq;
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+        sum += __shfl_xor_sync(0xffffffffu, sum, o);
+        eq += __shfl_xor_sync(0xffffffffu, eq, o);
+    }
+    if ((tid & 31) == 0) {
+        sSum[tid >> 5] = sum;
+        sEq[tid >> 5] = eq;
+    }
+    __syncthreads();
+    if (tid == 0) {
+        double s = 0.0;
+        unsigned q = 0;
+        for (int w = 0; w < (nt + 31) / 32; ++w) {
+            s += sSum[w];
+            q += sEq[w];
+        }
+        if (q > (unsigned)need) s += (double)(q - (unsigned)need) * (double)__uint_as_float(prefix);
+        out[blockIdx.x] = s / (double)(P - k);
+    }
+}
+
+void launch_error_trim(const float* err, int P, int k, int iterations, double* out, cudaStream_t s) {
+    if (iterations > 0 && P > k) k_error_trim<<<iterations, 1024, 0, s>>>(err, P, k, out);
 }
 
 void launch_variance_finish(const float* mean, const float* moment, int W, int H, float* out, double* sum, cudaStream_t s) {

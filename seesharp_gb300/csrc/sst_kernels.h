@@ -13,6 +13,8 @@ void launch_light_start(const DevJob* jobs, const LightParams& P, const LightPat
                         cudaStream_t s);
 void launch_light_walk(const DevJob* jobs, const LightParams& P, const LightPathBuf& A, const LightPathBuf& B, const float4* hits, const int* nIn,
                        int* nOut, SstPathVertexDev* verts, int* lengths, int maxItems, cudaStream_t s);
+// Outlier-rejecting RelMSE per iteration: `iterations` rows of P per-pixel errors -> out[row].
+void launch_error_trim(const float* err, int P, int k, int iterations, double* out, cudaStream_t s);
 void launch_variance_finish(const float* mean, const float* moment, int W, int H, float* out, double* sum, cudaStream_t s);
 void launch_film_fold(const DevJob* jobs, const WaveChunk* chunks, const WaveDesc* waves, int* curWave, const float* samples, DevStats* st,
                       int maxFold, int advance, cudaStream_t s);

@@ -135,7 +135,14 @@ struct DevLayers {
     float* aovAlbedo;   // W*H*3 running mean of the primary hit's scatter strength
     float* aovNormal;   // W*H*3 running mean of the primary hit's shading normal
     float* aovSamples;  // 6 per wave item: this iteration's (albedo, normal), written by the first shade
+    float* errPix;      // (iteration - errFirst) * W*H + pixel: the pixel's relative squared error after the
+                        // iteration (mean over the channels), for the outlier-rejecting RelMSE
+    int errFirst;       // first iteration of the call
+    int nOut;           // OutlierReplayCache heap capacity per pixel (0: not tracked), at most kMaxOutliers
+    float* outW;        // W*H*nOut heap priorities: the sample's channel average, 4-ary min-heap order
+    int* outIt;         // W*H*nOut heap elements: the sample's 0-based iteration, -1 for an empty slot
 };
+constexpr int kMaxOutliers = 8;
 
 // One render job: its scene and path-tracer settings (the kernels index this table by the job
 // id every path carries).

@@ -78,7 +78,8 @@ def _exr_unzip(data, expected):
     return out.tobytes()
 
 
-def read_exr(path):
+def read_exr_channels(path):
+    """Every channel of a scan-line OpenEXR file: {name: float32 (height, width)}."""
     with open(path, "rb") as f:
         b = f.read()
     attrs, p = _exr_header(b)
@@ -111,6 +112,11 @@ def read_exr(path):
                 cnt = w * dt.itemsize
                 planes[name][y0 + r] = np.frombuffer(data, dt, count=w, offset=q).astype(np.float32)
                 q += cnt
+    return planes
+
+
+def read_exr(path):
+    planes = read_exr_channels(path)
     if all(c in planes for c in "RGB"):
         rgb = np.stack([planes["R"], planes["G"], planes["B"]], -1)
     elif "Y" in planes:
@@ -118,6 +124,47 @@ def read_exr(path):
     else:
         raise ValueError("OpenEXR file has neither R, G, B nor Y channels")
     return np.ascontiguousarray(rgb, np.float32)
+
+
+def _attr(name, typ, payload):
+    return name.encode() + b"\0" + typ.encode() + b"\0" + struct.pack("<i", len(payload)) + payload
+
+
+def write_exr(path, channels):
+    """A single-part scan-line OpenEXR file, uncompressed, FLOAT channels.  channels: {name: (height,
+    width) array}; layer channels are named "layer.R" and so on, the main image "R", "G", "B".
+    Channels are stored in the alphabetical order the format requires."""
+    names = sorted(channels)
+    if not names:
+        raise ValueError("no channels")
+    h, w = np.shape(channels[names[0]])
+    planes = []
+    for n in names:
+        a = np.asarray(channels[n], np.float32)
+        if a.shape != (h, w):
+            raise ValueError(f"channel {n} has shape {a.shape}, expected {(h, w)}")
+        planes.append(a.astype("<f4"))
+    chlist = b"".join(n.encode() + b"\0" + struct.pack("<iB3xii", 2, 0, 1, 1) for n in names) + b"\0"
+    header = struct.pack("<ii", _EXR_MAGIC, 2)
+    header += _attr("channels", "chlist", chlist)
+    header += _attr("compression", "compression", b"\0")
+    header += _attr("dataWindow", "box2i", struct.pack("<4i", 0, 0, w - 1, h - 1))
+    header += _attr("displayWindow", "box2i", struct.pack("<4i", 0, 0, w - 1, h - 1))
+    header += _attr("lineOrder", "lineOrder", b"\0")
+    header += _attr("pixelAspectRatio", "float", struct.pack("<f", 1.0))
+    header += _attr("screenWindowCenter", "v2f", struct.pack("<ff", 0.0, 0.0))
+    header += _attr("screenWindowWidth", "float", struct.pack("<f", 1.0))
+    header += b"\0"
+    line_bytes = 4 * w * len(names)
+    start = len(header) + 8 * h
+    offsets = struct.pack(f"<{h}Q", *[start + y * (8 + line_bytes) for y in range(h)])
+    with open(path, "wb") as f:
+        f.write(header)
+        f.write(offsets)
+        for y in range(h):
+            f.write(struct.pack("<ii", y, line_bytes))
+            for pl in planes:
+                f.write(pl[y].tobytes())
 
 
 # ---------------------------------------------------------------------------------------------

@@ -9,8 +9,13 @@ from __future__ import annotations
 
 import enum
 import json
+import os
+from collections import namedtuple
 
 import numpy as np
+
+# Images/Pixel.cs: integer pixel coordinates, column from the left, row from the top
+Pixel = namedtuple("Pixel", "Col Row")
 
 
 class RgbColor:
@@ -196,6 +201,43 @@ class VarianceLayer(Layer):
         self.state = np.zeros((2, height, width), np.float32)
 
 
+class OutlierReplayCache:
+    """Integrators/Util/OutlierReplayCache.cs: per pixel the n samples with the largest channel
+    average, with the (0-based) iteration that produced them, so that a path can be replayed from
+    its seed.  The heaps are kept by the GPU film fold in the array order of .NET's PriorityQueue
+    (a 4-ary min-heap); GetPixelOutlier returns that order, as PriorityQueue.UnorderedItems does.
+    Only the sample's channel average (the priority) is kept, not its RGB weight."""
+
+    PathReplayInfo = namedtuple("PathReplayInfo", "Iteration")
+    Item = namedtuple("Item", "Element Priority")
+
+    class PixelOutliers:
+        def __init__(self, items):
+            self.UnorderedItems = items
+            self.Count = len(items)
+
+    def __init__(self, width, height, n):
+        self.width, self.nMax = int(width), int(n)
+        self.weight = np.zeros((int(height), self.width, self.nMax), np.float32)
+        self.iteration = np.full((int(height), self.width, self.nMax), -1, np.int32)
+
+    def GetPixelOutlier(self, pixel):
+        col, row = pixel
+        return OutlierReplayCache.PixelOutliers([OutlierReplayCache.Item(OutlierReplayCache.PathReplayInfo(int(i)), float(w))
+                                                 for w, i in zip(self.weight[row, col], self.iteration[row, col]) if i >= 0])
+
+    def outlier_layers(self):
+        """FrameBuffer.WriteToFile's "outlier-i" images (FrameBuffer.cs:321-335): per pixel the
+        iterations ordered by descending priority (a stable sort of the heap array), 0 where a
+        pixel has fewer entries."""
+        h, w, n = self.weight.shape
+        key = np.where(self.iteration >= 0, self.weight, -np.inf)
+        order = np.argsort(-key, axis=2, kind="stable")
+        its = np.take_along_axis(self.iteration, order, axis=2)
+        its = np.where(its >= 0, its, 0).astype(np.float32)
+        return [its[:, :, i] for i in range(n)]
+
+
 class FrameBuffer:
     """Progressive film with a running mean over iterations (Images/FrameBuffer.cs).
 
@@ -225,6 +267,8 @@ class FrameBuffer:
         self.NaNWarnings = []
         self.ReferenceImage = None   # RgbImage: per-iteration error metrics are recorded in Errors
         self.Errors = []             # (TimeMS, MSE, RelMSE, RelMSE_Outlier) per iteration
+        self.NumOutliersToTrack = 4  # FrameBuffer.cs:36; 0..8 on the GPU
+        self.OutlierCache = None     # created with the first iteration (FrameBuffer.Initialize, :229)
         self.layers = {}
         self.PixelVariance = None
         if self.flags & FrameBuffer.Flags.EstimatePixelVariance:
@@ -248,24 +292,51 @@ class FrameBuffer:
         self.CurIteration = 0
         self.Image = RgbImage(self.Width, self.Height)
         self.Errors = []
+        self.OutlierCache = None
         for layer in self.layers.values():
             layer.Init(self.Width, self.Height)
             if isinstance(layer, VarianceLayer):
                 layer.Average = 0.0
 
     def WriteToFile(self, filename=None):
-        """Writes the image as a PFM (little endian, bottom row first) and the metadata as JSON.
-
-        EXR output is out of scope; PFM is a lossless float format readable by common tools.
-        """
+        """FrameBuffer.WriteToFile (FrameBuffer.cs:312-368).  An ".exr" name gets one layered
+        OpenEXR file: the image as R, G, B, every layer as "<name>.R/G/B" (RGB) or "<name>.Y"
+        (monochrome), and the outlier cache's "outlier-i" images.  Any other name gets a PFM of the
+        image (little endian, bottom row first) and one PFM per layer, "<base>-<layer>.pfm".  The
+        metadata (with the error metrics and NaN warnings) goes to "<base>.json"."""
+        from . import imagefile
         name = filename or self.filename
         if not name:
             raise ValueError("no filename")
-        base = name.rsplit(".", 1)[0]
-        with open(base + ".pfm", "wb") as f:
-            f.write(b"PF\n%d %d\n-1.0\n" % (self.Width, self.Height))
-            f.write(np.ascontiguousarray(self.Image.data[::-1]).astype("<f4").tobytes())
+        base, ext = os.path.splitext(name)
+        images = [(n, layer.Image) for n, layer in self.layers.items() if layer.Image is not None]
+        if ext.lower() == ".exr":
+            ch = {}
+            for n, img in images + [(None, self.Image)]:
+                d = np.asarray(img.data, np.float32)
+                prefix = "" if n is None else n + "."
+                if d.ndim == 3 and d.shape[2] == 3:
+                    for c, k in zip("RGB", range(3)):
+                        ch[prefix + c] = d[:, :, k]
+                else:
+                    ch[prefix + "Y"] = d.reshape(self.Height, self.Width)
+            if self.OutlierCache is not None:
+                for i, img in enumerate(self.OutlierCache.outlier_layers()):
+                    ch[f"outlier-{i}.Y"] = img
+            imagefile.write_exr(name, ch)
+        else:
+            def pfm(path, d):
+                d = np.asarray(d, np.float32)
+                rgb = d.ndim == 3 and d.shape[2] == 3
+                with open(path, "wb") as f:
+                    f.write(b"%s\n%d %d\n-1.0\n" % (b"PF" if rgb else b"Pf", self.Width, self.Height))
+                    f.write(np.ascontiguousarray(d.reshape(self.Height, self.Width, -1)[::-1]).astype("<f4").tobytes())
+            pfm(base + ".pfm", self.Image.data)
+            for n, img in images:
+                pfm(f"{base}-{n}.pfm", img.data)
         meta = dict(self.MetaData)
+        if self.Errors:
+            meta["ErrorMetrics"] = [{"TimeMS": t, "MSE": a, "RelMSE": b, "RelMSE_Outlier": c} for (t, a, b, c) in self.Errors]
         meta["NaNWarnings"] = [{"Pixel": {"Col": c, "Row": r}, "Iteration": it} for (c, r, it) in self.NaNWarnings]
         with open(base + ".json", "w") as f:
             json.dump(meta, f, default=lambda o: o.__dict__ if hasattr(o, "__dict__") else str(o))
@@ -287,5 +358,20 @@ def rel_mse(image, reference, eps=1e-2):
     return float(np.mean((x - r) ** 2 / (r * r + eps)))
 
 
+def rel_mse_outlier_rejection(image, reference, percentage=0.1, eps=1e-2):
+    """Relative MSE without the worst pixels (SimpleImageIO's Metrics.RelMSE_OutlierRejection, not
+    vendored; this is the definition used here and by the GPU error metrics): each pixel's error is
+    its mean over the channels of (x - r)^2 / (r^2 + eps); the largest floor(pixels * percentage /
+    100) are dropped and the rest averaged."""
+    x = np.asarray(image, dtype=np.float32)
+    r = np.asarray(reference, dtype=np.float32)
+    d = (x - r).astype(np.float64)
+    r64 = r.astype(np.float64)
+    e = (d * d / (r64 * r64 + eps)).sum(axis=-1) / 3.0
+    e = np.sort(e.astype(np.float32).ravel())
+    k = int(e.size * percentage / 100)
+    return float(np.sum(e[:e.size - k], dtype=np.float64) / (e.size - k))
+
+
 __all__ = ["RgbColor", "RgbImage", "MonochromeImage", "TextureRgb", "TextureMono", "BorderHandling", "FrameBuffer",
-           "mean_rgb", "rel_mse"]
+           "OutlierReplayCache", "Pixel", "mean_rgb", "rel_mse", "rel_mse_outlier_rejection"]

@@ -11,7 +11,7 @@ from __future__ import annotations
 import numpy as np
 
 from . import _native
-from .images import MonochromeImage, RgbLayer
+from .images import MonochromeImage, OutlierReplayCache, RgbLayer
 
 
 class Integrator:
@@ -87,17 +87,23 @@ class PathTracer(Integrator):
         albedo = fb.layers["albedo"].Image.data if "albedo" in fb.layers else None
         normal = fb.layers["normal"].Image.data if "normal" in fb.layers else None
         var = fb.PixelVariance
-        if var is not None or fb.ReferenceImage is not None or albedo is not None:
+        if fb.CurIteration == 0 or fb.OutlierCache is None:
+            # FrameBuffer.Initialize (FrameBuffer.cs:229): a fresh cache with the first iteration
+            fb.OutlierCache = OutlierReplayCache(fb.Width, fb.Height, fb.NumOutliersToTrack)
+        oc = fb.OutlierCache
+        outliers = (oc.weight, oc.iteration) if oc.nMax > 0 else None
+        if var is not None or fb.ReferenceImage is not None or albedo is not None or outliers is not None:
             ref = None if fb.ReferenceImage is None else fb.ReferenceImage.data
             stats, vimg, avg, err = scene.native.render_layers(p, film.ctypes.data, variance_state=None if var is None else var.state,
-                                                               reference=ref, albedo=albedo, normal=normal)
+                                                               reference=ref, albedo=albedo, normal=normal, outliers=outliers)
             if var is not None:
                 var.Image = MonochromeImage(vimg)
                 var.Average = avg
             if err is not None:
                 # per-iteration times are not separable in the wavefront: the render time is prorated
                 n = int(stats.numIterations)
-                fb.Errors += [(int(round(stats.renderTimeMs * (k + 1) / max(n, 1))), float(err[k, 0]), float(err[k, 1]), None) for k in range(n)]
+                fb.Errors += [(int(round(stats.renderTimeMs * (k + 1) / max(n, 1))), float(err[k, 0]), float(err[k, 1]), float(err[k, 2]))
+                              for k in range(n)]
         else:
             stats = scene.native.render(p, film.ctypes.data)
         fb.CurIteration = fb.CurIteration + stats.numIterations

@@ -4,8 +4,10 @@ after every iteration (FrameBuffer.cs:276-277, 378-383) and the VarianceLayer
 import numpy as np
 import pytest
 
+from oracle import film_metrics as F
 from oracle import pyoracle as O
-from seesharp_gb300 import FrameBuffer, PathTracer, RgbImage, workloads
+from seesharp_gb300 import (DiffuseMaterial, EnvironmentMap, FrameBuffer, Matrix4x4, Mesh, PathTracer, PerspectiveCamera, Pixel, RgbColor,
+                            RgbImage, Scene, TextureRgb, workloads)
 
 pytestmark = pytest.mark.gpu
 
@@ -41,7 +43,35 @@ def test_error_metrics_equal_the_metrics_of_each_iterations_film():
         d = (film - ref).astype(np.float64)
         mse, rel = np.mean(d * d), np.mean(d * d / (r64 * r64 + 0.01))
         assert errs[k - 1][1] == pytest.approx(mse, rel=1e-9) and errs[k - 1][2] == pytest.approx(rel, rel=1e-9)
+        # the outlier-rejecting RelMSE: 3072 pixels, the largest 3 errors dropped
+        assert errs[k - 1][3] == pytest.approx(F.relmse_outlier_rejection(film, ref), rel=1e-9)
+        assert errs[k - 1][3] <= errs[k - 1][2] * (1 + 1e-9)
     assert errs[-1][2] < errs[0][2]
+
+
+@pytest.mark.parametrize("w,h", [(100, 80), (31, 17)])
+def test_outlier_rejecting_relmse_drops_the_fireflies(w, h):
+    """8000 pixels drop 8: a reference that is black at the 8 brightest pixels (the light) makes
+    those pixels' errors dominate the plain RelMSE, and the rejection removes them.  527 pixels
+    drop none (the plain RelMSE)."""
+    sc = workloads.cornell_box(w, h)
+    sc.Prepare()
+    ref = _render(sc, 64, seed=5)
+    bad = ref.copy()
+    if w * h >= 1000:
+        flat = bad.reshape(-1, 3)
+        flat[np.argsort(-ref.reshape(-1, 3).mean(axis=1))[:8]] = 0.0
+    fb = FrameBuffer(w, h)
+    fb.ReferenceImage = RgbImage(bad)
+    sc.FrameBuffer = fb
+    PathTracer(TotalSpp=2, MaxDepth=5).Render(sc)
+    film = fb.Image.data
+    got = fb.Errors[-1][3]
+    assert got == pytest.approx(F.relmse_outlier_rejection(film, bad), rel=1e-9)
+    if w * h >= 1000:
+        assert got < 0.5 * fb.Errors[-1][2]
+    else:
+        assert got == pytest.approx(fb.Errors[-1][2], rel=1e-6)
 
 
 def test_variance_layer_matches_the_oracle():
@@ -129,7 +159,8 @@ def test_denoiser_feature_layers_match_the_primary_hits():
 
 
 def test_layers_resume_like_the_film():
-    """Rendering 3 + 4 iterations equals rendering 7: film, variance layer and feature layers."""
+    """Rendering 3 + 4 iterations equals rendering 7: film, variance layer, feature layers and the
+    outlier replay cache."""
     def run(steps):
         sc = workloads.cornell_box(W, H)
         sc.FrameBuffer = FrameBuffer(W, H, flags=FrameBuffer.Flags.Recommended | FrameBuffer.Flags.EstimatePixelVariance)
@@ -137,6 +168,62 @@ def test_layers_resume_like_the_film():
         for s in steps:
             PathTracer(TotalSpp=s, MaxDepth=4).Render(sc)
         fb = sc.FrameBuffer
-        return fb.Image.data.copy(), fb.PixelVariance.Image.data.copy(), fb.PixelVariance.Average, fb.GetLayer("albedo").Image.data.copy()
+        return (fb.Image.data.copy(), fb.PixelVariance.Image.data.copy(), fb.PixelVariance.Average, fb.GetLayer("albedo").Image.data.copy(),
+                fb.OutlierCache.weight.copy(), fb.OutlierCache.iteration.copy())
     a, b = run([7]), run([3, 7])
     assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1]) and a[2] == b[2] and np.array_equal(a[3], b[3])
+    assert np.array_equal(a[4], b[4]) and np.array_equal(a[5], b[5])
+
+
+def test_outlier_cache_matches_the_oracle():
+    """OutlierReplayCache (OutlierReplayCache.cs:9-35): per pixel the 4 samples of largest channel
+    average, in the .NET heap's array order, against the oracle's restatement fed with the oracle's
+    per-iteration path values.  Pixels whose paths differ by an FP32 decision flip may disagree."""
+    S, w, h = 9, 40, 30
+    sc = workloads.cornell_box(w, h)
+    sc.Prepare()
+    sc.FrameBuffer.Reset()
+    PathTracer(TotalSpp=S, MaxDepth=5).Render(sc)
+    oc = sc.FrameBuffer.OutlierCache
+    o = O.OracleScene.from_scene(sc)
+    p = o.params(w, h, S, 5)
+    pix = np.arange(w * h, dtype=np.int32)
+    vals = np.stack([o.render_paths(p, it, pix)[0].reshape(h, w, 3) for it in range(S)])
+    ow, oi = F.outlier_cache(vals, 4)
+    same = np.all(oc.iteration == oi, axis=2) & np.all(np.abs(oc.weight - ow) <= 1e-4 * np.abs(ow) + 1e-6, axis=2)
+    assert same.mean() >= 0.97, same.mean()
+    assert (oc.iteration >= 0).all()  # 9 finite samples fill every heap
+    # the strongest sample of a pixel, looked up as OutlierCacheTest.cs:27-36 does
+    y, x = np.argwhere(same)[len(np.argwhere(same)) // 2]
+    q = oc.GetPixelOutlier(Pixel(int(x), int(y)))
+    best = max(q.UnorderedItems, key=lambda i: i.Priority)
+    assert q.Count == 4 and best.Element.Iteration == oi[y, x][np.argmax(ow[y, x])]
+
+
+def _constant_background_scene(w, h):
+    sc = Scene()
+    tri = Mesh([[-1, -1, 5], [1, -1, 5], [0, 1, 5]], [0, 1, 2])  # behind the camera
+    tri.Material = DiffuseMaterial(DiffuseMaterial.Parameters(BaseColor=TextureRgb(RgbColor(0.5, 0.5, 0.5))))
+    sc.Meshes.append(tri)
+    sc.Background = EnvironmentMap(RgbImage(np.tile(np.array([0.5, 0.25, 1.0], np.float32), (4, 8, 1))))
+    sc.Camera = PerspectiveCamera(Matrix4x4.CreateLookAt([0, 0, 0], [0, 0, -1], [0, 1, 0]), 50)
+    sc.FrameBuffer = FrameBuffer(w, h)
+    return sc
+
+
+@pytest.mark.parametrize("n", [0, 1, 4, 8])
+def test_outlier_cache_ties(n):
+    """Every camera ray escapes into a constant background, so every sample of every pixel has the
+    same value: the heap keeps the first n iterations in order (equal samples neither sift nor
+    replace the root)."""
+    S = 6
+    sc = _constant_background_scene(16, 12)
+    sc.FrameBuffer.NumOutliersToTrack = n
+    sc.Prepare()
+    PathTracer(TotalSpp=S, MaxDepth=3).Render(sc)
+    oc = sc.FrameBuffer.OutlierCache
+    assert np.allclose(sc.FrameBuffer.Image.data, np.array([0.5, 0.25, 1.0], np.float32), rtol=1e-6, atol=0)
+    want = [i if i < S else -1 for i in range(n)]
+    assert oc.iteration.shape == (12, 16, n) and np.all(oc.iteration == np.array(want, np.int32))
+    kept = oc.iteration >= 0
+    assert np.all(oc.weight[kept] == np.float32((np.float32(0.5) + np.float32(0.25) + np.float32(1.0)) / np.float32(3)))
