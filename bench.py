@@ -37,22 +37,31 @@ CONFIGS = {
             spp=512, depth=5, seed=571298512, recorded="CornellBox/References/MaxDepth5-Width512-Height512.json"),
 }
 CONFIGS[6] = dict(name="light_paths_sphere_field_1Mtri_262144paths_depth8", builder="lightpaths", spheres=200, W=1024, H=1024, paths=262144, depth=8)
+CONFIGS[7] = dict(name="batch_256smalljobs_10k-200ktri_64-256px_1-16spp_depth3-10", builder="batch", jobs=256, seed=7, tris=(1e4, 2e5),
+                  res=(64, 128, 256), spp=(1, 16), depth=(3, 10), scene_seed=5000)
 SCENE_DIR = os.path.join(ROOT, "tests", "golden", "scenes")
 
 
 def batch_jobs(cfg, seed_offset=0):
-    """The batched configuration: 64 jobs from the sphere-field generator with triangle counts
-    log-uniform in [10k, 1M], resolutions from {128, 256, 512, 1024} squared, spp U{4..64},
-    max depth U{3..10}."""
+    """The batched configurations: jobs from the sphere-field generator with triangle counts
+    log-uniform in cfg["tris"], square resolutions from cfg["res"], spp and max depth uniform over
+    the integer ranges cfg["spp"] and cfg["depth"].  Configuration 2 (uneven jobs): 64 jobs, [10k,
+    1M] triangles, 128..1024 pixels, 4..64 spp, depth 3..10.  Configuration 7 (serving-style small
+    jobs, none of which fills the GPU alone): 256 jobs, [10k, 200k] triangles, 64..256 pixels,
+    1..16 spp, depth 3..10."""
     from seesharp_gb300 import PathTracer, workloads
     rng = np.random.default_rng(cfg["seed"] + seed_offset)
+    lo, hi = cfg.get("tris", (1e4, 1e6))
+    res_choices = list(cfg.get("res", (128, 256, 512, 1024)))
+    spp_lo, spp_hi = cfg.get("spp", (4, 64))
+    d_lo, d_hi = cfg.get("depth", (3, 10))
     out = []
     for j in range(cfg["jobs"]):
-        tris = math.exp(rng.uniform(math.log(1e4), math.log(1e6)))
-        res = int(rng.choice([128, 256, 512, 1024]))
-        spp = int(rng.integers(4, 65))
-        depth = int(rng.integers(3, 11))
-        sc = workloads.sphere_field(max(2, int(round(tris / 5120))), res, res, seed=1000 + j)
+        tris = math.exp(rng.uniform(math.log(lo), math.log(hi)))
+        res = int(rng.choice(res_choices))
+        spp = int(rng.integers(spp_lo, spp_hi + 1))
+        depth = int(rng.integers(d_lo, d_hi + 1))
+        sc = workloads.sphere_field(max(2, int(round(tris / 5120))), res, res, seed=cfg.get("scene_seed", 1000) + j)
         out.append((sc, PathTracer(TotalSpp=spp, MaxDepth=depth)))
     return out
 
@@ -277,13 +286,33 @@ def make_scene(cfg):
 
 
 def scene_bytes(sc):
-    b = 0
+    """Bytes Scene.Prepare copies to the device: the packed triangle records (three float4
+    vertices, a float4 face normal, an int4 material/mesh/face record and an int4 of vertex ids:
+    96 bytes per triangle), the vertex normals and texture coordinates (for every vertex once any
+    mesh has them), image textures and the environment map."""
+    nt = sum(m.NumFaces for m in sc.Meshes)
+    nv = sum(m.NumVertices for m in sc.Meshes)
+    b = 96 * nt
+    b += 12 * nv if any(m.ShadingNormals is not None for m in sc.Meshes) else 0
+    b += 8 * nv if any(m.TextureCoordinates is not None for m in sc.Meshes) else 0
+    seen = set()
     for m in sc.Meshes:
-        b += m.Vertices.nbytes + m.Indices.nbytes
-        b += 0 if m.ShadingNormals is None else m.ShadingNormals.nbytes
-        b += 0 if m.TextureCoordinates is None else m.TextureCoordinates.nbytes
+        for t in vars(getattr(m.Material, "MaterialParameters", object())).values() if m.Material is not None else ():
+            img = getattr(t, "Image", None)
+            if img is not None and id(img) not in seen:
+                seen.add(id(img))
+                b += img.data.nbytes
     if sc.Background is not None:
         b += sc.Background.Image.data.nbytes
+    return int(b)
+
+
+def film_readback_bytes(fb):
+    """Bytes PathTracer.Render reads back into the frame buffer: the image, every layer and the
+    outlier replay cache."""
+    b = fb.Image.data.nbytes + sum(l.Image.data.nbytes for l in fb.layers.values() if l.Image is not None)
+    if fb.OutlierCache is not None:
+        b += fb.OutlierCache.weight.nbytes + fb.OutlierCache.iteration.nbytes
     return int(b)
 
 
@@ -416,9 +445,68 @@ def cpu_sample(cfg, seconds_target=15.0, min_paths=4096, nthreads=None, scene=No
     return n / dt / 1e6, f"{n} strided paths of iteration 1 ({n / npix:.3f} of one spp)", nthreads, o, p, n
 
 
+def run_reference_batch(args, cfg):
+    """The batched workloads on the CPU restatement: the reference renders jobs one after another,
+    so its throughput is the workload's samples over the sum of the jobs' times.  Bounded sample:
+    8 jobs drawn with probability proportional to their sample counts (seeded), and the same
+    number of strided paths of iteration 0 from each; the mean time per path of that sample
+    estimates the workload's mean time per sample."""
+    from oracle import pyoracle as O
+    pairs = batch_jobs(cfg)
+    sizes = np.array([sc.FrameBuffer.Width * sc.FrameBuffer.Height * pt.TotalSpp for sc, pt in pairs], np.float64)
+    pick = np.random.default_rng(cfg["seed"] + 99).choice(len(pairs), size=8, replace=True, p=sizes / sizes.sum())
+    nthreads = os.cpu_count() or 1
+    jobs = []
+    for j in pick:
+        sc, pt = pairs[int(j)]
+        o = O.OracleScene.from_scene(sc)
+        W, H = sc.FrameBuffer.Width, sc.FrameBuffer.Height
+        jobs.append((o, o.params(W, H, pt.TotalSpp, pt.MaxDepth), W * H))
+    per_job = 2048
+    o, p, npix = jobs[0]
+    t0 = time.perf_counter()
+    o.render_paths(p, 0, np.linspace(0, npix - 1, per_job).astype(np.int32), nthreads)
+    dt = max(time.perf_counter() - t0, 1e-6)
+    # size one step (all 8 jobs) for a few seconds of CPU work
+    per_job = int(max(1024, per_job * max(2.0, 60.0 / max(1, args.steps + args.warmup)) / (8 * dt)))
+
+    def step(it):
+        # per_job paths of each job: strided pixels of as many iterations as that takes
+        n = 0
+        for o, p, npix in jobs:
+            left, k = per_job, 0
+            while left > 0:
+                m = min(left, npix)
+                o.render_paths(p, it + k, np.linspace(0, npix - 1, m).astype(np.int32), nthreads)
+                left -= m
+                n += m
+                k += 1
+        return n
+    for w in range(args.warmup):
+        step(1000 * (w + 1))
+    t0 = time.perf_counter()
+    n = sum(step(100000 + 1000 * k) for k in range(args.steps))
+    dt = time.perf_counter() - t0
+    val = n / dt / 1e6
+    line = {
+        "metric": "Msamples/s PathTracer (batched jobs)", "value": round(val, 4), "unit": "Msamples/s", "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(dt / args.steps * 1000, 3), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scene generator)", "impl": "reference",
+        "config": {"workload": cfg["name"], "jobs": len(pairs)},
+        "cpu_baseline": {"value": round(val, 4), "unit": "Msamples/s", "cores": nthreads, "kind": "port",
+                         "sample": f"8 of the {len(pairs)} jobs drawn in proportion to their samples, {per_job} strided paths of each per step "
+                                   f"(consecutive iterations), C++ restatement of the reference PathTracer on {nthreads} host threads"},
+        "e2e": {"value": round(val, 4), "unit": "Msamples/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
 def run_reference(args, cfg):
     ws, rank, _ = dist_info()
     if rank != 0:
+        return
+    if cfg["builder"] == "batch":
+        run_reference_batch(args, cfg)
         return
     from seesharp_gb300 import workloads  # noqa: F401  (scene generator only)
     sc = make_scene(cfg)
@@ -512,7 +600,6 @@ def run_ours(args, cfg):
     from seesharp_gb300 import FrameBuffer
     e2e_steps = 0 if args.no_e2e else max(1, min(args.steps, 3))
     h2d = scene_bytes(sc)
-    d2h = W * H * 12
     barrier(ws)
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
@@ -521,6 +608,7 @@ def run_ours(args, cfg):
         PathTracer(TotalSpp=spp, MaxDepth=depth, BaseSeed=cfg.get("seed", 0xC030114)).Render(sc)
     e2e_s = max_over_ranks(ws, (time.perf_counter() - t0) / max(e2e_steps, 1))
     e2e_val = samples * ws / e2e_s / 1e6 if e2e_steps else None
+    d2h = film_readback_bytes(sc.FrameBuffer) if e2e_steps else W * H * 12
     if e2e_steps:
         assert np.isfinite(sc.FrameBuffer.Image.data).all()
 
@@ -558,7 +646,7 @@ def run_ours(args, cfg):
                        "width": W, "height": H, "spp": spp, "max_depth": depth, "l2": "256 MB buffer written between timed steps",
                        "parallelism": f"replicas x{ws}"},
             "e2e": {"value": None if e2e_val is None else round(e2e_val, 3), "unit": "Msamples/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                    "s_per_step": round(e2e_s, 4), "includes": "Scene.Prepare (upload + BVH build) + PathTracer.Render (film read-back)"},
+                    "s_per_step": round(e2e_s, 4), "includes": "Scene.Prepare (upload + BVH build) + PathTracer.Render (film, layers and outlier cache read back)"},
             "roofline": roofline,
             "bytes_per_sample": round(b_sample, 1), "rays_per_sample": round(ext, 4), "shadow_rays_per_sample": round(sh, 4),
             "gpu_launches": launches,

@@ -17,6 +17,7 @@
 #include <mutex>
 #include <stdexcept>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/sst.h"
@@ -86,8 +87,32 @@ struct DevBuf {
         ensure(std::max<size_t>(1, v.size() * sizeof(T)));
         if (!v.empty()) CUDA_CHECK(cudaMemcpyAsync(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, s));
     }
+    template <class T> void upload(const T* v, size_t n, cudaStream_t s) {
+        ensure(std::max<size_t>(1, n * sizeof(T)));
+        if (n) CUDA_CHECK(cudaMemcpyAsync(p, v, n * sizeof(T), cudaMemcpyHostToDevice, s));
+    }
     template <class T> T* as() const { return static_cast<T*>(p); }
 };
+
+// Runs fn(begin, end) over [0, n) in contiguous ranges on up to 16 host threads (one range per
+// thread, at least minPerThread items each).  fn must not throw.
+template <class F>
+static void parallelRanges(size_t n, size_t minPerThread, F fn) {
+    const size_t hw = std::max(1u, std::thread::hardware_concurrency());
+    const size_t nt = std::min<size_t>(std::min<size_t>(hw, 16), (n + minPerThread - 1) / std::max<size_t>(1, minPerThread));
+    if (nt <= 1) {
+        fn(size_t(0), n);
+        return;
+    }
+    const size_t chunk = (n + nt - 1) / nt;
+    std::vector<std::thread> th;
+    for (size_t t = 1; t < nt; ++t) {
+        size_t b = t * chunk, e = std::min(n, b + chunk);
+        if (b < e) th.emplace_back(fn, b, e);
+    }
+    fn(size_t(0), std::min(n, chunk));
+    for (auto& x : th) x.join();
+}
 
 // ---------------------------------------------------------------------------------------------
 // context
@@ -170,8 +195,19 @@ struct HostMesh {
     std::vector<float> V, N, UV;
     std::vector<int> I;
     int material = -1;
-    std::vector<float> faceN;  // 3 per face
 };
+// Normalized cross(v2 - v1, v3 - v1) of a face (the geometric normal, Triangle.cs:22-36).  One
+// out-of-line instance, so that the triangle records and the emitter table get the same bits.
+__attribute__((noinline)) static void faceNormal(const float* V, const int* I, size_t f, float out[3]) {
+    const float* a = &V[3 * size_t(I[3 * f])];
+    const float* b = &V[3 * size_t(I[3 * f + 1])];
+    const float* c = &V[3 * size_t(I[3 * f + 2])];
+    float e1[3] = {b[0] - a[0], b[1] - a[1], b[2] - a[2]}, e2[3] = {c[0] - a[0], c[1] - a[1], c[2] - a[2]};
+    float n[3] = {e1[1] * e2[2] - e1[2] * e2[1], e1[2] * e2[0] - e1[0] * e2[2], e1[0] * e2[1] - e1[1] * e2[0]};
+    float l = std::sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+    for (int k = 0; k < 3; ++k) out[k] = n[k] / l;
+}
+
 struct HostEmitter {
     int mesh, face;
     float rad[3];
@@ -463,33 +499,36 @@ static void commitScene(sst_scene* s, int W, int H) {
         if (triEmitter[g] >= 0) fail(SST_ERR_INVALID_SCENE, "two emitters on the same triangle");
         triEmitter[g] = int(e);
     }
-    // per-triangle records in global order
-    std::vector<float4> trivG(3 * size_t(nt)), triNG(nt);
-    std::vector<int4> auxG(nt), vtxG(nt);
-    {
-        int g = 0;
-        for (size_t mi = 0; mi < s->meshes.size(); ++mi) {
+    // per-triangle records in global order, packed by several host threads over triangle ranges
+    // (uninitialised arrays: every entry is written, and each thread touches its own pages first)
+    std::unique_ptr<float4[]> trivG(new float4[3 * size_t(nt)]), triNG(new float4[nt]);
+    std::unique_ptr<int4[]> auxG(new int4[nt]), vtxG(new int4[nt]);
+    parallelRanges(size_t(nt), 1 << 16, [&](size_t g0, size_t g1) {
+        size_t mi = size_t(std::upper_bound(s->meshTriOffset.begin(), s->meshTriOffset.end(), int(g0)) - s->meshTriOffset.begin()) - 1;
+        for (size_t g = g0; g < g1; ++g) {
+            while (mi + 1 < s->meshes.size() && int(g) >= s->meshTriOffset[mi + 1]) ++mi;
             const HostMesh& m = s->meshes[mi];
-            int vo = vtxOffset[mi];
-            int flags = (m.N.empty() ? 0 : 1) | (m.UV.empty() ? 0 : 2);
-            for (size_t f = 0; f < m.I.size() / 3; ++f, ++g) {
-                int i0 = m.I[3 * f], i1 = m.I[3 * f + 1], i2 = m.I[3 * f + 2];
-                const float* a = &m.V[3 * size_t(i0)];
-                const float* bb = &m.V[3 * size_t(i1)];
-                const float* c = &m.V[3 * size_t(i2)];
-                float gw;
-                std::memcpy(&gw, &g, 4);
-                trivG[3 * size_t(g)] = make_float4(a[0], a[1], a[2], gw);
-                trivG[3 * size_t(g) + 1] = make_float4(bb[0], bb[1], bb[2], 0.f);
-                trivG[3 * size_t(g) + 2] = make_float4(c[0], c[1], c[2], 0.f);
-                float ew;
-                std::memcpy(&ew, &triEmitter[g], 4);
-                triNG[g] = make_float4(m.faceN[3 * f], m.faceN[3 * f + 1], m.faceN[3 * f + 2], ew);
-                auxG[g] = make_int4(m.material, int(mi), int(f), flags);
-                vtxG[g] = make_int4(vo + i0, vo + i1, vo + i2, 0);
-            }
+            const size_t f = g - size_t(s->meshTriOffset[mi]);
+            const int vo = vtxOffset[mi];
+            const int flags = (m.N.empty() ? 0 : 1) | (m.UV.empty() ? 0 : 2);
+            int i0 = m.I[3 * f], i1 = m.I[3 * f + 1], i2 = m.I[3 * f + 2];
+            const float* a = &m.V[3 * size_t(i0)];
+            const float* bb = &m.V[3 * size_t(i1)];
+            const float* c = &m.V[3 * size_t(i2)];
+            int gi = int(g);
+            float gw;
+            std::memcpy(&gw, &gi, 4);
+            trivG[3 * g] = make_float4(a[0], a[1], a[2], gw);
+            trivG[3 * g + 1] = make_float4(bb[0], bb[1], bb[2], 0.f);
+            trivG[3 * g + 2] = make_float4(c[0], c[1], c[2], 0.f);
+            float ew, fn[3];
+            std::memcpy(&ew, &triEmitter[g], 4);
+            faceNormal(m.V.data(), m.I.data(), f, fn);
+            triNG[g] = make_float4(fn[0], fn[1], fn[2], ew);
+            auxG[g] = make_int4(m.material, int(mi), int(f), flags);
+            vtxG[g] = make_int4(vo + i0, vo + i1, vo + i2, 0);
         }
-    }
+    });
     const char* bvhEnv = getenv("SST_BVH");
     bool hostBuild = bvhEnv && std::string(bvhEnv) == "sah";
     s->triv.ensure(std::max<size_t>(1, sizeof(float4) * 3 * size_t(nt)));
@@ -499,10 +538,10 @@ static void commitScene(sst_scene* s, int W, int H) {
     if (!hostBuild && nt > 0) {
         // GPU linear BVH (sst_bvh.cu) and a leaf-order gather on the device
         DevBuf gTriv, gTriN, gAux, gVtx, order, scratch;
-        gTriv.upload(trivG, st);
-        gTriN.upload(triNG, st);
-        gAux.upload(auxG, st);
-        gVtx.upload(vtxG, st);
+        gTriv.upload(trivG.get(), 3 * size_t(nt), st);
+        gTriN.upload(triNG.get(), size_t(nt), st);
+        gAux.upload(auxG.get(), size_t(nt), st);
+        gVtx.upload(vtxG.get(), size_t(nt), st);
         s->nodes.ensure(sizeof(float4) * 4 * size_t(std::max(1, nt - 1)));
         order.ensure(sizeof(int) * size_t(nt));
         size_t sb = lbvhScratchBytes(nt);
@@ -600,7 +639,9 @@ static void commitScene(sst_scene* s, int W, int H) {
         for (int k = 0; k < 3; ++k) { e1[k] = p[1][k] - p[0][k]; e2[k] = p[2][k] - p[0][k]; }
         float cx = e1[1] * e2[2] - e1[2] * e2[1], cy = e1[2] * e2[0] - e1[0] * e2[2], cz = e1[0] * e2[1] - e1[1] * e2[0];
         float area = std::sqrt(cx * cx + cy * cy + cz * cz) * 0.5f;
-        d.faceN = make_float4(m.faceN[3 * f], m.faceN[3 * f + 1], m.faceN[3 * f + 2], 1.0f / area);
+        float fn[3];
+        faceNormal(m.V.data(), m.I.data(), size_t(f), fn);
+        d.faceN = make_float4(fn[0], fn[1], fn[2], 1.0f / area);
         d.rad = make_float4(he.rad[0], he.rad[1], he.rad[2], he.exponent);
         d.norm = (he.exponent + 1.0f) / (2.0f * 3.14159265f);  // GlossyEmitter.cs:14
         d.globalTri = s->meshTriOffset[he.mesh] + f;
@@ -1249,21 +1290,20 @@ int sst_scene_add_mesh(sst_scene* s, const float* V, int32_t nV, const int32_t* 
         HostMesh m;
         m.V.assign(V, V + 3 * size_t(nV));
         m.I.assign(I, I + 3 * size_t(nT));
-        for (int32_t k = 0; k < 3 * nT; ++k)
-            if (m.I[k] < 0 || m.I[k] >= nV) fail(SST_ERR_INVALID_ARGUMENT, "vertex index out of range");
         if (N) m.N.assign(N, N + 3 * size_t(nV));
         if (UV) m.UV.assign(UV, UV + 2 * size_t(nV));
         m.material = material;
-        m.faceN.resize(3 * size_t(nT));
-        for (int f = 0; f < nT; ++f) {  // normalized cross(v2 - v1, v3 - v1)
-            const float* a = &m.V[3 * size_t(m.I[3 * f])];
-            const float* b = &m.V[3 * size_t(m.I[3 * f + 1])];
-            const float* c = &m.V[3 * size_t(m.I[3 * f + 2])];
-            float e1[3] = {b[0] - a[0], b[1] - a[1], b[2] - a[2]}, e2[3] = {c[0] - a[0], c[1] - a[1], c[2] - a[2]};
-            float n[3] = {e1[1] * e2[2] - e1[2] * e2[1], e1[2] * e2[0] - e1[0] * e2[2], e1[0] * e2[1] - e1[1] * e2[0]};
-            float l = std::sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
-            for (int k = 0; k < 3; ++k) m.faceN[3 * size_t(f) + k] = n[k] / l;
-        }
+        std::mutex badLock;
+        bool anyBad = false;
+        parallelRanges(size_t(nT) * 3, 1 << 18, [&](size_t k0, size_t k1) {
+            bool rangeBad = false;
+            for (size_t k = k0; k < k1; ++k) rangeBad |= m.I[k] < 0 || m.I[k] >= nV;
+            if (rangeBad) {
+                std::lock_guard<std::mutex> g(badLock);
+                anyBad = true;
+            }
+        });
+        if (anyBad) fail(SST_ERR_INVALID_ARGUMENT, "vertex index out of range");
         s->meshes.push_back(std::move(m));
         s->committed = false;
         *out = int(s->meshes.size()) - 1;
