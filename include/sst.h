@@ -262,7 +262,13 @@ int sst_trace_light_paths(sst_scene* scene, uint32_t seed, uint32_t iteration, i
  *    strength and of the shading normal;
  *  - the OutlierReplayCache (Integrators/Util/OutlierReplayCache.cs:9-35, notified by
  *    FrameBuffer.Splat, FrameBuffer.cs:187-190): per pixel the numOutliers samples of largest channel
- *    average with their iteration, in the array order of .NET's 4-ary PriorityQueue min-heap.
+ *    average with their iteration, in the array order of .NET's 4-ary PriorityQueue min-heap;
+ *  - the technique pyramids of PathTracer.RenderTechniquePyramid (PathTracer.cs:73-82, 204-266,
+ *    Integrators/Bidir/TechPyramid.cs): every sample that RegisterSample would log (emitter and
+ *    background hits of length d, visible next-event samples of length d), divided by TotalSpp, summed
+ *    per technique image, raw and times its MIS weight.  48 * maxDepth bytes of device memory per
+ *    pixel; not cumulative over calls.  A next-event sample whose MIS-weighted contribution is zero
+ *    is not logged (the reference logs it with its raw contribution; this needs a zero MIS weight).
  * The running means and the heaps resume like the film: when firstIteration > 0 the state arrays
  * hold the layers after iteration firstIteration and are read, and they are always written back. */
 typedef struct SstFilmLayers {
@@ -279,6 +285,9 @@ typedef struct SstFilmLayers {
     int32_t numOutliers;    /* OutlierReplayCache capacity per pixel, 0..8 (FrameBuffer.NumOutliersToTrack; 0: none) */
     float* outlierWeight;   /* in/out: width*height*numOutliers heap priorities (the sample's channel average) */
     int32_t* outlierIteration; /* in/out: width*height*numOutliers heap elements (0-based iteration, -1: empty) */
+    float* techPyramid;     /* out: the technique pyramids of this call, or NULL: 2 * 2*maxDepth images of
+                               width*height*3, the raw ones, then the MIS-weighted ones; image 2(d-1) is
+                               "{d}-hit", image 2(d-1)+1 "{d}-next-event" (unused for d = 1) */
 } SstFilmLayers;
 /* sst_render that also fills the requested layers. */
 int sst_render_layers(sst_scene* scene, const SstPathTracerParams* params, float* film, int32_t memory, const SstFilmLayers* layers,

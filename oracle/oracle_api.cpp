@@ -237,6 +237,47 @@ int ora_render(void* p, const PTParams* P, float* film, int nthreads, uint64_t* 
     return 0;
 }
 
+// The PathTracer's technique pyramids (RenderTechniquePyramid, PathTracer.cs:73-82, 204-266;
+// Integrators/Bidir/TechPyramid.cs): every registered sample, divided by TotalSpp, is added to the
+// image of its technique, "{d}-hit" (layer 2(d-1)) or "{d}-next-event" (layer 2(d-1)+1), in the
+// raw pyramid (pyr) and, times its MIS weight, in the weighted one (pyr + 2*maxDepth layers).
+// Iterations [iterFirst, iterFirst + iterCount), pixels in order, on one thread (the reference's
+// per-pixel order of additions).  pyr: 2 * 2*maxDepth * W*H*3 floats, accumulated into.
+namespace {
+struct PyramidLog : SampleLog<float> {
+    float* pyr;
+    size_t P;
+    int layers, pixel;
+    float spp;
+    void Register(int depth, bool nextEvent, const Rgb<float>& weight, float mis) override {
+        Rgb<float> w(weight.r / spp, weight.g / spp, weight.b / spp);
+        int L = 2 * (depth - 1) + (nextEvent ? 1 : 0);
+        float* a = pyr + (size_t(L) * P + size_t(pixel)) * 3;
+        float* b = pyr + (size_t(layers + L) * P + size_t(pixel)) * 3;
+        a[0] += w.r; a[1] += w.g; a[2] += w.b;
+        Rgb<float> m = w * mis;
+        b[0] += m.r; b[1] += m.g; b[2] += m.b;
+    }
+};
+}  // namespace
+
+int ora_render_pyramid(void* p, const PTParams* P, int iterFirst, int iterCount, float* pyr) {
+    Handle* H = static_cast<Handle*>(p);
+    if (H->fp64) return -1;
+    PyramidLog log;
+    log.pyr = pyr;
+    log.P = size_t(P->width) * P->height;
+    log.layers = 2 * P->maxDepth;
+    log.spp = float(P->totalSpp);
+    for (int it = iterFirst; it < iterFirst + iterCount; ++it)
+        for (uint32_t pix = 0; pix < uint32_t(log.P); ++pix) {
+            log.pixel = int(pix);
+            Rng rng(P->baseSeed, pix, uint32_t(it));
+            RenderPixel(H->s32, *P, pix / uint32_t(P->width), pix % uint32_t(P->width), rng, nullptr, &log);
+        }
+    return 0;
+}
+
 // Radiance of individual paths: rgb[3*i] for pixel index pixels[i] and the given sample index.
 int ora_render_paths(void* p, const PTParams* P, uint32_t sampleIndex, const int* pixels, int n, float* rgb, uint64_t* stats, int nthreads) {
     Handle* H = static_cast<Handle*>(p);

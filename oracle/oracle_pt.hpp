@@ -865,9 +865,19 @@ template <class T> inline T SurfaceAreaToSolidAngle(const SurfacePoint<T>& from,
     return std::fabs(dot(to.normal, -d)) / (dsq * std::sqrt(dsq));
 }
 
+// PathTracerBase.RegisterSample (PathTracer.cs:73-82): called once per complete path sample with
+// its length (edges), whether it is a next-event sample, its contribution (the reference's
+// `contrib * state.PrefixWeight`; for next-event samples without the Russian-roulette division
+// that the radiance estimate applies) and its MIS weight.  The technique pyramid is built from it.
+template <class T> struct SampleLog {
+    virtual void Register(int depth, bool nextEvent, const Rgb<T>& weight, T mis) = 0;
+    virtual ~SampleLog() = default;
+};
+
 // PathTracerBase.RenderPixel + EstimateIncidentRadiance (PathTracer.cs:287-382) for one
 // (pixel, sample).  Returns the radiance estimate that RenderPixel splats.
-template <class T> Rgb<T> RenderPixel(const Scene<T>& sc, const PTParams& P, uint32_t row, uint32_t col, Rng& rng, PathStats* stats) {
+template <class T> Rgb<T> RenderPixel(const Scene<T>& sc, const PTParams& P, uint32_t row, uint32_t col, Rng& rng, PathStats* stats,
+                                      SampleLog<T>* log = nullptr) {
     const int nEm = int(sc.emitters.size());
     const T nShadow = T(P.numShadowRays);
     V2<float> off = rng.NextFloat2D();  // :289
@@ -893,6 +903,7 @@ template <class T> Rgb<T> RenderPixel(const Scene<T>& sc, const PTParams& P, uin
                     mis = T(1) / (T(1) + pdfNE / prevPdf);
                 }
                 Rgb<T> em = sc.env->EmittedRadiance(ray.dir);
+                if (log) log->Register(int(depth), false, em * prefix, mis);  // :397
                 radiance = radiance + prefix * mis * em;
             }
             break;
@@ -913,6 +924,7 @@ template <class T> Rgb<T> RenderPixel(const Scene<T>& sc, const PTParams& P, uin
                 if (!P.enableBsdfDI) mis = T(0);
             }
             Rgb<T> em = light.EmittedRadiance(hit, -ray.dir);
+            if (log) log->Register(int(depth), false, em * prefix, mis);  // :418
             radiance = radiance + prefix * mis * em;
         }
 
@@ -935,6 +947,7 @@ template <class T> Rgb<T> RenderPixel(const Scene<T>& sc, const PTParams& P, uin
                         if (!(pdfBsdf == T(0) || bs.Pdf == T(0))) {
                             T mis = P.enableBsdfDI ? T(1) / (T(1) + pdfBsdf / (bs.Pdf * nShadow)) : T(1);
                             Rgb<T> contrib = bs.Weight * bsdfCos / nShadow;
+                            if (log) log->Register(int(depth) + 1, true, contrib * prefix, mis);  // :443
                             nee = nee + mis * contrib;
                         }
                     }
@@ -960,6 +973,7 @@ template <class T> Rgb<T> RenderPixel(const Scene<T>& sc, const PTParams& P, uin
                             T mis = P.enableBsdfDI ? T(1) / (ratio + T(1)) : T(1);
                             T pdf = light.invArea / jac * selProb * nShadow;
                             Rgb<T> contrib = em / pdf * bsdfCos;
+                            if (log) log->Register(int(depth) + 1, true, contrib * prefix, mis);  // :492
                             nee = nee + mis * contrib;
                         }
                     }

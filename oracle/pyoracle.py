@@ -42,6 +42,7 @@ def lib():
         L.ora_bvh_nodes.argtypes = [vp]
         L.ora_render.argtypes = [vp, ctypes.POINTER(PTParams), vp, i, vp, i, i]
         L.ora_render_paths.argtypes = [vp, ctypes.POINTER(PTParams), u32, vp, i, vp, vp, i]
+        L.ora_render_pyramid.argtypes = [vp, ctypes.POINTER(PTParams), i, i, vp]
         L.ora_trace.argtypes = [vp, vp, i, vp, i]
         L.ora_trace_brute64.argtypes = [vp, vp, i, vp, vp]
         L.ora_camera_ray.argtypes = [vp, f, f, vp, vp]
@@ -191,6 +192,16 @@ class OracleScene:
         stats = np.zeros(2, np.uint64)
         self.L.ora_render_paths(self.h, ctypes.byref(params), int(sample_index), _p(pixels), pixels.size, _p(rgb), _p(stats), int(nthreads))
         return rgb, int(stats[0]), int(stats[1])
+
+    def render_pyramid(self, params, iter_first=0, iter_count=None):
+        """The raw and MIS-weighted technique pyramids (PathTracer.RenderTechniquePyramid) of
+        iterations [iter_first, iter_first + iter_count): float32 (2, 2*maxDepth, H, W, 3); layer
+        2(d-1) is "{d}-hit", 2(d-1)+1 "{d}-next-event"."""
+        n = params.totalSpp - iter_first if iter_count is None else iter_count
+        pyr = np.zeros((2, 2 * params.maxDepth, params.height, params.width, 3), np.float32)
+        if self.L.ora_render_pyramid(self.h, ctypes.byref(params), int(iter_first), int(n), _p(pyr)) != 0:
+            raise RuntimeError("the technique pyramid is computed in FP32 only")
+        return pyr
 
     def trace(self, rays, any_hit=False):
         rays = f32(rays, (-1, 8))

@@ -80,7 +80,8 @@ class SstTuning(ctypes.Structure):
 class SstFilmLayers(ctypes.Structure):
     _fields_ = [("variance", ctypes.c_void_p), ("varianceAverage", ctypes.c_void_p), ("varianceState", ctypes.c_void_p), ("reference", ctypes.c_void_p),
                 ("errors", ctypes.c_void_p), ("albedo", ctypes.c_void_p), ("normal", ctypes.c_void_p), ("memory", ctypes.c_int32),
-                ("numOutliers", ctypes.c_int32), ("outlierWeight", ctypes.c_void_p), ("outlierIteration", ctypes.c_void_p)]
+                ("numOutliers", ctypes.c_int32), ("outlierWeight", ctypes.c_void_p), ("outlierIteration", ctypes.c_void_p),
+                ("techPyramid", ctypes.c_void_p)]
 
 
 class SstCamera(ctypes.Structure):
@@ -384,10 +385,11 @@ class SceneHandle:
         check(self.lib.sst_occluded_noalloc(self.handle, ptr(rays), rays.shape[0], ptr(occ), SST_MEM_HOST))
         return occ
 
-    def render_layers(self, params, film, variance_state=None, reference=None, albedo=None, normal=None, outliers=None):
+    def render_layers(self, params, film, variance_state=None, reference=None, albedo=None, normal=None, outliers=None, pyramid=None):
         """sst_render_layers into a host film.  variance_state: (2, H, W) float32 running means (in/out)
         or None; albedo / normal: (H, W, 3) float32 layers (in/out) or None; outliers: a pair of
-        (H, W, n) float32 heap priorities and int32 heap iterations (in/out) or None.  Returns (stats,
+        (H, W, n) float32 heap priorities and int32 heap iterations (in/out) or None; pyramid: a
+        float32 (2, 2*maxDepth, H, W, 3) array for the technique pyramids (out) or None.  Returns (stats,
         variance image or None, variance average or None, (iterations of this call, 3) array of
         (MSE, RelMSE, RelMSE_Outlier) or None)."""
         W, H = params.width, params.height
@@ -398,10 +400,12 @@ class SceneHandle:
         err = np.zeros((max(0, params.totalSpp - params.firstIteration), 3), np.float64) if reference is not None else None
         ow, oi = outliers if outliers is not None else (None, None)
         for name, arr in (("variance", var), ("varianceAverage", avg), ("varianceState", variance_state), ("reference", ref), ("errors", err),
-                          ("albedo", albedo), ("normal", normal), ("outlierWeight", ow), ("outlierIteration", oi)):
+                          ("albedo", albedo), ("normal", normal), ("outlierWeight", ow), ("outlierIteration", oi), ("techPyramid", pyramid)):
             if arr is not None:
                 assert arr.flags["C_CONTIGUOUS"]
                 setattr(L, name, arr.ctypes.data)
+        if pyramid is not None:
+            assert pyramid.dtype == np.float32 and pyramid.shape == (2, 2 * params.maxDepth, H, W, 3)
         if outliers is not None:
             assert ow.dtype == np.float32 and oi.dtype == np.int32 and ow.shape == oi.shape == (H, W, ow.shape[2])
             L.numOutliers = ow.shape[2]

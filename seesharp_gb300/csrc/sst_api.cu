@@ -142,7 +142,7 @@ struct sst_ctx {
     // light paths (sst_trace_light_paths)
     DevBuf lightA[9], lightB[9], lightHits, lightVerts, lightLengths, lightCnt;
     // frame-buffer layers (sst_render_layers)
-    DevBuf layMean, layRef, layErr, layVar, laySum, layAlb, layNrm, aovSamples, layErrPix, layTrim, layOutW, layOutIt;
+    DevBuf layMean, layRef, layErr, layVar, laySum, layAlb, layNrm, aovSamples, layErrPix, layTrim, layOutW, layOutIt, layPyr, pyrG;
     // batched adjoint: the jobs of the last sst_forward_batch, their path radiance, dLoss/dImage
     std::vector<BatchSig> batchSig;
     std::vector<std::unique_ptr<DevBuf>> batchRecord, batchDLdI;
@@ -892,9 +892,15 @@ static void renderJobs(sst_ctx* c, std::vector<JobIn>& jobs, SstRenderStats* out
     for (auto& j : jobs)
         for (auto& m : j.s->materials) generic |= m.type == kGeneric;
     // per-item samples of the denoiser feature layers (written by the first shade, read by the fold)
-    bool anyAov = false;
-    for (auto& j : jobs) anyAov |= j.lay.aovAlbedo != nullptr;
+    bool anyAov = false, pyramid = false;
+    for (auto& j : jobs) {
+        anyAov |= j.lay.aovAlbedo != nullptr;
+        pyramid |= j.lay.pyr != nullptr;
+    }
     if (anyAov) c->aovSamples.ensure(size_t(w.wb.cap) * 24);
+    if (pyramid && replay) fail(SST_ERR_UNSUPPORTED, "the technique pyramid is not available in the adjoint replay");
+    // technique pyramid: the payload of every NEE slot
+    if (pyramid) c->pyrG.ensure(size_t(w.wb.cap) * 16 * 2 * ns);
     // job table
     std::vector<DevJob> hj(jobs.size());
     for (size_t k = 0; k < jobs.size(); ++k) {
@@ -943,8 +949,13 @@ static void renderJobs(sst_ctx* c, std::vector<JobIn>& jobs, SstRenderStats* out
             }
             {
                 KTimer kt(c, 2);
-                launch_shade(ns, replay, generic, dj, A, B, w.wb.hits, w.wb.nee, w.wb.neeG, w.wb.cap, w.wb.shRo, w.wb.shRd, w.wb.shTgt, w.wb.shJob,
-                             cnt + kCntQueue + d, cnt + kCntQueue + d + 1, cnt + kCntShadow + d, c->samples.as<float>(), dstats, maxItems, st);
+                if (pyramid)
+                    launch_shade_pyramid(ns, dj, A, B, w.wb.hits, w.wb.nee, w.wb.cap, w.wb.shRo, w.wb.shRd, w.wb.shTgt, w.wb.shJob, cnt + kCntQueue + d,
+                                         cnt + kCntQueue + d + 1, cnt + kCntShadow + d, c->samples.as<float>(), dstats,
+                                         PyrArgs{dch, dwv, dcur, c->pyrG.as<float4>()}, maxItems, st);
+                else
+                    launch_shade(ns, replay, generic, dj, A, B, w.wb.hits, w.wb.nee, w.wb.neeG, w.wb.cap, w.wb.shRo, w.wb.shRd, w.wb.shTgt, w.wb.shJob,
+                                 cnt + kCntQueue + d, cnt + kCntQueue + d + 1, cnt + kCntShadow + d, c->samples.as<float>(), dstats, maxItems, st);
             }
             {
                 KTimer kt(c, 3);
@@ -1687,6 +1698,14 @@ int sst_render_layers(sst_scene* s, const SstPathTracerParams* p, float* film, i
                 lay.errFirst = first;
             }
         }
+        if (L->techPyramid) {
+            // technique pyramids of this call (the reference creates them anew in every Render)
+            const size_t bytes = 2 * 2 * size_t(p->maxDepth) * P * 12;
+            c->layPyr.ensure(bytes);
+            CUDA_CHECK(cudaMemsetAsync(c->layPyr.p, 0, bytes, st));
+            lay.pyr = c->layPyr.as<float>();
+            lay.pyrSpp = p->totalSpp;
+        }
         const int nOut = L->numOutliers;
         if (nOut > 0) {
             // OutlierReplayCache: created empty with the frame buffer's first iteration, kept after that
@@ -1705,6 +1724,7 @@ int sst_render_layers(sst_scene* s, const SstPathTracerParams* p, float* film, i
             lay.outIt = c->layOutIt.as<int>();
         }
         if (first < S) renderJobs(c, jobs, &local);
+        if (L->techPyramid) CUDA_CHECK(cudaMemcpyAsync(L->techPyramid, lay.pyr, 2 * 2 * size_t(p->maxDepth) * P * 12, out, st));
         if (nOut > 0) {
             const size_t n = P * size_t(nOut);
             CUDA_CHECK(cudaMemcpyAsync(L->outlierWeight, lay.outW, n * 4, out, st));

@@ -570,4 +570,14 @@ SST_D void cameraRay(const DevCamera& c, float fx, float fy, float3& org, float3
     dir = normalize(d);
 }
 
+// Last chunk of a wave with itemOffset <= item (the chunks are sorted by itemOffset).
+__device__ __forceinline__ int findChunk(const WaveChunk* ch, int lo, int hi, int item) {
+    // last chunk with itemOffset <= item (chunks are sorted by itemOffset)
+    while (hi - lo > 1) {
+        int mid = (lo + hi) >> 1;
+        if (ch[mid].itemOffset <= item) lo = mid; else hi = mid;
+    }
+    return lo;
+}
+
 }  // namespace sst

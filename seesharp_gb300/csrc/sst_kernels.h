@@ -39,6 +39,10 @@ void launch_trace_query(const TraceTuning& t, const DevJob* jobs, const float4* 
 void launch_shade(int ns, bool adj, bool generic, const DevJob* jobs, const PathBuf& A, const PathBuf& B, const float4* hits, float4* nee,
                   float4* neeG, int cap, float4* shRo, float4* shRd, int* shTgt, uint32_t* shJob, const int* nIn, int* nOut, int* nSh, float* samples,
                   DevStats* stats, int maxItems, cudaStream_t s);
+// k_shade with the technique pyramids (sst_pyramid.cu); the generic-material variant, no adjoint.
+void launch_shade_pyramid(int ns, const DevJob* jobs, const PathBuf& A, const PathBuf& B, const float4* hits, float4* nee, int cap, float4* shRo,
+                          float4* shRd, int* shTgt, uint32_t* shJob, const int* nIn, int* nOut, int* nSh, float* samples, DevStats* stats,
+                          const PyrArgs& pyr, int maxItems, cudaStream_t s);
 void launch_debug_material_eval(const DevScene& sc, int mat, int n, const float* pts, const float* outs, const float* ins, float* vals, float* pdfs,
                                 cudaStream_t s);
 void launch_debug_material_sample(const DevScene& sc, int mat, int n, const float* pts, const float* outs, const float* us, float* dirs, float* pdfs,

@@ -141,6 +141,9 @@ struct DevLayers {
     int nOut;           // OutlierReplayCache heap capacity per pixel (0: not tracked), at most kMaxOutliers
     float* outW;        // W*H*nOut heap priorities: the sample's channel average, 4-ary min-heap order
     int* outIt;         // W*H*nOut heap elements: the sample's 0-based iteration, -1 for an empty slot
+    float* pyr;         // technique pyramids (raw, then MIS-weighted): 2 * 2*maxDepth layers of W*H*3;
+                        // layer 2(d-1) is "{d}-hit", 2(d-1)+1 "{d}-next-event"
+    int pyrSpp;         // TotalSpp: every registered sample is divided by it
 };
 constexpr int kMaxOutliers = 8;
 
@@ -166,6 +169,17 @@ struct WaveChunk {
     int foldOffset;
     int pad;
     float* film;
+};
+
+// Technique-pyramid arguments of the shade kernel: the wave's chunk table (to map a wave item to
+// its pixel) and the payload of each queued next-event sample (its contribution and MIS weight,
+// added to the pyramid once the shadow ray has found it visible).
+struct WaveDesc;
+struct PyrArgs {
+    const WaveChunk* chunks;
+    const WaveDesc* waves;
+    const int* curWave;
+    float4* pyrG;  // one per NEE slot
 };
 
 // Per-wave parameters read by the kernels from device memory, so that the same kernel sequence

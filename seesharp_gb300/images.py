@@ -275,6 +275,13 @@ class FrameBuffer:
             self.PixelVariance = VarianceLayer()
             self.AddLayer("variance", self.PixelVariance)
 
+    @property
+    def Basename(self):
+        """FrameBuffer.Basename (FrameBuffer.cs:79-87): the image file's path without its extension."""
+        if not self.filename:
+            return ""
+        return os.path.join(os.path.dirname(self.filename), os.path.splitext(os.path.basename(self.filename))[0])
+
     def AddLayer(self, name, layer):
         """FrameBuffer.AddLayer (FrameBuffer.cs:60): the layer is initialised to the buffer's size."""
         layer.Init(self.Width, self.Height)

@@ -8,10 +8,12 @@ run Python code per path (the reference's hooks at PathTracer.cs:277-530).
 """
 from __future__ import annotations
 
+import os
+
 import numpy as np
 
 from . import _native
-from .images import MonochromeImage, OutlierReplayCache, RgbLayer
+from .images import MonochromeImage, OutlierReplayCache, RgbImage, RgbLayer
 
 
 class Integrator:
@@ -60,8 +62,6 @@ class PathTracer(Integrator):
         for name in _BEHAVIOUR_HOOKS:
             if getattr(type(self), name) is not getattr(PathTracer, name):
                 raise NotImplementedError(f"PathTracer.{name} is overridden; the GPU path tracer runs the reference behaviour only")
-        if self.RenderTechniquePyramid:
-            raise NotImplementedError("RenderTechniquePyramid is not supported by the GPU path tracer")
 
     def params(self, scene):
         fb = scene.FrameBuffer
@@ -87,15 +87,19 @@ class PathTracer(Integrator):
         albedo = fb.layers["albedo"].Image.data if "albedo" in fb.layers else None
         normal = fb.layers["normal"].Image.data if "normal" in fb.layers else None
         var = fb.PixelVariance
+        pyramid = None
+        if self.RenderTechniquePyramid:
+            # PathTracer.cs:204-209: new pyramids for every Render call
+            pyramid = np.zeros((2, 2 * int(self.MaxDepth), fb.Height, fb.Width, 3), np.float32)
         if fb.CurIteration == 0 or fb.OutlierCache is None:
             # FrameBuffer.Initialize (FrameBuffer.cs:229): a fresh cache with the first iteration
             fb.OutlierCache = OutlierReplayCache(fb.Width, fb.Height, fb.NumOutliersToTrack)
         oc = fb.OutlierCache
         outliers = (oc.weight, oc.iteration) if oc.nMax > 0 else None
-        if var is not None or fb.ReferenceImage is not None or albedo is not None or outliers is not None:
+        if var is not None or fb.ReferenceImage is not None or albedo is not None or outliers is not None or pyramid is not None:
             ref = None if fb.ReferenceImage is None else fb.ReferenceImage.data
             stats, vimg, avg, err = scene.native.render_layers(p, film.ctypes.data, variance_state=None if var is None else var.state,
-                                                               reference=ref, albedo=albedo, normal=normal, outliers=outliers)
+                                                               reference=ref, albedo=albedo, normal=normal, outliers=outliers, pyramid=pyramid)
             if var is not None:
                 var.Image = MonochromeImage(vimg)
                 var.Average = avg
@@ -117,6 +121,52 @@ class PathTracer(Integrator):
                 fb.NaNWarnings.append((px % fb.Width, px // fb.Width, stats.nanIteration[k]))
         fb.MetaData["NumNaNOrInf"] = int(stats.numNanOrInf)
         self.last_stats = stats
+        if pyramid is not None:
+            # PathTracer.cs:261-266
+            self.techPyramidRaw = TechPyramid(int(self.MinDepth), int(self.MaxDepth), pyramid[0])
+            self.techPyramidWeighted = TechPyramid(int(self.MinDepth), int(self.MaxDepth), pyramid[1])
+            self.techPyramidRaw.WriteToFiles(os.path.join(fb.Basename, "techs-raw"))
+            self.techPyramidWeighted.WriteToFiles(os.path.join(fb.Basename, "techs-weighted"))
+
+
+class TechPyramid:
+    """Integrators/Bidir/TechPyramid.cs as the PathTracer builds it (no merges, connections or light
+    tracing): per path length d in [minDepth, maxDepth] the images of the techniques "{d}-hit" and,
+    for d >= 2, "{d}-next-event".  `layers` is one pyramid as the GPU fills it, (2*maxDepth, H, W, 3)
+    with layer 2(d-1) the hit technique and 2(d-1)+1 the next-event one."""
+
+    def __init__(self, minDepth, maxDepth, layers):
+        self.minDepth, self.maxDepth = int(minDepth), int(maxDepth)
+        self.techniqueNames = {}
+        self.techniqueImages = {}
+        for depth in range(self.minDepth, self.maxDepth + 1):
+            self.techniqueNames[(depth, 0, depth)] = f"{depth}-hit"
+            self.techniqueImages[(depth, 0, depth)] = RgbImage(np.ascontiguousarray(layers[2 * (depth - 1)]))
+            if depth == 1:
+                continue
+            self.techniqueNames[(depth - 1, 0, depth)] = f"{depth}-next-event"
+            self.techniqueImages[(depth - 1, 0, depth)] = RgbImage(np.ascontiguousarray(layers[2 * (depth - 1) + 1]))
+
+    def GetImagesForPathLength(self, totalEdges):
+        return [(self.techniqueNames[k], img) for k, img in self.techniqueImages.items() if k[2] == totalEdges]
+
+    def Normalize(self, scalingFactor):
+        for img in self.techniqueImages.values():
+            img.Scale(scalingFactor)
+
+    def WriteToFiles(self, basename):
+        """One layered OpenEXR file per path length, "<basename>-depth-<d>.exr", a layer per
+        technique (channels "<technique>.R/G/B")."""
+        from .imagefile import write_exr
+        d = os.path.dirname(basename)
+        if d:
+            os.makedirs(d, exist_ok=True)
+        for depth in range(self.minDepth, self.maxDepth + 1):
+            ch = {}
+            for name, img in self.GetImagesForPathLength(depth):
+                for c, k in zip("RGB", range(3)):
+                    ch[f"{name}.{c}"] = img.data[:, :, k]
+            write_exr(f"{basename}-depth-{depth}.exr", ch)
 
 
 def autotune(scene, integrator, trial_iterations=2):
