@@ -249,6 +249,15 @@ typedef struct SstPathVertex {
 int sst_trace_light_paths(sst_scene* scene, uint32_t seed, uint32_t iteration, int32_t numPaths, int32_t maxDepth, SstPathVertex* vertices,
                           int32_t* lengths, int32_t memory, SstRenderStats* stats);
 
+/* ---- path replay (PathTracerBase.ReplayPixel, PathTracer.cs:60-68) ------------------------------
+ * Renders the n paths (pixels[k], iterations[k]) exactly as sst_render renders them (a path is a
+ * function of BaseSeed, its pixel index row*width+col and its 0-based iteration) and writes each
+ * path's estimate, the value RenderPixel splats, to rgb[3k..3k+2].  Nothing is added to a film.
+ * The path graph of the reference's ReplayPixel (a debugging aid) is not built.  memory applies to
+ * pixels, iterations and rgb. */
+int sst_render_paths(sst_scene* scene, const SstPathTracerParams* params, const int32_t* pixels, const int32_t* iterations, int32_t n,
+                     float* rgb, int32_t memory, SstRenderStats* stats);
+
 /* ---- frame-buffer layers ------------------------------------------------------------------------
  * Computed on the device while the film is folded:
  *  - the VarianceLayer (FrameBuffer.Flags.EstimatePixelVariance, Images/VarianceLayer.cs:10-84);

@@ -127,6 +127,7 @@ SIGNATURES = {
     "sst_forward_batch": [_vp, _vp, _i32, _P(SstRenderStats)],
     "sst_trace_light_paths": [_vp, ctypes.c_uint32, ctypes.c_uint32, _i32, _i32, _vp, _vp, _i32, _P(SstRenderStats)],
     "sst_render_layers": [_vp, _P(SstPathTracerParams), _vp, _i32, _P(SstFilmLayers), _P(SstRenderStats)],
+    "sst_render_paths": [_vp, _P(SstPathTracerParams), _vp, _vp, _i32, _vp, _i32, _P(SstRenderStats)],
     "sst_backward_batch": [_vp, _vp, _i32, _vp, _i32, _vp, _P(SstRenderStats)],
     "sst_forward": [_vp, _P(SstPathTracerParams), _vp, _i32, _P(SstRenderStats)],
     "sst_backward": [_vp, _P(SstPathTracerParams), _vp, _i32, _P(SstGradients), _P(SstRenderStats)],
@@ -413,6 +414,17 @@ class SceneHandle:
         stats = SstRenderStats()
         check(self.lib.sst_render_layers(self.handle, ctypes.byref(params), ctypes.c_void_p(film), SST_MEM_HOST, ctypes.byref(L), ctypes.byref(stats)))
         return stats, var, None if avg is None else float(avg[0]), err
+
+    def render_paths(self, params, pixels, iterations):
+        """sst_render_paths: the estimates (n, 3) float32 of the paths (pixels[k], iterations[k])."""
+        px = np.ascontiguousarray(pixels, np.int32).reshape(-1)
+        it = np.ascontiguousarray(iterations, np.int32).reshape(-1)
+        if px.shape != it.shape:
+            raise ValueError("pixels and iterations differ in length")
+        rgb = np.zeros((px.size, 3), np.float32)
+        stats = SstRenderStats()
+        check(self.lib.sst_render_paths(self.handle, ctypes.byref(params), ptr(px), ptr(it), px.size, ptr(rgb), SST_MEM_HOST, ctypes.byref(stats)))
+        return rgb, stats
 
     def trace_light_paths(self, seed, iteration, num_paths, max_depth):
         """sst_trace_light_paths: (floats (n, maxDepth+1, 16), ints (n, maxDepth+1, 6), lengths (n,),

@@ -855,7 +855,11 @@ static void planWaves(std::vector<JobIn>& jobs, int cap, bool iterationPerWave, 
 }
 
 // Renders the jobs' iterations [iterFirst, iterEnd) into their device films.
-static void renderJobs(sst_ctx* c, std::vector<JobIn>& jobs, SstRenderStats* out, bool replay = false) {
+// paths: instead of the jobs' iteration ranges, render exactly these single-path chunks (one
+// (pixel, iteration) each, at most one wave) without folding them into a film; each path's
+// estimate is left in c->samples at its chunk's item offset.
+static void renderJobs(sst_ctx* c, std::vector<JobIn>& jobs, SstRenderStats* out, bool replay = false,
+                       const std::vector<WaveChunk>* paths = nullptr) {
     cudaStream_t st = c->stream;
     if (jobs.empty()) return;
     long long totalItems = 0;
@@ -867,6 +871,7 @@ static void renderJobs(sst_ctx* c, std::vector<JobIn>& jobs, SstRenderStats* out
         maxDepth = std::max(maxDepth, j.p.maxDepth);
         timeLimit |= j.p.maximumRenderTimeMs > 0;
     }
+    if (paths) totalItems = (long long)paths->size();
     if (totalItems == 0) return;
     if (timeLimit && jobs.size() > 1) fail(SST_ERR_UNSUPPORTED, "MaximumRenderTimeMs is supported for single renders only");
     int cap = int(std::min<long long>(c->waveCapacity > 0 ? c->waveCapacity : defaultWaveCapacity(), totalItems));
@@ -915,7 +920,12 @@ static void renderJobs(sst_ctx* c, std::vector<JobIn>& jobs, SstRenderStats* out
     std::vector<WaveChunk> chunks;
     std::vector<WaveDesc> waves;
     std::vector<std::vector<int>> iterEnds;
-    planWaves(jobs, w.wb.cap, timeLimit, chunks, waves, iterEnds);
+    if (paths) {
+        chunks = *paths;
+        waves.push_back(WaveDesc{0, int(chunks.size()), int(chunks.size()), 0});
+    } else {
+        planWaves(jobs, w.wb.cap, timeLimit, chunks, waves, iterEnds);
+    }
     c->jobsBuf.upload(hj, st);
     c->chunksBuf.upload(chunks, st);
     c->wavesBuf.upload(waves, st);
@@ -974,7 +984,7 @@ static void renderJobs(sst_ctx* c, std::vector<JobIn>& jobs, SstRenderStats* out
         }
         {
             KTimer kt(c, 4);
-            launch_film_fold(dj, dch, dwv, dcur, replay ? nullptr : c->samples.as<float>(), dstats, maxFold, 1, st);
+            launch_film_fold(dj, dch, dwv, dcur, (replay || paths) ? nullptr : c->samples.as<float>(), dstats, maxFold, 1, st);
         }
     };
 
@@ -1455,6 +1465,55 @@ int sst_render(sst_scene* s, const SstPathTracerParams* p, float* film, int32_t 
         if (memory != SST_MEM_DEVICE) CUDA_CHECK(cudaMemcpy(film, dFilm, filmBytes, cudaMemcpyDeviceToHost));
         fbMs += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - tfb1).count();
         local.frameBufferTimeMs = fbMs;
+        if (stats) *stats = local;
+    });
+}
+
+int sst_render_paths(sst_scene* s, const SstPathTracerParams* p, const int32_t* pixels, const int32_t* iterations, int32_t n, float* rgb,
+                     int32_t memory, SstRenderStats* stats) {
+    return guarded([&] {
+        if (!s || !p || n < 0 || (n > 0 && (!pixels || !iterations || !rgb))) fail(SST_ERR_INVALID_ARGUMENT, "invalid path list");
+        checkParams(s, p);
+        sst_ctx* c = s->ctx;
+        CUDA_CHECK(cudaSetDevice(c->device));
+        SstRenderStats local{};
+        for (int k = 0; k < 4; ++k) { local.nanPixel[k] = -1; local.nanIteration[k] = -1; }
+        std::vector<int32_t> px(pixels ? size_t(n) : 0), it(iterations ? size_t(n) : 0);
+        if (n > 0) {
+            const cudaMemcpyKind k = memory == SST_MEM_DEVICE ? cudaMemcpyDeviceToHost : cudaMemcpyHostToHost;
+            CUDA_CHECK(cudaMemcpy(px.data(), pixels, size_t(n) * 4, k));
+            CUDA_CHECK(cudaMemcpy(it.data(), iterations, size_t(n) * 4, k));
+        }
+        const long long P = (long long)p->width * p->height;
+        for (int32_t k = 0; k < n; ++k)
+            if (px[k] < 0 || px[k] >= P || it[k] < 0) fail(SST_ERR_INVALID_ARGUMENT, "pixel or iteration out of range");
+        const int batch = c->waveCapacity > 0 ? c->waveCapacity : defaultWaveCapacity();
+        std::vector<WaveChunk> chunks;
+        for (int32_t b0 = 0; b0 < n; b0 += batch) {
+            const int cnt = std::min(batch, n - b0);
+            chunks.assign(size_t(cnt), WaveChunk{});
+            for (int k = 0; k < cnt; ++k) {
+                WaveChunk& ck = chunks[k];
+                ck.job = 0;
+                ck.iterBase = it[b0 + k];
+                ck.nIter = 1;
+                ck.pixStart = px[b0 + k];
+                ck.pixCount = 1;
+                ck.itemOffset = k;
+                ck.film = nullptr;
+            }
+            std::vector<JobIn> jobs(1);
+            jobs[0].s = s;
+            jobs[0].p = *p;
+            jobs[0].p.maximumRenderTimeMs = 0;
+            jobs[0].iterFirst = 0;
+            jobs[0].iterEnd = 1;
+            renderJobs(c, jobs, &local, false, &chunks);
+            const cudaMemcpyKind k = memory == SST_MEM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+            CUDA_CHECK(cudaMemcpyAsync(rgb + 3 * size_t(b0), c->samples.p, size_t(cnt) * 12, k, c->stream));
+            CUDA_CHECK(cudaStreamSynchronize(c->stream));
+        }
+        local.numIterations = 0;
         if (stats) *stats = local;
     });
 }

@@ -13,7 +13,7 @@ import os
 import numpy as np
 
 from . import _native
-from .images import MonochromeImage, OutlierReplayCache, RgbImage, RgbLayer
+from .images import MonochromeImage, OutlierReplayCache, RgbColor, RgbImage, RgbLayer
 
 
 class Integrator:
@@ -127,6 +127,19 @@ class PathTracer(Integrator):
             self.techPyramidWeighted = TechPyramid(int(self.MinDepth), int(self.MaxDepth), pyramid[1])
             self.techPyramidRaw.WriteToFiles(os.path.join(fb.Basename, "techs-raw"))
             self.techPyramidWeighted.WriteToFiles(os.path.join(fb.Basename, "techs-weighted"))
+
+    def ReplayPixel(self, scene, pixel, iteration):
+        """PathTracerBase.ReplayPixel (PathTracer.cs:60-68): re-renders the path of `pixel` (a Pixel or
+        (col, row)) in the 0-based `iteration` from its seed and returns (graph, estimate).  The path
+        graph is a debugging aid of the reference that is not built here (None)."""
+        self._check_hooks()
+        col, row = pixel
+        fb = scene.FrameBuffer
+        if not (0 <= col < fb.Width and 0 <= row < fb.Height):
+            raise ValueError("pixel outside the frame buffer")
+        p = self.params(scene)
+        rgb, _ = scene.native.render_paths(p, [row * fb.Width + col], [int(iteration)])
+        return None, RgbColor(*rgb[0])
 
 
 class TechPyramid:

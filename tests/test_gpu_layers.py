@@ -200,6 +200,31 @@ def test_outlier_cache_matches_the_oracle():
     assert q.Count == 4 and best.Element.Iteration == oi[y, x][np.argmax(ow[y, x])]
 
 
+def test_replay_pixel_reproduces_the_cached_outliers():
+    """PathTracer.ReplayPixel (PathTracer.cs:60-68) re-renders one (pixel, iteration) path from its
+    seed: its channel average equals the outlier cache's priority for that entry bit for bit, as
+    OutlierCacheTest.cs:24-38 relies on, and iteration 0 equals the 1-spp film."""
+    S, w, h = 6, 24, 16
+    sc = workloads.cornell_box(w, h)
+    sc.Prepare()
+    pt = PathTracer(TotalSpp=S, MaxDepth=5)
+    pt.Render(sc)
+    oc = sc.FrameBuffer.OutlierCache
+    rng = np.random.default_rng(4)
+    for col, row in zip(rng.integers(0, w, 12), rng.integers(0, h, 12)):
+        q = oc.GetPixelOutlier(Pixel(int(col), int(row)))
+        for item in q.UnorderedItems:
+            graph, est = pt.ReplayPixel(sc, Pixel(int(col), int(row)), item.Element.Iteration)
+            r, g, b = (np.float32(x) for x in est.array())
+            assert graph is None and np.float32((r + g + b) / np.float32(3)) == np.float32(item.Priority)
+    # a batch of paths through the C ABI: iteration 0 of every pixel is the 1-spp film
+    sc.FrameBuffer = FrameBuffer(w, h)
+    PathTracer(TotalSpp=1, MaxDepth=5).Render(sc)
+    film = sc.FrameBuffer.Image.data.reshape(-1, 3)
+    rgb, _ = sc.native.render_paths(pt.params(sc), np.arange(w * h), np.zeros(w * h))
+    assert np.array_equal(rgb, film)
+
+
 def _constant_background_scene(w, h):
     sc = Scene()
     tri = Mesh([[-1, -1, 5], [1, -1, 5], [0, 1, 5]], [0, 1, 2])  # behind the camera
