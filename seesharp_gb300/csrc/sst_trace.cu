@@ -243,8 +243,10 @@ SST_D TraceResult traverse4(const Bvh4 sc, float3 org, float3 dir, float tmin, f
 // mode 0: closest hit -> hits[i]; mode 1: shadow rays, zero nee[tgt[i]] when occluded;
 // mode 2: any hit -> occl[i] = 1/0.
 // Resident threads per SM the traversal kernels are compiled for (register budget); 0: no bound.
+// 1024 caps every block size at 64 registers: shadow rays 3% faster on the 1M-triangle scene than
+// the unbounded build (66 registers for closest hit); 1280 (48 registers) is 10-30% slower.
 #ifndef SST_TRACE_MIN_THREADS
-#define SST_TRACE_MIN_THREADS 0
+#define SST_TRACE_MIN_THREADS 1024
 #endif
 template <int MODE, int BLOCK, int SSTACK, bool WIDE>
 __global__ void __launch_bounds__(BLOCK, SST_TRACE_MIN_THREADS > 0 ? SST_TRACE_MIN_THREADS / BLOCK : 1) k_trace(const DevJob* __restrict__ jobs, const uint32_t* __restrict__ rayJob, const float4* ro,
