@@ -1518,11 +1518,11 @@ int sst_render_paths(sst_scene* s, const SstPathTracerParams* p, const int32_t* 
     });
 }
 
-static TraceTuning toTrace(const SstTuning& t) { return TraceTuning{t.traceBlock, t.traceStackShared, t.traceBlocksPerSM, t.traceBvhWidth}; }
+static TraceTuning toTrace(const SstTuning& t) { return TraceTuning{t.traceBlock, t.traceStackShared, t.traceBlocksPerSM, t.traceBvhWidth, t.traceRefillIdle}; }
 
 static void checkTuning(const SstTuning& t) {
     if (!traceTuningValid(toTrace(t)))
-        fail(SST_ERR_INVALID_ARGUMENT, "traceBlock must be 64, 128 or 256, traceStackShared 16, 24 or 32, and traceBvhWidth 2 or 4");
+        fail(SST_ERR_INVALID_ARGUMENT, "traceBlock must be 64, 128 or 256, traceStackShared 16, 24 or 32, traceBvhWidth 2 or 4, and traceRefillIdle in [1, 32]");
     if (t.waveCapacity != 0 && (t.waveCapacity < 1024 || t.waveCapacity > (1 << 24)))
         fail(SST_ERR_INVALID_ARGUMENT, "waveCapacity must be 0 or in [1024, 2^24]");
     if (t.traceBlocksPerSM < 0 || t.traceBlocksPerSM > 64) fail(SST_ERR_INVALID_ARGUMENT, "traceBlocksPerSM must be in [0, 64]");
@@ -1535,6 +1535,7 @@ static SstTuning currentTuning(const sst_ctx* c) {
     t.traceStackShared = c->trace.smemStack;
     t.traceBlocksPerSM = c->trace.blocksPerSM;
     t.traceBvhWidth = c->trace.width;
+    t.traceRefillIdle = c->trace.refillIdle;
     return t;
 }
 
@@ -1569,8 +1570,8 @@ int sst_autotune(sst_scene* s, const SstPathTracerParams* p, int32_t trialIterat
         film.ensure(size_t(tp.width) * tp.height * 3 * sizeof(float));
         const bool prof = c->profiling;
         c->profiling = false;
-        // one candidate: the faster of two trial renders
-        auto trial = [&](const SstTuning& t) {
+        // one candidate: the faster of two trial renders of `iters` iterations
+        auto trial = [&](const SstTuning& t, int iters) {
             c->trace = toTrace(t);
             c->waveCapacity = t.waveCapacity;
             double best = 1e300;
@@ -1578,9 +1579,10 @@ int sst_autotune(sst_scene* s, const SstPathTracerParams* p, int32_t trialIterat
                 std::vector<JobIn> jobs(1);
                 jobs[0].s = s;
                 jobs[0].p = tp;
+                jobs[0].p.totalSpp = iters;
                 jobs[0].dFilm = film.as<float>();
                 jobs[0].iterFirst = 0;
-                jobs[0].iterEnd = tp.totalSpp;
+                jobs[0].iterEnd = iters;
                 SstRenderStats st{};
                 renderJobs(c, jobs, &st);
                 best = std::min(best, st.renderTimeMs);
@@ -1599,29 +1601,46 @@ int sst_autotune(sst_scene* s, const SstPathTracerParams* p, int32_t trialIterat
                         t.traceBlock = b;
                         t.traceStackShared = k;
                         t.traceBlocksPerSM = 0;
-                        double ms = trial(t);
+                        double ms = trial(t, trialIterations);
                         if (ms < bestMs) { bestMs = ms; best = t; }
                     }
+            // refill threshold of the 4-wide traversal
+            if (best.traceBvhWidth == 4)
+                for (int ri : {32, 12, 24}) {
+                    if (ri == best.traceRefillIdle) continue;
+                    SstTuning t = best;
+                    t.traceRefillIdle = ri;
+                    double ms = trial(t, trialIterations);
+                    if (ms < bestMs) { bestMs = ms; best = t; }
+                }
             // resident traversal blocks per SM
             int m = traceMaxBlocksPerSM(toTrace(best));
             for (int bps : {m / 2, (3 * m) / 4}) {
                 if (bps < 1 || bps >= m) continue;
                 SstTuning t = best;
                 t.traceBlocksPerSM = bps;
-                double ms = trial(t);
+                double ms = trial(t, trialIterations);
                 if (ms < bestMs) { bestMs = ms; best = t; }
             }
-            // wave capacity
-            long long items = (long long)tp.width * tp.height * tp.totalSpp;
+            // wave capacity: the trials hold about four waves of the largest candidate (within the
+            // caller's spp), since a trial of one or two short waves favours small waves that
+            // leave the GPU idle in their last bounces of a long render
+            const long long pixels = (long long)tp.width * tp.height;
+            const int wcIters = (int)std::max<long long>(trialIterations, std::min<long long>(p->totalSpp, (4LL << 22) / pixels + 1));
+            const long long items = pixels * wcIters;
+            SstTuning cur = best;
+            double curMs = trial(cur, wcIters);
             for (int capLog = 19; capLog <= 22; ++capLog) {
                 int cap = 1 << capLog;
-                if (cap == (best.waveCapacity > 0 ? best.waveCapacity : defaultWaveCapacity())) continue;
+                if (cap == (cur.waveCapacity > 0 ? cur.waveCapacity : defaultWaveCapacity())) continue;
                 if ((long long)cap > 2 * items) break;
-                SstTuning t = best;
+                SstTuning t = cur;
                 t.waveCapacity = cap;
-                double ms = trial(t);
-                if (ms < bestMs) { bestMs = ms; best = t; }
+                double ms = trial(t, wcIters);
+                if (ms < curMs) { curMs = ms; best = t; }
             }
+            // the reported time is that of a trial of trialIterations iterations
+            bestMs = wcIters == trialIterations ? curMs : trial(best, trialIterations);
         } catch (...) {
             c->trace = toTrace(start);
             c->waveCapacity = start.waveCapacity;

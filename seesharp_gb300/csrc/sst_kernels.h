@@ -26,6 +26,9 @@ struct TraceTuning {
     int smemStack = kSmemStack;
     int blocksPerSM = 0;
     int width = 4;  // BVH width: 2 (binary) or 4
+    // 4-wide traversal: finished rays of a warp are replaced once this many of its 32 lanes are
+    // idle (32: only when the whole warp is); the other lanes pause in place meanwhile
+    int refillIdle = kTraceRefillIdle;
 };
 bool traceTuningValid(const TraceTuning& t);
 int traceGrid(const TraceTuning& t);

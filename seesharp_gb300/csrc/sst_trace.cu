@@ -2,8 +2,10 @@
 // (Integrators/PathTracer.cs:319,428,467).
 //
 // Binary BVH with both child boxes stored in the parent (64-byte nodes read as four 128-bit
-// loads), watertight ray/triangle test (Woop, Benthin, Wald 2013), a per-thread traversal stack
-// in shared memory with a local-memory tail, and persistent warps that fetch 32 rays at a time.
+// loads) or the 4-wide BVH over the same leaves (128-byte nodes), watertight ray/triangle test
+// (Woop, Benthin, Wald 2013), a per-thread traversal stack in shared memory with a local-memory
+// tail, and persistent warps: the binary kernel fetches 32 rays at a time, the 4-wide one replaces
+// finished rays once a set number of the warp's lanes are idle.
 // The block size and the number of stack entries kept in shared memory are template parameters;
 // the autotuner picks one of the instantiated variants per context (TraceTuning).  The result of
 // a query does not depend on the variant: the traversal order is the same, and closest-hit ties
@@ -164,25 +166,55 @@ SST_D void cswap(float& ka, uint32_t& ra, float& kb, uint32_t& rb) {
     ra = r;
 }
 
+// One lane's 4-wide traversal, resumable: the next node to visit, the stack depth and the closest
+// hit so far stay in the structure when trav4Run pauses.
+struct Trav4 {
+    Bvh4 bvh;
+    float3 org, inv, oi;
+    RayPre pre;
+    float tmin;
+    TraceResult r;
+    int bestGid;
+    int sp;
+    uint32_t ref;
+    bool done;
+};
+
+SST_D void trav4Begin(Trav4& s, const Bvh4 bvh, float3 org, float3 dir, float tmin, float tmax) {
+    s.bvh = bvh;
+    s.org = org;
+    s.pre = rayPre(dir);
+    s.inv = mk(1.0f / dir.x, 1.0f / dir.y, 1.0f / dir.z);
+    s.oi = mk(-org.x * s.inv.x, -org.y * s.inv.y, -org.z * s.inv.z);
+    s.tmin = tmin;
+    s.r = TraceResult{tmax, 0.f, 0.f, -1};
+    s.bestGid = 0x7FFFFFFF;
+    s.sp = 0;
+    s.ref = 0;  // root
+    s.done = bvh.nNodes4 == 0 || !(tmax > tmin);
+}
+
+// Traversal steps until the ray is finished (returns true, result in s.r) or, with pauseIdle > 0,
+// until pauseIdle lanes of the warp are outside this loop (returns false after at least one
+// step; a later call resumes).  The lanes are counted at the loop head, where every lane still
+// traversing reconverges (__activemask counts the lanes converged at the instruction: counted
+// after a stack pop instead, the lanes that had just descended were missing, warps paused after
+// almost every step, and traversal was 45% slower).  lstack: this lane's local-memory stack tail.
 template <bool ANY, int BLOCK, int SSTACK>
-SST_D TraceResult traverse4(const Bvh4 sc, float3 org, float3 dir, float tmin, float tmax, int* sstack, int* errFlags) {
-    TraceResult r{tmax, 0.f, 0.f, -1};
-    if (sc.nNodes4 == 0 || !(tmax > tmin)) return r;
-    int bestGid = 0x7FFFFFFF;
-    RayPre pre = rayPre(dir);
-    float3 inv = mk(1.0f / dir.x, 1.0f / dir.y, 1.0f / dir.z);
-    float3 oi = mk(-org.x * inv.x, -org.y * inv.y, -org.z * inv.z);
-    int lstack[kMaxStack4 - SSTACK];
-    int sp = 0;
-    uint32_t ref = 0;  // root
+SST_D bool trav4Run(Trav4& s, int* sstack, int* lstack, int* errFlags, int pauseIdle) {
     const int tid = threadIdx.x;
+    const Bvh4& sc = s.bvh;
+    bool first = true;
     for (;;) {
+        if (!first && pauseIdle > 0 && 32 - __popc(__activemask()) >= pauseIdle) return false;
+        first = false;
+        const uint32_t ref = s.ref;
         if (!(ref & kLeafFlag)) {
             const float4* nd = sc.nodes4 + 8 * (size_t)ref;
             float4 lx = __ldg(nd), hx = __ldg(nd + 1), ly = __ldg(nd + 2), hy = __ldg(nd + 3), lz = __ldg(nd + 4), hz = __ldg(nd + 5);
             float4 rf = __ldg(nd + 6), meta = __ldg(nd + 7);
             const int cnt = __float_as_int(meta.x);
-            const float hitT = r.t * 1.0000004f;
+            const float hitT = s.r.t * 1.0000004f;  // conservative far bound (box/triangle rounding)
             float key[4];
             uint32_t cr[4];
             const float* LX = &lx.x; const float* HX = &hx.x; const float* LY = &ly.x; const float* HY = &hy.x;
@@ -190,10 +222,10 @@ SST_D TraceResult traverse4(const Bvh4 sc, float3 org, float3 dir, float tmin, f
             int nh = 0;
 #pragma unroll
             for (int k = 0; k < 4; ++k) {
-                float a = fmaf(LX[k], inv.x, oi.x), b = fmaf(HX[k], inv.x, oi.x);
-                float c = fmaf(LY[k], inv.y, oi.y), d = fmaf(HY[k], inv.y, oi.y);
-                float e = fmaf(LZ[k], inv.z, oi.z), f = fmaf(HZ[k], inv.z, oi.z);
-                float tn = fmaxf(fmaxf(fminf(a, b), fminf(c, d)), fmaxf(fminf(e, f), tmin));
+                float a = fmaf(LX[k], s.inv.x, s.oi.x), b = fmaf(HX[k], s.inv.x, s.oi.x);
+                float c = fmaf(LY[k], s.inv.y, s.oi.y), d = fmaf(HY[k], s.inv.y, s.oi.y);
+                float e = fmaf(LZ[k], s.inv.z, s.oi.z), f = fmaf(HZ[k], s.inv.z, s.oi.z);
+                float tn = fmaxf(fmaxf(fminf(a, b), fminf(c, d)), fmaxf(fminf(e, f), s.tmin));
                 float tf = fminf(fminf(fmaxf(a, b), fmaxf(c, d)), fminf(fmaxf(e, f), hitT));
                 bool hit = k < cnt && tn <= tf * 1.0000004f;
                 key[k] = hit ? tn : CUDART_INF_F;
@@ -210,34 +242,34 @@ SST_D TraceResult traverse4(const Bvh4 sc, float3 org, float3 dir, float tmin, f
                 // push the farther hit children, farthest first
                 for (int k = nh - 1; k >= 1; --k) {
                     uint32_t pr = k == 3 ? cr[3] : (k == 2 ? cr[2] : cr[1]);
-                    if (sp < SSTACK) sstack[sp * BLOCK + tid] = (int)pr;
-                    else if (sp < kMaxStack4) lstack[sp - SSTACK] = (int)pr;
-                    else { atomicOr(errFlags, 1); return r; }
-                    ++sp;
+                    if (s.sp < SSTACK) sstack[s.sp * BLOCK + tid] = (int)pr;
+                    else if (s.sp < kMaxStack4) lstack[s.sp - SSTACK] = (int)pr;
+                    else { atomicOr(errFlags, 1); return true; }
+                    ++s.sp;
                 }
-                ref = cr[0];
+                s.ref = cr[0];
                 continue;
             }
         } else {
-            int first = (int)(ref & kLeafFirstMask);
+            int firstTri = (int)(ref & kLeafFirstMask);
             int cnt = (int)((ref >> kLeafCountShift) & 0xF) + 1;
             for (int k = 0; k < cnt; ++k) {
-                int ti = first + k;
+                int ti = firstTri + k;
                 float4 a = __ldg(&sc.triv[3 * (size_t)ti]), b = __ldg(&sc.triv[3 * (size_t)ti + 1]), c = __ldg(&sc.triv[3 * (size_t)ti + 2]);
                 float t, u, v;
-                float lim = ANY ? r.t : __uint_as_float(__float_as_uint(r.t) + (r.t < CUDART_INF_F ? 1u : 0u));
-                if (isectTri(org, pre, f3(a), f3(b), f3(c), tmin, lim, t, u, v)) {
+                // allow an equal distance so that ties can resolve to the smaller id
+                float lim = ANY ? s.r.t : __uint_as_float(__float_as_uint(s.r.t) + (s.r.t < CUDART_INF_F ? 1u : 0u));
+                if (isectTri(s.org, s.pre, f3(a), f3(b), f3(c), s.tmin, lim, t, u, v)) {
                     int gid = __float_as_int(a.w);
-                    if (ANY) { r.t = t; r.u = u; r.v = v; r.tri = ti; return r; }
-                    if (t < r.t || (t == r.t && gid < bestGid)) { r.t = t; r.u = u; r.v = v; r.tri = ti; bestGid = gid; }
+                    if (ANY) { s.r.t = t; s.r.u = u; s.r.v = v; s.r.tri = ti; return true; }
+                    if (t < s.r.t || (t == s.r.t && gid < s.bestGid)) { s.r.t = t; s.r.u = u; s.r.v = v; s.r.tri = ti; s.bestGid = gid; }
                 }
             }
         }
-        if (sp == 0) break;
-        --sp;
-        ref = (uint32_t)(sp < SSTACK ? sstack[sp * BLOCK + tid] : lstack[sp - SSTACK]);
+        if (s.sp == 0) return true;
+        --s.sp;
+        s.ref = (uint32_t)(s.sp < SSTACK ? sstack[s.sp * BLOCK + tid] : lstack[s.sp - SSTACK]);
     }
-    return r;
 }
 
 // mode 0: closest hit -> hits[i]; mode 1: shadow rays, zero nee[tgt[i]] when occluded;
@@ -251,13 +283,53 @@ SST_D TraceResult traverse4(const Bvh4 sc, float3 org, float3 dir, float tmin, f
 template <int MODE, int BLOCK, int SSTACK, bool WIDE>
 __global__ void __launch_bounds__(BLOCK, SST_TRACE_MIN_THREADS > 0 ? SST_TRACE_MIN_THREADS / BLOCK : 1) k_trace(const DevJob* __restrict__ jobs, const uint32_t* __restrict__ rayJob, const float4* ro,
                                                  const float4* rd, const int* count, int* work, float4* hits, const int* tgt, float4* nee,
-                                                 int* occl, DevStats* stats, int countRays) {
+                                                 int* occl, DevStats* stats, int countRays, int refillIdle) {
     __shared__ int sstack[SSTACK * BLOCK];
     const int n = *count;
     const int lane = threadIdx.x & 31;
     if (countRays && blockIdx.x == 0 && threadIdx.x == 0) {
         if (MODE == 0) atomicAdd(&stats->rays, (unsigned long long)n);
     }
+    if constexpr (WIDE) {
+        // Lanes whose ray is finished take new rays together once refillIdle of the warp's lanes
+        // are idle (32: once the whole warp is); the others pause in place and resume after the
+        // refill.  A scene without a 4-wide BVH has no triangles: every ray misses.
+        int lstack[kMaxStack4 - SSTACK];
+        Trav4 s;
+        int i = -1;
+        bool exhausted = false;
+        const int thr = refillIdle > 0 && refillIdle < 32 ? refillIdle : 32;
+        for (;;) {
+            const unsigned idle = __ballot_sync(0xffffffffu, i < 0);
+            if (!exhausted && __popc(idle) >= thr) {
+                const int nIdle = __popc(idle);
+                int base = 0;
+                if (lane == 0) base = atomicAdd(work, nIdle);
+                base = __shfl_sync(0xffffffffu, base, 0);
+                if (base + nIdle >= n) exhausted = true;
+                if (i < 0) {
+                    const int j = base + __popc(idle & ((1u << lane) - 1u));
+                    if (j < n) {
+                        i = j;
+                        const float4 o = ro[j], d = rd[j];
+                        const uint32_t jb = rayJob ? rayJob[j] : 0u;
+                        trav4Begin(s, bvh4Of(jobs[jb].sc), f3(o), f3(d), o.w, d.w);
+                    }
+                }
+            }
+            if (__ballot_sync(0xffffffffu, i >= 0) == 0) break;  // every lane idle: the queue is drained
+            if (i >= 0) {
+                const bool fin = s.done || trav4Run<MODE != 0, BLOCK, SSTACK>(s, sstack, lstack, &stats->errorFlags, exhausted ? 0 : thr);
+                if (fin) {
+                    const TraceResult& h = s.r;
+                    if (MODE == 0) hits[i] = make_float4(h.t, h.u, h.v, __int_as_float(h.tri));
+                    else if (MODE == 1) { if (h.tri >= 0) nee[tgt[i]] = make_float4(0.f, 0.f, 0.f, 0.f); }
+                    else occl[i] = h.tri >= 0 ? 1 : 0;
+                    i = -1;
+                }
+            }
+        }
+    } else {
     for (;;) {
         int base = 0;
         if (lane == 0) base = atomicAdd(work, 32);
@@ -268,9 +340,7 @@ __global__ void __launch_bounds__(BLOCK, SST_TRACE_MIN_THREADS > 0 ? SST_TRACE_M
             float4 o = ro[i], d = rd[i];
             uint32_t jb = rayJob ? rayJob[i] : 0u;
             const DevScene& sc = jobs[jb].sc;
-            TraceResult h = (WIDE && sc.nNodes4 > 0)
-                                ? traverse4<MODE != 0, BLOCK, SSTACK>(bvh4Of(sc), f3(o), f3(d), o.w, d.w, sstack, &stats->errorFlags)
-                                : traverse<MODE != 0, BLOCK, SSTACK>(bvhOf(sc), f3(o), f3(d), o.w, d.w, sstack, &stats->errorFlags);
+            TraceResult h = traverse<MODE != 0, BLOCK, SSTACK>(bvhOf(sc), f3(o), f3(d), o.w, d.w, sstack, &stats->errorFlags);
             if (MODE == 0) {
                 hits[i] = make_float4(h.t, h.u, h.v, __int_as_float(h.tri));
             } else if (MODE == 1) {
@@ -280,13 +350,14 @@ __global__ void __launch_bounds__(BLOCK, SST_TRACE_MIN_THREADS > 0 ? SST_TRACE_M
             }
         }
     }
+    }
 }
 
 // ---------------------------------------------------------------------------------------------
 // Variant table: BVH width x block size x shared stack entries, for each of the three modes.
 // ---------------------------------------------------------------------------------------------
 using TraceKernel = void (*)(const DevJob*, const uint32_t*, const float4*, const float4*, const int*, int*, float4*, const int*, float4*, int*,
-                             DevStats*, int);
+                             DevStats*, int, int);
 
 template <int BLOCK, int SSTACK, bool WIDE>
 struct TraceVariant {
@@ -334,7 +405,7 @@ static TraceKernel traceKernel(int mode, int variant) {
 #undef SST_TV
 }
 
-bool traceTuningValid(const TraceTuning& t) { return variantOf(t) >= 0 && t.blocksPerSM >= 0; }
+bool traceTuningValid(const TraceTuning& t) { return variantOf(t) >= 0 && t.blocksPerSM >= 0 && t.refillIdle >= 1 && t.refillIdle <= 32; }
 
 // Resident blocks per SM of a variant (occupancy), computed once per variant for the device that
 // first asks (the devices of one machine are identical).
@@ -377,7 +448,8 @@ static void launch(const TraceTuning& t, int mode, const DevJob* jobs, const uin
                    int* work, float4* hits, const int* tgt, float4* nee, int* occl, DevStats* stats, int countRays, cudaStream_t s) {
     int v = variantOf(t);
     if (v < 0) v = 4;  // 128 threads, 24 shared entries, binary
-    traceKernel(mode, v)<<<traceGrid(t), kBlocks[(v % 9) / 3], 0, s>>>(jobs, rayJob, ro, rd, count, work, hits, tgt, nee, occl, stats, countRays);
+    traceKernel(mode, v)<<<traceGrid(t), kBlocks[(v % 9) / 3], 0, s>>>(jobs, rayJob, ro, rd, count, work, hits, tgt, nee, occl, stats, countRays,
+                                                                        t.refillIdle);
 }
 
 void launch_trace_closest(const TraceTuning& t, const DevJob* jobs, const uint32_t* rayJob, const float4* ro, const float4* rd, const int* count,

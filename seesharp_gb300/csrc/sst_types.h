@@ -8,6 +8,7 @@ namespace sst {
 constexpr int kMaxShadowRays = 4;     // NumShadowRays supported per vertex
 constexpr int kTraceBlock = 128;      // threads per block of the traversal kernels
 constexpr int kSmemStack = 24;        // traversal stack entries kept in shared memory per thread
+constexpr int kTraceRefillIdle = 20;  // idle lanes of a warp at which the 4-wide traversal takes new rays
 constexpr int kMaxStack = 64;         // total stack entries (the BVH builder caps the depth below this)
 constexpr int kMaxStack4 = 192;       // 4-wide traversal: at most 3 pending children per level of at most 60 levels
 constexpr int kMaxBvhDepth = 60;
