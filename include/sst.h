@@ -178,16 +178,21 @@ typedef struct SstTuning {
     int32_t traceBvhWidth;    /* BVH traversed: 2 (binary) or 4 (4-wide, same leaves; the default) */
     int32_t traceRefillIdle;  /* 4-wide traversal: a warp's finished rays are replaced once this many of its
                                  32 lanes are idle (1..32; 32 = only when all are; the default is 20) */
+    int32_t shadeBlocks;      /* resident 128-thread blocks per SM the forward shade kernel with GenericMaterials
+                                 is built for: 8 (64 registers; the default) or 14 (32 registers, more
+                                 warps, more spilling; one shadow ray per technique only) */
 } SstTuning;
 int sst_get_tuning(sst_ctx* ctx, SstTuning* out);
 /* Invalid values return SST_ERR_INVALID_ARGUMENT and leave the setting unchanged. */
 int sst_set_tuning(sst_ctx* ctx, const SstTuning* tuning);
-/* Chooses the setting for this scene and these parameters by timing trial renders of
- * trialIterations iterations (into a scratch film; the caller's films are not touched):
+/* Chooses the setting for this scene and these parameters by timing trial renders into a scratch
+ * film (the caller's films are not touched), keeping the fastest of two runs per candidate:
  * first the traversal variant (BVH width x block size x shared stack entries), then the refill
- * threshold of the 4-wide traversal, then the resident blocks per SM, then the wave capacity,
- * keeping the fastest of two runs per candidate.  The choice is applied to the scene's context
- * and returned in `chosen` (bestTrialMs may be NULL). */
+ * threshold of the 4-wide traversal, then the shade kernel's build, then the resident blocks per
+ * SM, each with trials of at least trialIterations iterations and at least 2^21 paths; then the
+ * wave capacity, with trials of about four waves of 2^22 paths (within the parameters' spp).  The
+ * choice is applied to the scene's context and returned in `chosen`; bestTrialMs (may be NULL)
+ * receives the time of a trialIterations-iteration render with it. */
 int sst_autotune(sst_scene* scene, const SstPathTracerParams* params, int32_t trialIterations, SstTuning* chosen, double* bestTrialMs);
 
 /* ---- allocation-free occlusion query: no counterpart in the reference --------------------------

@@ -149,6 +149,7 @@ struct sst_ctx {
     // launch configuration (sst_set_tuning / sst_autotune)
     TraceTuning trace;
     int waveCapacity = 0;  // 0: the default
+    int shadeBlocks = 8;   // resident blocks per SM of the forward shade kernel with GenericMaterials: 8 or 14
     // kernel timing (sst_set_profiling)
     bool profiling = false;
     std::vector<cudaEvent_t> evPool;
@@ -964,7 +965,7 @@ static void renderJobs(sst_ctx* c, std::vector<JobIn>& jobs, SstRenderStats* out
                                          cnt + kCntQueue + d + 1, cnt + kCntShadow + d, c->samples.as<float>(), dstats,
                                          PyrArgs{dch, dwv, dcur, c->pyrG.as<float4>()}, maxItems, st);
                 else
-                    launch_shade(ns, replay, generic, dj, A, B, w.wb.hits, w.wb.nee, w.wb.neeG, w.wb.cap, w.wb.shRo, w.wb.shRd, w.wb.shTgt, w.wb.shJob,
+                    launch_shade(ns, replay, generic, c->shadeBlocks, dj, A, B, w.wb.hits, w.wb.nee, w.wb.neeG, w.wb.cap, w.wb.shRo, w.wb.shRd, w.wb.shTgt, w.wb.shJob,
                                  cnt + kCntQueue + d, cnt + kCntQueue + d + 1, cnt + kCntShadow + d, c->samples.as<float>(), dstats, maxItems, st);
             }
             {
@@ -1526,6 +1527,7 @@ static void checkTuning(const SstTuning& t) {
     if (t.waveCapacity != 0 && (t.waveCapacity < 1024 || t.waveCapacity > (1 << 24)))
         fail(SST_ERR_INVALID_ARGUMENT, "waveCapacity must be 0 or in [1024, 2^24]");
     if (t.traceBlocksPerSM < 0 || t.traceBlocksPerSM > 64) fail(SST_ERR_INVALID_ARGUMENT, "traceBlocksPerSM must be in [0, 64]");
+    if (t.shadeBlocks != 8 && t.shadeBlocks != 14) fail(SST_ERR_INVALID_ARGUMENT, "shadeBlocks must be 8 or 14");
 }
 
 static SstTuning currentTuning(const sst_ctx* c) {
@@ -1536,6 +1538,7 @@ static SstTuning currentTuning(const sst_ctx* c) {
     t.traceBlocksPerSM = c->trace.blocksPerSM;
     t.traceBvhWidth = c->trace.width;
     t.traceRefillIdle = c->trace.refillIdle;
+    t.shadeBlocks = c->shadeBlocks;
     return t;
 }
 
@@ -1552,6 +1555,7 @@ int sst_set_tuning(sst_ctx* c, const SstTuning* t) {
         checkTuning(*t);
         c->trace = toTrace(*t);
         c->waveCapacity = t->waveCapacity;
+        c->shadeBlocks = t->shadeBlocks;
     });
 }
 
@@ -1574,6 +1578,7 @@ int sst_autotune(sst_scene* s, const SstPathTracerParams* p, int32_t trialIterat
         auto trial = [&](const SstTuning& t, int iters) {
             c->trace = toTrace(t);
             c->waveCapacity = t.waveCapacity;
+            c->shadeBlocks = t.shadeBlocks;
             double best = 1e300;
             for (int r = 0; r < 2; ++r) {
                 std::vector<JobIn> jobs(1);
@@ -1591,6 +1596,10 @@ int sst_autotune(sst_scene* s, const SstPathTracerParams* p, int32_t trialIterat
         };
         SstTuning best = start;
         double bestMs = 1e300;
+        // the kernel stages time trials of at least one full default wave of paths: a trial of a
+        // few small iterations lasts a fraction of a millisecond and its timing is mostly noise
+        const long long tpix = (long long)tp.width * tp.height;
+        const int kIters = (int)std::max<long long>(trialIterations, ((long long)defaultWaveCapacity() + tpix - 1) / tpix);
         try {
             // traversal variant
             for (int wdt : {2, 4})
@@ -1601,7 +1610,7 @@ int sst_autotune(sst_scene* s, const SstPathTracerParams* p, int32_t trialIterat
                         t.traceBlock = b;
                         t.traceStackShared = k;
                         t.traceBlocksPerSM = 0;
-                        double ms = trial(t, trialIterations);
+                        double ms = trial(t, kIters);
                         if (ms < bestMs) { bestMs = ms; best = t; }
                     }
             // refill threshold of the 4-wide traversal
@@ -1610,16 +1619,23 @@ int sst_autotune(sst_scene* s, const SstPathTracerParams* p, int32_t trialIterat
                     if (ri == best.traceRefillIdle) continue;
                     SstTuning t = best;
                     t.traceRefillIdle = ri;
-                    double ms = trial(t, trialIterations);
+                    double ms = trial(t, kIters);
                     if (ms < bestMs) { bestMs = ms; best = t; }
                 }
+            // occupancy build of the shade kernel with GenericMaterials
+            {
+                SstTuning t = best;
+                t.shadeBlocks = best.shadeBlocks == 8 ? 14 : 8;
+                double ms = trial(t, kIters);
+                if (ms < bestMs) { bestMs = ms; best = t; }
+            }
             // resident traversal blocks per SM
             int m = traceMaxBlocksPerSM(toTrace(best));
             for (int bps : {m / 2, (3 * m) / 4}) {
                 if (bps < 1 || bps >= m) continue;
                 SstTuning t = best;
                 t.traceBlocksPerSM = bps;
-                double ms = trial(t, trialIterations);
+                double ms = trial(t, kIters);
                 if (ms < bestMs) { bestMs = ms; best = t; }
             }
             // wave capacity: the trials hold about four waves of the largest candidate (within the

@@ -376,13 +376,18 @@ void launch_film_fold(const DevJob* jobs, const WaveChunk* chunks, const WaveDes
     k_film_fold<<<grid, 256, 0, s>>>(jobs, chunks, waves, curWave, samples, st, advance);
 }
 
-void launch_shade(int ns, bool adj, bool generic, const DevJob* jobs, const PathBuf& A, const PathBuf& B, const float4* hits, float4* nee,
-                  float4* neeG, int cap, float4* shRo, float4* shRd, int* shTgt, uint32_t* shJob, const int* nIn, int* nOut, int* nSh, float* samples,
-                  DevStats* stats, int maxItems, cudaStream_t s) {
+void launch_shade(int ns, bool adj, bool generic, int shadeBlocks, const DevJob* jobs, const PathBuf& A, const PathBuf& B, const float4* hits,
+                  float4* nee, float4* neeG, int cap, float4* shRo, float4* shRd, int* shTgt, uint32_t* shJob, const int* nIn, int* nOut, int* nSh,
+                  float* samples, DevStats* stats, int maxItems, cudaStream_t s) {
     int grid = (maxItems + 127) / 128;
     if (grid == 0) return;
     if (!generic && !adj && ns == 1) {
         k_shade<1, false, false><<<grid, 128, 0, s>>>(jobs, A, B, hits, nee, neeG, cap, shRo, shRd, shTgt, shJob, nIn, nOut, nSh, samples, stats, PyrArgs{});
+        return;
+    }
+    if (generic && !adj && ns == 1 && shadeBlocks == SST_SHADE_GEN_DENSE_BLOCKS) {
+        k_shade<1, false, true, false, SST_SHADE_GEN_DENSE_BLOCKS><<<grid, 128, 0, s>>>(jobs, A, B, hits, nee, neeG, cap, shRo, shRd, shTgt, shJob, nIn, nOut,
+                                                                                     nSh, samples, stats, PyrArgs{});
         return;
     }
 #define SST_SHADE_CASE(N)                                                                                                                    \

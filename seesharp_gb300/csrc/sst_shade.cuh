@@ -16,14 +16,19 @@ namespace cg = cooperative_groups;
 // shade 18% faster than the unconstrained 131-register build on the 1M-triangle scene and are
 // the fastest cap on the Cornell box; the adjoint variant is fastest at 16 blocks (32 registers).
 // SST_SHADE_MIN_BLOCKS is the cap of the variant without GenericMaterials (8 is fastest there:
-// 10, 12 and 16 blocks shade the Cornell box 15-42% slower); SST_SHADE_GEN_MIN_BLOCKS the one of
-// the forward variants with them (14 blocks, 36 registers: 6% faster shading than 8 on the
-// 1M-triangle scene, the same as 16).
+// 10, 12 and 16 blocks shade the Cornell box 15-42% slower).  The forward variant with
+// GenericMaterials is compiled twice, and the launch tuning picks one per context: for
+// SST_SHADE_GEN_MIN_BLOCKS (8, 64 registers; the default) and for SST_SHADE_GEN_DENSE_BLOCKS (14,
+// 32 registers).  The dense build shades the 1M-triangle sphere field 6% faster; on the Cornell box
+// with generic boxes it renders 19% slower, because its spills outgrow the caches.
 #ifndef SST_SHADE_MIN_BLOCKS
 #define SST_SHADE_MIN_BLOCKS 8
 #endif
 #ifndef SST_SHADE_GEN_MIN_BLOCKS
-#define SST_SHADE_GEN_MIN_BLOCKS 14
+#define SST_SHADE_GEN_MIN_BLOCKS 8
+#endif
+#ifndef SST_SHADE_GEN_DENSE_BLOCKS
+#define SST_SHADE_GEN_DENSE_BLOCKS 14
 #endif
 #ifndef SST_SHADE_ADJ_MIN_BLOCKS
 #define SST_SHADE_ADJ_MIN_BLOCKS 16
@@ -80,8 +85,10 @@ SST_D int aggAppend(int* counter) {
 // GEN = false: a wave without GenericMaterials (the generic code is not compiled in, which keeps
 // the kernel's instruction footprint small).
 // PYR = true: the technique pyramids (PathTracer.RenderTechniquePyramid) are filled as well.
-template <int NS, bool ADJ, bool GEN, bool PYR = false>
-__global__ void __launch_bounds__(128, ADJ ? SST_SHADE_ADJ_MIN_BLOCKS : (GEN ? SST_SHADE_GEN_MIN_BLOCKS : SST_SHADE_MIN_BLOCKS)) k_shade(const DevJob* __restrict__ jobs, PathBuf A, PathBuf B,
+// MINB: the resident blocks per SM the variant is compiled for.
+template <int NS, bool ADJ, bool GEN, bool PYR = false,
+          int MINB = (ADJ ? SST_SHADE_ADJ_MIN_BLOCKS : (GEN ? SST_SHADE_GEN_MIN_BLOCKS : SST_SHADE_MIN_BLOCKS))>
+__global__ void __launch_bounds__(128, MINB) k_shade(const DevJob* __restrict__ jobs, PathBuf A, PathBuf B,
                                                                    const float4* __restrict__ hits, float4* nee, float4* neeG, int cap,
                                                                    float4* shRo, float4* shRd, int* shTgt, uint32_t* shJob, const int* nIn,
                                                                    int* nOut, int* nSh, float* samples, DevStats* stats, PyrArgs pyrA) {
