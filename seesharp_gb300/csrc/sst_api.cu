@@ -114,6 +114,40 @@ static void parallelRanges(size_t n, size_t minPerThread, F fn) {
     for (auto& x : th) x.join();
 }
 
+// Faults in the pages of host output buffers on a helper thread while the GPU renders, so that the
+// read-back afterwards runs at link speed.  A device-to-host copy into pages the process has not
+// touched yet (a fresh numpy or malloc buffer) is bound by page faults: on the Grace host the 71 MB
+// of film, denoiser layers and outlier cache of a 1024x1024 render took 10 ms that way, against
+// 0.4 ms into touched pages.  Each page is read and the same byte written back, so the contents
+// (the input of a resumed render) are unchanged.
+class HostPrefault {
+public:
+    void add(void* p, size_t bytes) {
+        if (p && bytes) bufs_.push_back({static_cast<char*>(p), bytes});
+    }
+    void start() {
+        if (!bufs_.empty()) th_ = std::thread([this] { run(); });
+    }
+    void finish() {
+        if (th_.joinable()) th_.join();
+    }
+    ~HostPrefault() { finish(); }
+
+private:
+    void run() {
+        const size_t step = 4096;
+        for (auto& b : bufs_) {
+            volatile char* c = b.first;
+            for (size_t off = 0; off < b.second; off += step) {
+                const char v = c[off];
+                c[off] = v;
+            }
+        }
+    }
+    std::vector<std::pair<char*, size_t>> bufs_;
+    std::thread th_;
+};
+
 // ---------------------------------------------------------------------------------------------
 // context
 // ---------------------------------------------------------------------------------------------
@@ -1453,6 +1487,9 @@ int sst_render(sst_scene* s, const SstPathTracerParams* p, float* film, int32_t 
         }
         CUDA_CHECK(cudaStreamSynchronize(c->stream));
         double fbMs = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - tfb0).count();
+        HostPrefault prefault;
+        if (memory != SST_MEM_DEVICE) prefault.add(film, filmBytes);
+        prefault.start();
         if (p->firstIteration < p->totalSpp) {
             std::vector<JobIn> jobs(1);
             jobs[0].s = s;
@@ -1462,6 +1499,7 @@ int sst_render(sst_scene* s, const SstPathTracerParams* p, float* film, int32_t 
             jobs[0].iterEnd = p->totalSpp;
             renderJobs(c, jobs, &local);
         }
+        prefault.finish();
         auto tfb1 = std::chrono::steady_clock::now();
         if (memory != SST_MEM_DEVICE) CUDA_CHECK(cudaMemcpy(film, dFilm, filmBytes, cudaMemcpyDeviceToHost));
         fbMs += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - tfb1).count();
@@ -1817,7 +1855,24 @@ int sst_render_layers(sst_scene* s, const SstPathTracerParams* p, float* film, i
             lay.outW = c->layOutW.as<float>();
             lay.outIt = c->layOutIt.as<int>();
         }
+        HostPrefault prefault;
+        if (memory != SST_MEM_DEVICE) prefault.add(film, P * 12);
+        if (L->memory != SST_MEM_DEVICE) {
+            if (L->techPyramid) prefault.add(L->techPyramid, 2 * 2 * size_t(p->maxDepth) * P * 12);
+            if (nOut > 0) {
+                prefault.add(L->outlierWeight, P * size_t(nOut) * 4);
+                prefault.add(L->outlierIteration, P * size_t(nOut) * 4);
+            }
+            if (wantVar) prefault.add(L->varianceState, P * 8);
+            if (L->variance) prefault.add(L->variance, P * 4);
+            if (L->albedo) {
+                prefault.add(L->albedo, P * 12);
+                prefault.add(L->normal, P * 12);
+            }
+        }
+        prefault.start();
         if (first < S) renderJobs(c, jobs, &local);
+        prefault.finish();
         if (L->techPyramid) CUDA_CHECK(cudaMemcpyAsync(L->techPyramid, lay.pyr, 2 * 2 * size_t(p->maxDepth) * P * 12, out, st));
         if (nOut > 0) {
             const size_t n = P * size_t(nOut);
@@ -1969,7 +2024,12 @@ int sst_render_batch(sst_ctx* ctx, const SstRenderJob* jobs, int32_t numJobs, Ss
         batchJobs(ctx, jobs, numJobs, in, staged, false);
         CUDA_CHECK(cudaStreamSynchronize(ctx->stream));
         double fbMs = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+        HostPrefault prefault;
+        for (int j = 0; j < numJobs; ++j)
+            if (jobs[j].memory != SST_MEM_DEVICE) prefault.add(jobs[j].film, size_t(jobs[j].params.width) * jobs[j].params.height * 12);
+        prefault.start();
         renderJobs(ctx, in, &total);
+        prefault.finish();
         auto t1 = std::chrono::steady_clock::now();
         batchFilmsOut(ctx, jobs, numJobs, in);
         fbMs += std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t1).count();
