@@ -94,6 +94,29 @@ struct DevBuf {
     template <class T> T* as() const { return static_cast<T*>(p); }
 };
 
+// Page-locked host memory that only grows (one per context): staging for large uploads, so that
+// the copies run as asynchronous DMA and the pages stay resident from one scene commit to the next.
+struct PinnedBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+    PinnedBuf() = default;
+    PinnedBuf(const PinnedBuf&) = delete;
+    PinnedBuf& operator=(const PinnedBuf&) = delete;
+    ~PinnedBuf() { release(); }
+    void release() {
+        if (p) cudaFreeHost(p);
+        p = nullptr;
+        bytes = 0;
+    }
+    void ensure(size_t b) {
+        if (b <= bytes) return;
+        release();
+        CUDA_CHECK(cudaHostAlloc(&p, b, cudaHostAllocDefault));
+        bytes = b;
+    }
+    template <class T> T* as() const { return static_cast<T*>(p); }
+};
+
 // Runs fn(begin, end) over [0, n) in contiguous ranges on up to 16 host threads (one range per
 // thread, at least minPerThread items each).  fn must not throw.
 template <class F>
@@ -163,6 +186,10 @@ struct sst_ctx {
     int device = 0;
     cudaStream_t stream = nullptr;
     int numSMs = 0;
+    // scene commit: pinned staging of the packed triangle records and the BVH build's temporaries
+    // (kept across commits: no allocation or device-wide free per Scene.Prepare once they fit)
+    PinnedBuf commitStage;
+    DevBuf commitTri[4], commitOrder, commitScratch, commitScratch4;
     // wavefront buffers
     DevBuf pathA[9], pathB[9];
     DevBuf hits, nee, shRo, shRd, shTgt, shJob, counters, samples, stats, film;
@@ -536,8 +563,12 @@ static void commitScene(sst_scene* s, int W, int H) {
     }
     // per-triangle records in global order, packed by several host threads over triangle ranges
     // (uninitialised arrays: every entry is written, and each thread touches its own pages first)
-    std::unique_ptr<float4[]> trivG(new float4[3 * size_t(nt)]), triNG(new float4[nt]);
-    std::unique_ptr<int4[]> auxG(new int4[nt]), vtxG(new int4[nt]);
+    sst_ctx* const cx = s->ctx;
+    cx->commitStage.ensure(std::max<size_t>(1, 96 * size_t(nt)));
+    float4* const trivG = cx->commitStage.as<float4>();
+    float4* const triNG = trivG + 3 * size_t(nt);
+    int4* const auxG = reinterpret_cast<int4*>(triNG + nt);
+    int4* const vtxG = auxG + nt;
     parallelRanges(size_t(nt), 1 << 16, [&](size_t g0, size_t g1) {
         size_t mi = size_t(std::upper_bound(s->meshTriOffset.begin(), s->meshTriOffset.end(), int(g0)) - s->meshTriOffset.begin()) - 1;
         for (size_t g = g0; g < g1; ++g) {
@@ -572,11 +603,12 @@ static void commitScene(sst_scene* s, int W, int H) {
     s->triVtx.ensure(std::max<size_t>(1, sizeof(int4) * size_t(nt)));
     if (!hostBuild && nt > 0) {
         // GPU linear BVH (sst_bvh.cu) and a leaf-order gather on the device
-        DevBuf gTriv, gTriN, gAux, gVtx, order, scratch;
-        gTriv.upload(trivG.get(), 3 * size_t(nt), st);
-        gTriN.upload(triNG.get(), size_t(nt), st);
-        gAux.upload(auxG.get(), size_t(nt), st);
-        gVtx.upload(vtxG.get(), size_t(nt), st);
+        DevBuf &gTriv = cx->commitTri[0], &gTriN = cx->commitTri[1], &gAux = cx->commitTri[2], &gVtx = cx->commitTri[3];
+        DevBuf &order = cx->commitOrder, &scratch = cx->commitScratch;
+        gTriv.upload(trivG, 3 * size_t(nt), st);
+        gTriN.upload(triNG, size_t(nt), st);
+        gAux.upload(auxG, size_t(nt), st);
+        gVtx.upload(vtxG, size_t(nt), st);
         s->nodes.ensure(sizeof(float4) * 4 * size_t(std::max(1, nt - 1)));
         order.ensure(sizeof(int) * size_t(nt));
         size_t sb = lbvhScratchBytes(nt);
@@ -631,7 +663,7 @@ static void commitScene(sst_scene* s, int W, int H) {
     s->nNodes4 = 0;
     s->bvh4Depth = 0;
     if (s->nNodes > 0) {
-        DevBuf scratch4;
+        DevBuf& scratch4 = s->ctx->commitScratch4;
         s->nodes4.ensure(sizeof(float4) * 8 * size_t(s->nNodes));
         scratch4.ensure(bvh4ScratchBytes(s->nNodes));
         int rc = buildBvh4(s->nodes.as<float4>(), s->nNodes, s->nodes4.as<float4>(), scratch4.p, &s->nNodes4, &s->bvh4Depth, st);
