@@ -1597,7 +1597,8 @@ static void checkTuning(const SstTuning& t) {
     if (t.waveCapacity != 0 && (t.waveCapacity < 1024 || t.waveCapacity > (1 << 24)))
         fail(SST_ERR_INVALID_ARGUMENT, "waveCapacity must be 0 or in [1024, 2^24]");
     if (t.traceBlocksPerSM < 0 || t.traceBlocksPerSM > 64) fail(SST_ERR_INVALID_ARGUMENT, "traceBlocksPerSM must be in [0, 64]");
-    if (t.shadeBlocks != 8 && t.shadeBlocks != 14) fail(SST_ERR_INVALID_ARGUMENT, "shadeBlocks must be 8 or 14");
+    if (!shadeBlocksValid(t.shadeBlocks))
+        fail(SST_ERR_INVALID_ARGUMENT, "shadeBlocks must be 8 or " + std::to_string(shadeDenseBlocks()));
 }
 
 static SstTuning currentTuning(const sst_ctx* c) {
@@ -1695,7 +1696,7 @@ int sst_autotune(sst_scene* s, const SstPathTracerParams* p, int32_t trialIterat
             // occupancy build of the shade kernel with GenericMaterials
             {
                 SstTuning t = best;
-                t.shadeBlocks = best.shadeBlocks == 8 ? 14 : 8;
+                t.shadeBlocks = best.shadeBlocks == 8 ? shadeDenseBlocks() : 8;
                 double ms = trial(t, kIters);
                 if (ms < bestMs) { bestMs = ms; best = t; }
             }

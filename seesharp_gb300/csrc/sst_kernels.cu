@@ -376,6 +376,9 @@ void launch_film_fold(const DevJob* jobs, const WaveChunk* chunks, const WaveDes
     k_film_fold<<<grid, 256, 0, s>>>(jobs, chunks, waves, curWave, samples, st, advance);
 }
 
+int shadeDenseBlocks() { return SST_SHADE_GEN_DENSE_BLOCKS; }
+bool shadeBlocksValid(int b) { return b == SST_SHADE_GEN_MIN_BLOCKS || b == SST_SHADE_GEN_DENSE_BLOCKS; }
+
 void launch_shade(int ns, bool adj, bool generic, int shadeBlocks, const DevJob* jobs, const PathBuf& A, const PathBuf& B, const float4* hits,
                   float4* nee, float4* neeG, int cap, float4* shRo, float4* shRd, int* shTgt, uint32_t* shJob, const int* nIn, int* nOut, int* nSh,
                   float* samples, DevStats* stats, int maxItems, cudaStream_t s) {

@@ -39,8 +39,11 @@ void launch_trace_shadow(const TraceTuning& t, const DevJob* jobs, const uint32_
                          const int* count, int* work, float4* nee, DevStats* stats, cudaStream_t s);
 void launch_trace_query(const TraceTuning& t, const DevJob* jobs, const float4* ro, const float4* rd, const int* count, int* work, float4* hits,
                         int* occl, DevStats* stats, bool anyHit, cudaStream_t s);
-// shadeBlocks: the resident blocks per SM of the forward variant with GenericMaterials (8 or 14;
-// one shadow ray per technique has both builds, more shadow rays the 8-block one).
+// shadeBlocks: the resident blocks per SM of the forward variant with GenericMaterials: the
+// default build (8) or the dense one (shadeDenseBlocks()); one shadow ray per technique has both
+// builds, more shadow rays the default one.
+int shadeDenseBlocks();
+bool shadeBlocksValid(int blocks);
 void launch_shade(int ns, bool adj, bool generic, int shadeBlocks, const DevJob* jobs, const PathBuf& A, const PathBuf& B, const float4* hits,
                   float4* nee, float4* neeG, int cap, float4* shRo, float4* shRd, int* shTgt, uint32_t* shJob, const int* nIn, int* nOut, int* nSh,
                   float* samples, DevStats* stats, int maxItems, cudaStream_t s);
