@@ -562,8 +562,10 @@ def run_ours(args, cfg):
         return sc.native.render(params, film.data_ptr(), _native.SST_MEM_DEVICE)
 
     # launch configuration for this scene (sst_autotune: short trial renders, results unchanged)
+    if args.tuning:
+        _native.set_tuning(ctx, **json.loads(args.tuning))
     tuning, tune_s = _native.get_tuning(ctx), 0.0
-    if not args.no_autotune:
+    if not args.no_autotune and not args.tuning:
         t0 = time.perf_counter()
         tuning, _ = _native.autotune(sc.native, params, 2)
         tune_s = time.perf_counter() - t0
@@ -681,6 +683,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--tuning", default=None, help="pin the launch configuration (JSON of SstTuning fields; implies --no-autotune)")
     ap.add_argument("--width", type=int, default=None, help="override (profiling cases)")
     ap.add_argument("--height", type=int, default=None)
     ap.add_argument("--spp", type=int, default=None)
