@@ -193,6 +193,7 @@ struct sst_ctx {
     // wavefront buffers
     DevBuf pathA[9], pathB[9];
     DevBuf hits, nee, shRo, shRd, shTgt, shJob, counters, samples, stats, film;
+    DevBuf shadeOrderBuf;  // k_partition's shade order of the current queue (cap ints)
     DevBuf jobsBuf, chunksBuf, wavesBuf, curWave;
     DevBuf adjA[3], adjB[3], neeG;
     int cap = 0, shCap = 0, neeSlots = 0;
@@ -211,6 +212,7 @@ struct sst_ctx {
     TraceTuning trace;
     int waveCapacity = 0;  // 0: the default
     int shadeBlocks = 8;   // resident blocks per SM of the forward shade kernel with GenericMaterials: 8 or 14
+    int shadeOrder = 1;    // 1: each bounce's queue is shaded surface hits first (k_partition); 0: in queue order
     // kernel timing (sst_set_profiling)
     bool profiling = false;
     std::vector<cudaEvent_t> evPool;
@@ -811,6 +813,8 @@ static void bindPath(DevBuf* bufs, PathBuf& p, int cap) {
     p.prev = bufs[6].as<float4>();
     p.ro = bufs[7].as<float4>();
     p.rd = bufs[8].as<float4>();
+    p.order = nullptr;
+    p.neeIn = p.neeGIn = p.pyrGIn = nullptr;
 }
 
 static int defaultWaveCapacity() {
@@ -832,13 +836,14 @@ static void ensureWave(sst_ctx* c, int cap, int ns, Wave& w) {
     bindPath(c->pathA, w.wb.a, c->cap);
     bindPath(c->pathB, w.wb.b, c->cap);
     c->neeSlots = std::max(c->neeSlots, 2 * ns);
-    c->nee.ensure(size_t(c->cap) * 16 * c->neeSlots);
+    c->nee.ensure(2 * size_t(c->cap) * 16 * c->neeSlots);  // two buffers: read and written bounce by bounce
     size_t shCap = size_t(c->cap) * 2 * ns;
     c->shRo.ensure(shCap * 16);
     c->shRd.ensure(shCap * 16);
     c->shTgt.ensure(shCap * 4);
     c->shJob.ensure(shCap * 4);
     c->counters.ensure(sizeof(int) * kNumCounters);
+    c->shadeOrderBuf.ensure(size_t(c->cap) * 4);
     c->stats.ensure(sizeof(DevStats));
     w.wb.hits = c->hits.as<float4>();
     w.wb.nee = c->nee.as<float4>();
@@ -847,6 +852,7 @@ static void ensureWave(sst_ctx* c, int cap, int ns, Wave& w) {
     w.wb.shTgt = c->shTgt.as<int>();
     w.wb.shJob = c->shJob.as<uint32_t>();
     w.wb.counters = c->counters.as<int>();
+    w.wb.order = c->shadeOrderBuf.as<int>();
     w.wb.cap = c->cap;
     w.wb.shCap = int(shCap);
 }
@@ -954,7 +960,7 @@ static void renderJobs(sst_ctx* c, std::vector<JobIn>& jobs, SstRenderStats* out
         for (int k = 0; k < 2; ++k) { c->adjA[k].ensure(cp * 16); c->adjB[k].ensure(cp * 16); }
         c->adjA[2].ensure(cp * 48);
         c->adjB[2].ensure(cp * 48);
-        c->neeG.ensure(cp * 48 * 2 * ns);
+        c->neeG.ensure(2 * cp * 48 * 2 * ns);
         w.wb.a.adjL = c->adjA[0].as<float4>(); w.wb.a.adjD = c->adjA[1].as<float4>(); w.wb.a.adjP = c->adjA[2].as<float4>();
         w.wb.b.adjL = c->adjB[0].as<float4>(); w.wb.b.adjD = c->adjB[1].as<float4>(); w.wb.b.adjP = c->adjB[2].as<float4>();
         w.wb.neeG = c->neeG.as<float4>();
@@ -972,7 +978,7 @@ static void renderJobs(sst_ctx* c, std::vector<JobIn>& jobs, SstRenderStats* out
     if (anyAov) c->aovSamples.ensure(size_t(w.wb.cap) * 24);
     if (pyramid && replay) fail(SST_ERR_UNSUPPORTED, "the technique pyramid is not available in the adjoint replay");
     // technique pyramid: the payload of every NEE slot
-    if (pyramid) c->pyrG.ensure(size_t(w.wb.cap) * 16 * 2 * ns);
+    if (pyramid) c->pyrG.ensure(2 * size_t(w.wb.cap) * 16 * 2 * ns);
     // job table
     std::vector<DevJob> hj(jobs.size());
     for (size_t k = 0; k < jobs.size(); ++k) {
@@ -1019,6 +1025,7 @@ static void renderJobs(sst_ctx* c, std::vector<JobIn>& jobs, SstRenderStats* out
         }
         PathBuf A = w.wb.a, B = w.wb.b;
         int maxItems = items;
+        float4* curNee = w.wb.nee;  // the next-event slots the current bounce writes
         for (int d = 1; d <= maxDepth; ++d) {
             {
                 KTimer kt(c, 1);
@@ -1026,20 +1033,42 @@ static void renderJobs(sst_ctx* c, std::vector<JobIn>& jobs, SstRenderStats* out
             }
             {
                 KTimer kt(c, 2);
+                PathBuf Ao = A;
+                if (c->shadeOrder) {
+                    launch_partition(A.depth, w.wb.hits, cnt + kCntQueue + d, w.wb.order, cnt + kCntPart + 2 * d, maxItems, st);
+                    Ao.order = w.wb.order;
+                }
+                // next-event slots: read the buffer the previous bounce wrote, write the other
+                const size_t neeHalf = size_t(w.wb.cap) * size_t(c->neeSlots);
+                float4* neeOut = w.wb.nee + (d & 1) * neeHalf;
+                Ao.neeIn = w.wb.nee + ((d + 1) & 1) * neeHalf;
+                float4* neeGOut = nullptr;
+                if (w.wb.neeG) {
+                    const size_t gHalf = size_t(w.wb.cap) * 3 * 2 * size_t(ns);
+                    neeGOut = w.wb.neeG + (d & 1) * gHalf;
+                    Ao.neeGIn = w.wb.neeG + ((d + 1) & 1) * gHalf;
+                }
+                float4* pyrGOut = nullptr;
+                if (pyramid) {
+                    const size_t pHalf = size_t(w.wb.cap) * 2 * size_t(ns);
+                    pyrGOut = c->pyrG.as<float4>() + (d & 1) * pHalf;
+                    Ao.pyrGIn = c->pyrG.as<float4>() + ((d + 1) & 1) * pHalf;
+                }
+                curNee = neeOut;
                 if (pyramid)
-                    launch_shade_pyramid(ns, dj, A, B, w.wb.hits, w.wb.nee, w.wb.cap, w.wb.shRo, w.wb.shRd, w.wb.shTgt, w.wb.shJob, cnt + kCntQueue + d,
+                    launch_shade_pyramid(ns, dj, Ao, B, w.wb.hits, neeOut, w.wb.cap, w.wb.shRo, w.wb.shRd, w.wb.shTgt, w.wb.shJob, cnt + kCntQueue + d,
                                          cnt + kCntQueue + d + 1, cnt + kCntShadow + d, c->samples.as<float>(), dstats,
-                                         PyrArgs{dch, dwv, dcur, c->pyrG.as<float4>()}, maxItems, st);
+                                         PyrArgs{dch, dwv, dcur, pyrGOut}, maxItems, st);
                 else
-                    launch_shade(ns, replay, generic, c->shadeBlocks, dj, A, B, w.wb.hits, w.wb.nee, w.wb.neeG, w.wb.cap, w.wb.shRo, w.wb.shRd, w.wb.shTgt, w.wb.shJob,
+                    launch_shade(ns, replay, generic, c->shadeBlocks, dj, Ao, B, w.wb.hits, neeOut, neeGOut, w.wb.cap, w.wb.shRo, w.wb.shRd, w.wb.shTgt, w.wb.shJob,
                                  cnt + kCntQueue + d, cnt + kCntQueue + d + 1, cnt + kCntShadow + d, c->samples.as<float>(), dstats, maxItems, st);
             }
             {
                 KTimer kt(c, 3);
-                launch_trace_shadow(c->trace, dj, w.wb.shJob, w.wb.shRo, w.wb.shRd, w.wb.shTgt, cnt + kCntShadow + d, cnt + kCntWork + 2 * d + 1, w.wb.nee,
+                launch_trace_shadow(c->trace, dj, w.wb.shJob, w.wb.shRo, w.wb.shRd, w.wb.shTgt, cnt + kCntShadow + d, cnt + kCntWork + 2 * d + 1, curNee,
                                     dstats, st);
             }
-            launches += 3;  // closest hit, shade, shadow rays
+            launches += c->shadeOrder ? 4 : 3;  // closest hit, shade order, shade, shadow rays
             std::swap(A, B);
             if (allowEarlyExit && d >= 6 && d < maxDepth) {
                 // stop early once the queue is empty (long MaxDepth with Russian roulette)
@@ -1597,6 +1626,7 @@ static void checkTuning(const SstTuning& t) {
     if (t.waveCapacity != 0 && (t.waveCapacity < 1024 || t.waveCapacity > (1 << 24)))
         fail(SST_ERR_INVALID_ARGUMENT, "waveCapacity must be 0 or in [1024, 2^24]");
     if (t.traceBlocksPerSM < 0 || t.traceBlocksPerSM > 64) fail(SST_ERR_INVALID_ARGUMENT, "traceBlocksPerSM must be in [0, 64]");
+    if (t.shadeOrder != 0 && t.shadeOrder != 1) fail(SST_ERR_INVALID_ARGUMENT, "shadeOrder must be 0 or 1");
     if (!shadeBlocksValid(t.shadeBlocks))
         fail(SST_ERR_INVALID_ARGUMENT, "shadeBlocks must be 8 or " + std::to_string(shadeDenseBlocks()));
 }
@@ -1610,6 +1640,7 @@ static SstTuning currentTuning(const sst_ctx* c) {
     t.traceBvhWidth = c->trace.width;
     t.traceRefillIdle = c->trace.refillIdle;
     t.shadeBlocks = c->shadeBlocks;
+    t.shadeOrder = c->shadeOrder;
     return t;
 }
 
@@ -1627,6 +1658,7 @@ int sst_set_tuning(sst_ctx* c, const SstTuning* t) {
         c->trace = toTrace(*t);
         c->waveCapacity = t->waveCapacity;
         c->shadeBlocks = t->shadeBlocks;
+        c->shadeOrder = t->shadeOrder;
     });
 }
 
@@ -1650,6 +1682,7 @@ int sst_autotune(sst_scene* s, const SstPathTracerParams* p, int32_t trialIterat
             c->trace = toTrace(t);
             c->waveCapacity = t.waveCapacity;
             c->shadeBlocks = t.shadeBlocks;
+            c->shadeOrder = t.shadeOrder;
             double best = 1e300;
             for (int r = 0; r < 2; ++r) {
                 std::vector<JobIn> jobs(1);
@@ -1700,6 +1733,13 @@ int sst_autotune(sst_scene* s, const SstPathTracerParams* p, int32_t trialIterat
                 double ms = trial(t, kIters);
                 if (ms < bestMs) { bestMs = ms; best = t; }
             }
+            // shade order: surface hits first, or queue order
+            {
+                SstTuning t = best;
+                t.shadeOrder = 1 - best.shadeOrder;
+                double ms = trial(t, kIters);
+                if (ms < bestMs) { bestMs = ms; best = t; }
+            }
             // resident traversal blocks per SM
             int m = traceMaxBlocksPerSM(toTrace(best));
             for (int bps : {m / 2, (3 * m) / 4}) {
@@ -1731,12 +1771,16 @@ int sst_autotune(sst_scene* s, const SstPathTracerParams* p, int32_t trialIterat
         } catch (...) {
             c->trace = toTrace(start);
             c->waveCapacity = start.waveCapacity;
+            c->shadeBlocks = start.shadeBlocks;
+            c->shadeOrder = start.shadeOrder;
             c->profiling = prof;
             throw;
         }
         c->profiling = prof;
         c->trace = toTrace(best);
         c->waveCapacity = best.waveCapacity;
+        c->shadeBlocks = best.shadeBlocks;
+        c->shadeOrder = best.shadeOrder;
         if (chosen) *chosen = best;
         if (bestTrialMs) *bestTrialMs = bestMs;
     });

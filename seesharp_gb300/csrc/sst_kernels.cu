@@ -376,6 +376,38 @@ void launch_film_fold(const DevJob* jobs, const WaveChunk* chunks, const WaveDes
     k_film_fold<<<grid, 256, 0, s>>>(jobs, chunks, waves, curWave, samples, st, advance);
 }
 
+// Shade order of one bounce's queue: the paths that hit a surface first, then the misses and the
+// finished paths, whose lanes only add the background or resolve pending next-event samples.  In
+// queue order the expensive surface shading runs in every warp with the cheap lanes idle beside
+// it; ordered, it runs in fewer, fuller warps.  Every path's result is the same in any order.
+// counts[0], counts[1]: this bounce's append counters (zeroed with the wave's counters).
+__global__ void __launch_bounds__(256) k_partition(const uint32_t* __restrict__ depth, const float4* __restrict__ hits, const int* nIn, int* order,
+                                                    int* counts) {
+    const int n = *nIn;
+    if ((int)(blockIdx.x * blockDim.x) >= n) return;  // whole blocks: every warp below is complete
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool valid = i < n;
+    const bool surf = valid && !(depth[i] & kDoneFlag) && __float_as_int(hits[i].w) >= 0;
+    const unsigned ms = __ballot_sync(0xffffffffu, surf), mo = __ballot_sync(0xffffffffu, valid && !surf);
+    const int lane = threadIdx.x & 31;
+    int bs = 0, bo = 0;
+    if (lane == 0) {
+        if (ms) bs = atomicAdd(&counts[0], __popc(ms));
+        if (mo) bo = atomicAdd(&counts[1], __popc(mo));
+    }
+    bs = __shfl_sync(0xffffffffu, bs, 0);
+    bo = __shfl_sync(0xffffffffu, bo, 0);
+    const unsigned below = (1u << lane) - 1u;
+    if (surf) order[bs + __popc(ms & below)] = i;                   // from the front
+    else if (valid) order[n - 1 - (bo + __popc(mo & below))] = i;   // from the back
+}
+
+void launch_partition(const uint32_t* depth, const float4* hits, const int* nIn, int* order, int* counts, int maxItems, cudaStream_t s) {
+    const int grid = (maxItems + 255) / 256;
+    if (grid == 0) return;
+    k_partition<<<grid, 256, 0, s>>>(depth, hits, nIn, order, counts);
+}
+
 int shadeDenseBlocks() { return SST_SHADE_GEN_DENSE_BLOCKS; }
 bool shadeBlocksValid(int b) { return b == SST_SHADE_GEN_MIN_BLOCKS || b == SST_SHADE_GEN_DENSE_BLOCKS; }
 

@@ -43,6 +43,8 @@ void launch_trace_query(const TraceTuning& t, const DevJob* jobs, const float4* 
 // default build (8) or the dense one (shadeDenseBlocks()); one shadow ray per technique has both
 // builds, more shadow rays the default one.
 int shadeDenseBlocks();
+// Writes the shade order of a bounce's queue (surface hits first) into order[0, *nIn).
+void launch_partition(const uint32_t* depth, const float4* hits, const int* nIn, int* order, int* counts, int maxItems, cudaStream_t s);
 bool shadeBlocksValid(int blocks);
 void launch_shade(int ns, bool adj, bool generic, int shadeBlocks, const DevJob* jobs, const PathBuf& A, const PathBuf& B, const float4* hits,
                   float4* nee, float4* neeG, int cap, float4* shRo, float4* shRd, int* shTgt, uint32_t* shJob, const int* nIn, int* nOut, int* nSh,

@@ -94,8 +94,9 @@ __global__ void __launch_bounds__(128, MINB) k_shade(const DevJob* __restrict__ 
                                                                    int* nOut, int* nSh, float* samples, DevStats* stats, PyrArgs pyrA) {
     const int n = *nIn;
     if ((int)(blockIdx.x * blockDim.x) >= n) return;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const bool valid = i < n;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool valid = t < n;
+    const int i = (valid && A.order) ? A.order[t] : t;  // the queued path this thread shades
 
     bool cont = false;
     uint32_t job = 0;
@@ -148,10 +149,10 @@ __global__ void __launch_bounds__(128, MINB) k_shade(const DevJob* __restrict__ 
             for (int k = 0; k < 2 * NS; ++k) {
                 if (!(pm & (1u << k))) continue;
                 size_t slot = (size_t)k * cap + i;
-                float4 nv = nee[slot];
+                float4 nv = A.neeIn[slot];
                 if (nv.w == 0.0f) continue;  // occluded
                 radiance = radiance + f3(nv);
-                float4 g0 = neeG[3 * slot], g1 = neeG[3 * slot + 1], g2 = neeG[3 * slot + 2];
+                float4 g0 = A.neeGIn[3 * slot], g1 = A.neeGIn[3 * slot + 1], g2 = A.neeGIn[3 * slot + 2];
                 addBaseGrad(adj, __float_as_int(g0.x), g0.y, g0.z, g0.w);
                 addRoughGrad(adj, __float_as_int(g1.x), g1.y);
                 addEmitterGrad(adj, __float_as_int(g1.z), f3(g2));
@@ -172,10 +173,10 @@ __global__ void __launch_bounds__(128, MINB) k_shade(const DevJob* __restrict__ 
 #pragma unroll
             for (int k = 0; k < 2 * NS; ++k) {
                 if (!(pm & (1u << k))) continue;
-                const float4 nv = nee[(size_t)k * cap + i];
+                const float4 nv = A.neeIn[(size_t)k * cap + i];
                 radiance = radiance + f3(nv);
                 if (PYR && nv.w != 0.0f) {  // visible: the next-event sample of length `depth` counts
-                    const float4 pg = pyrA.pyrG[(size_t)k * cap + i];
+                    const float4 pg = A.pyrGIn[(size_t)k * cap + i];
                     pyrAdd(jobs[job], pyrPixel, (int)(dw & kDepthMask), true, f3(pg), pg.w);
                 }
             }

@@ -217,6 +217,15 @@ struct PathBuf {
     float4* adjL;      // path radiance from the forward pass, w = base-colour target (int bits)
     float4* adjD;      // dLoss/dSample per channel, w = roughness target (int bits)
     float4* adjP;      // 3 float4 per path: d ln f_c / d(base r, g, b, roughness) of the pending BSDF factor
+    // shade input only: the order in which the shade kernel's threads take the queued paths
+    // (thread t shades path order[t]); NULL: thread t shades path t
+    const int* order;
+    // shade input only: the next-event slots of the queued paths, written by the previous bounce.
+    // The shade kernel writes the next bounce's slots into the other buffer of the pair, so no
+    // thread reads a slot that another thread of the same launch writes.
+    const float4* neeIn;
+    const float4* neeGIn;  // adjoint payloads of those slots
+    const float4* pyrGIn;  // technique-pyramid payloads of those slots
 };
 
 constexpr uint32_t kDepthMask = 0xFFFFu;
@@ -234,16 +243,19 @@ struct WaveBuffers {
     int* shTgt;          // nee slot index
     uint32_t* shJob;     // render job of the shadow ray
     int* counters;       // per bounce queue lengths and work counters
+    int* order;          // shade order of the current queue (k_partition)
     int cap;             // paths per wave
     int shCap;           // shadow queue capacity
 };
 
 // Counter layout (ints): [0, 1024) queue length per depth; [1024, 2048) shadow-queue length per
-// depth; [2048, 4096) work-fetch counters of the persistent traversal kernels (two per depth).
+// depth; [2048, 4096) work-fetch counters of the persistent traversal kernels (two per depth);
+// [4096, 6144) append counters of the shade-order partition (two per depth).
 constexpr int kMaxPathDepth = 1000;
 constexpr int kCntQueue = 0;
 constexpr int kCntShadow = 1024;
 constexpr int kCntWork = 2048;
-constexpr int kNumCounters = 4096;
+constexpr int kCntPart = 4096;
+constexpr int kNumCounters = 6144;
 
 }  // namespace sst

@@ -502,9 +502,9 @@ def test_graph_replay_equals_plain_launches():
 
 def test_tuning_and_autotune_leave_images_and_queries_unchanged():
     """Wave capacity, traversal block size, shared stack entries, resident traversal blocks, the
-    refill threshold of the 4-wide traversal and the shade kernel's occupancy build change the launch
-    shape and the order in which rays are traced only: the film and the query results stay bitwise
-    the same."""
+    refill threshold of the 4-wide traversal, the shade kernel's occupancy build and the shade order
+    change the launch shape and the order in which rays and paths are processed only: the film and
+    the query results stay bitwise the same."""
     from seesharp_gb300 import autotune
     sc = workloads.sphere_field(12, 96, 80, level=3)
     sc.Prepare()
@@ -520,11 +520,11 @@ def test_tuning_and_autotune_leave_images_and_queries_unchanged():
         ref, st0 = render_gpu(sc, 4, 6)
         hits0, occ0 = sc.native.trace(rays), sc.native.occluded(rays)
         assert st0.numKernelLaunches > 0
-        for t in [dict(traceBlock=64, traceStackShared=16, traceBlocksPerSM=1, waveCapacity=4096, traceBvhWidth=2, traceRefillIdle=20, shadeBlocks=14),
-                  dict(traceBlock=256, traceStackShared=32, traceBlocksPerSM=0, waveCapacity=0, traceBvhWidth=4, traceRefillIdle=32, shadeBlocks=8),
-                  dict(traceBlock=64, traceStackShared=16, traceBlocksPerSM=3, waveCapacity=8192, traceBvhWidth=4, traceRefillIdle=1, shadeBlocks=14),
-                  dict(traceBlock=128, traceStackShared=24, traceBlocksPerSM=2, waveCapacity=1 << 20, traceBvhWidth=4, traceRefillIdle=12, shadeBlocks=8),
-                  dict(traceBlock=128, traceStackShared=24, traceBlocksPerSM=2, waveCapacity=1 << 20, traceBvhWidth=2, traceRefillIdle=8, shadeBlocks=14)]:
+        for t in [dict(traceBlock=64, traceStackShared=16, traceBlocksPerSM=1, waveCapacity=4096, traceBvhWidth=2, traceRefillIdle=20, shadeBlocks=14, shadeOrder=0),
+                  dict(traceBlock=256, traceStackShared=32, traceBlocksPerSM=0, waveCapacity=0, traceBvhWidth=4, traceRefillIdle=32, shadeBlocks=8, shadeOrder=1),
+                  dict(traceBlock=64, traceStackShared=16, traceBlocksPerSM=3, waveCapacity=8192, traceBvhWidth=4, traceRefillIdle=1, shadeBlocks=14, shadeOrder=1),
+                  dict(traceBlock=128, traceStackShared=24, traceBlocksPerSM=2, waveCapacity=1 << 20, traceBvhWidth=4, traceRefillIdle=12, shadeBlocks=8, shadeOrder=0),
+                  dict(traceBlock=128, traceStackShared=24, traceBlocksPerSM=2, waveCapacity=1 << 20, traceBvhWidth=2, traceRefillIdle=8, shadeBlocks=14, shadeOrder=1)]:
             _native.set_tuning(ctx, **t)
             assert _native.get_tuning(ctx) == t
             img, _ = render_gpu(sc, 4, 6)
@@ -539,7 +539,8 @@ def test_tuning_and_autotune_leave_images_and_queries_unchanged():
         img, _ = render_gpu(sc, 4, 6)
         assert np.array_equal(img, ref)
         for bad in (dict(traceBlock=96), dict(traceStackShared=20), dict(waveCapacity=100), dict(traceBlocksPerSM=-1), dict(traceBvhWidth=8),
-                    dict(traceRefillIdle=0), dict(traceRefillIdle=33), dict(shadeBlocks=12)):
+                    dict(traceRefillIdle=0), dict(traceRefillIdle=33), dict(shadeBlocks=12),
+                    dict(shadeOrder=2)):
             with pytest.raises(_native.SstError):
                 _native.set_tuning(ctx, **bad)
             assert _native.get_tuning(ctx) == chosen
