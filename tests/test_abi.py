@@ -43,6 +43,18 @@ def test_struct_layouts_match_header():
     assert ctypes.sizeof(_native.SstRenderStats) == 80
 
 
+def test_tuning_struct_matches_header():
+    """SstTuning grows with the launch options; the ctypes mirror must list the header's int32
+    fields in the header's order."""
+    text = open(os.path.join(ROOT, "include", "sst.h")).read()
+    body = re.search(r"typedef struct SstTuning \{(.*?)\} SstTuning;", text, flags=re.S).group(1)
+    body = re.sub(r"/\*.*?\*/", "", body, flags=re.S)
+    fields = re.findall(r"int32_t\s+(\w+)\s*;", body)
+    assert [n for n, _ in _native.SstTuning._fields_] == fields
+    assert all(t is ctypes.c_int32 for _, t in _native.SstTuning._fields_)
+    assert ctypes.sizeof(_native.SstTuning) == 4 * len(fields)
+
+
 def test_version_and_error_buffer(lib):
     maj, mnr = ctypes.c_int32(), ctypes.c_int32()
     assert lib.sst_version(ctypes.byref(maj), ctypes.byref(mnr)) == 0
