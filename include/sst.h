@@ -9,10 +9,13 @@
  * pointers on the context's device; SST_MEM_HOST buffers are ordinary host memory.
  *
  * One host thread at a time per context.  Calls are synchronous: they return after the GPU work
- * they issued has finished.
+ * they issued has finished.  Device arrays (SST_MEM_DEVICE) are read and written on the context's
+ * own stream, which is not ordered with the caller's streams: the caller finishes its writes to an
+ * input before the call (for example by synchronizing the stream that wrote it), and the outputs are
+ * complete when the call returns.
  *
  * Each declaration names the SeeSharp interface it replaces (paths relative to the SeeSharp
- * project root).  The C# binding a maintainer adds to SeeSharp is shown in INTEGRATION.md.
+ * project root).
  */
 #ifndef SST_H
 #define SST_H
@@ -99,8 +102,14 @@ typedef struct SstRenderStats {
     uint64_t numRays;       /* RayTracerStats.NumRays */
     uint64_t numShadowRays; /* RayTracerStats.NumShadowRays */
     uint64_t numNanOrInf;   /* FrameBuffer.NaNWarnings count */
-    int32_t nanPixel[4];    /* first logged (pixel index) entries, -1 if unused */
-    int32_t nanIteration[4];
+    int32_t nanPixel[4];    /* FrameBuffer.NaNWarnings: the first entries in (iteration, pixel index) order, -1 if unused */
+    int32_t nanIteration[4]; /* their 1-based iteration (FrameBuffer.CurIteration) */
+    /* ShadingStats (Shading/ShadingStats.cs:5-9, MetaData["ShadingStats"], PathTracer.cs:256): the material
+     * Evaluate / Sample / Pdf calls the reference PathTracer makes for the rendered paths.  Counted only while
+     * sst_set_shading_stats is on for the context (zero otherwise). */
+    uint64_t numMaterialEval;
+    uint64_t numMaterialSample;
+    uint64_t numMaterialPdf;
 } SstRenderStats;
 
 /* ---- library / context --------------------------------------------------------------------- */
@@ -215,7 +224,9 @@ int sst_autotune(sst_scene* scene, const SstPathTracerParams* params, int32_t tr
  *  - All calls on a device share the array, so two calls whose GPU work overlapped would race.
  *    The function holds a process-wide lock for the whole call and returns only after its GPU
  *    work has finished, so its own calls in one process never overlap.
- *  - rays / occluded are host arrays (SST_MEM_HOST) or device arrays (SST_MEM_DEVICE). */
+ *  - rays / occluded are host arrays (SST_MEM_HOST) or device arrays (SST_MEM_DEVICE).  Device arrays
+ *    are accessed on the context's stream, with no ordering against the caller's streams: finish
+ *    the writes to `rays` before the call; `occluded` is complete when the call returns. */
 #define SST_NOALLOC_MAX_RAYS 65536
 int sst_occluded_noalloc(sst_scene* scene, const SstRay* rays, int32_t n, int32_t* occluded, int32_t memory);
 
@@ -368,6 +379,16 @@ int sst_backward(sst_scene* scene, const SstPathTracerParams* params, const floa
 #define SST_KERNEL_CLASSES 5
 int sst_set_profiling(sst_ctx* ctx, int32_t enable);
 int sst_get_kernel_times(sst_ctx* ctx, double* ms, int64_t* launches, int64_t* items, int32_t numClasses);
+
+/* ---- shading statistics (ShadingStatCounter, Shading/ShadingStats.cs:11-33) ---------------------
+ * While enabled, renders on the context count the material calls that the reference PathTracer makes
+ * for the same paths (SstRenderStats.numMaterial*): a BSDF sample per sampled direction (plus an
+ * evaluation and a pdf for a DiffuseMaterial, whose Sample calls both), and an evaluation and a pdf
+ * per next-event sample whose shadow ray finds the light visible (PathTracer.cs:428-430, 467-477).
+ * The wavefront evaluates next-event BSDFs before their shadow rays are traced and traces only the
+ * samples that contribute, so the counts need the visibility of the others as well: while enabled,
+ * every next-event sample's shadow ray is traced.  Images are unchanged.  Disabled by default. */
+int sst_set_shading_stats(sst_ctx* ctx, int32_t enable);
 
 /* ---- function-level entry points used by the parity tests --------------------------------------
  * Each runs the device code of one reference function on a batch of inputs (host arrays). */

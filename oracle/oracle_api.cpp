@@ -103,7 +103,7 @@ template <class T> SurfacePoint<T> PointFrom(const float* pt) {
 template <class T> void renderRows(Handle* h, const PTParams& P, uint32_t sampleIndex, float* film, int nthreads, uint64_t* stats, bool runningMean) {
     const Scene<T>& sc = S<T>(h);
     std::atomic<int> nextRow(0);
-    std::atomic<uint64_t> rays(0), srays(0);
+    std::atomic<uint64_t> rays(0), srays(0), mEval(0), mSample(0), mPdf(0);
     float k = float(sampleIndex + 1);
     auto worker = [&]() {
         PathStats st;
@@ -131,13 +131,17 @@ template <class T> void renderRows(Handle* h, const PTParams& P, uint32_t sample
             }
         }
         rays += st.rays; srays += st.shadowRays;
+        mEval += st.matEval; mSample += st.matSample; mPdf += st.matPdf;
     };
     int nt = std::max(1, nthreads);
     std::vector<std::thread> th;
     for (int i = 1; i < nt; ++i) th.emplace_back(worker);
     worker();
     for (auto& t : th) t.join();
-    if (stats) { stats[0] += rays.load(); stats[1] += srays.load(); }
+    if (stats) {
+        stats[0] += rays.load(); stats[1] += srays.load();
+        stats[2] += mEval.load(); stats[3] += mSample.load(); stats[4] += mPdf.load();
+    }
 }
 template <class T> static void matEval(const Scene<T>& sc, int mat, const float* pt, const float* outDir, const float* inDir, float* value, float* pdf2,
                                        float* comp) {
@@ -227,7 +231,8 @@ int ora_bvh_nodes(void* p) {
 }
 
 // Progressive render of iterations [iterFirst, iterFirst + iterCount) into film (W*H*3, in/out)
-// with the frame buffer's running mean.  stats[0] = traced rays, stats[1] = shadow rays.
+// with the frame buffer's running mean.  stats[0] = traced rays, stats[1] = shadow rays, stats[2..4] =
+// ShadingStats (material evaluations, samples, pdfs).
 int ora_render(void* p, const PTParams* P, float* film, int nthreads, uint64_t* stats, int iterFirst, int iterCount) {
     Handle* H = static_cast<Handle*>(p);
     for (int it = iterFirst; it < iterFirst + iterCount; ++it) {
@@ -358,6 +363,34 @@ int ora_trace_brute64(void* p, const double* rays, int n, double* hits, double* 
                 second[i] = best;
             }
         }
+    };
+    if (H->fp64) run(H->s64); else run(H->s32);
+    return 0;
+}
+
+// FP64 closest hit over the BVH with the runner-up distance, on nthreads host threads.
+// rays: n * 8 doubles (org xyz, tmin, dir xyz, tmax); hits: n * 4 doubles (t, u, v, tri); second: n.
+int ora_trace_two64(void* p, const double* rays, int n, double* hits, double* second, int nthreads) {
+    Handle* H = static_cast<Handle*>(p);
+    std::atomic<int> next{0};
+    auto worker = [&](auto& sc) {
+        for (;;) {
+            int i0 = next.fetch_add(64);
+            if (i0 >= n) return;
+            for (int i = i0; i < std::min(n, i0 + 64); ++i) {
+                const double* r = rays + 8 * size_t(i);
+                HitRec<double> hr; double sec;
+                sc.IntersectTwo64(V3<double>(r[0], r[1], r[2]), V3<double>(r[4], r[5], r[6]), r[3], r[7], hr, sec);
+                hits[4 * size_t(i)] = hr.t; hits[4 * size_t(i) + 1] = hr.u; hits[4 * size_t(i) + 2] = hr.v; hits[4 * size_t(i) + 3] = hr.tri;
+                second[i] = sec;
+            }
+        }
+    };
+    auto run = [&](auto& sc) {
+        std::vector<std::thread> th;
+        for (int t = 1; t < std::max(1, nthreads); ++t) th.emplace_back([&] { worker(sc); });
+        worker(sc);
+        for (auto& t : th) t.join();
     };
     if (H->fp64) run(H->s64); else run(H->s32);
     return 0;

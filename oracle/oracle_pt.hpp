@@ -532,6 +532,42 @@ template <class T> struct Scene {
         return best;
     }
 
+    // FP64 closest hit over the BVH and the distance of the runner-up surface (the nearest hit of
+    // any other triangle), for the intersection parity screening of near-ties.  Ties in t resolve
+    // to the smaller global triangle id, as in Intersect.
+    void IntersectTwo64(V3<double> org, V3<double> dir, double tmin, double tmax, HitRec<double>& best, double& second) const {
+        Ray<double> r; r.org = org; r.dir = dir; r.tmin = tmin; r.tmax = tmax;
+        RayPre<double> pre(dir);
+        V3<double> inv(1.0 / dir.x, 1.0 / dir.y, 1.0 / dir.z);
+        best = HitRec<double>(); best.t = tmax; best.tri = -1;
+        second = tmax;
+        if (nodes.empty()) return;
+        int stack[128]; int sp = 0;
+        stack[sp++] = 0;
+        while (sp) {
+            const BvhNode& n = nodes[stack[--sp]];
+            if (!Scene<double>::BoxHit(n, org, inv, tmin, second)) continue;
+            if (n.count > 0) {
+                for (int i = n.first; i < n.first + n.count; ++i) {
+                    int g = order[i];
+                    V3<double> a(tv0[g].x, tv0[g].y, tv0[g].z), b(tv1[g].x, tv1[g].y, tv1[g].z), c(tv2[g].x, tv2[g].y, tv2[g].z);
+                    double t, u, v;
+                    if (!IntersectTri<double>(r, pre, a, b, c, std::nextafter(second, std::numeric_limits<double>::infinity()), t, u, v)) continue;
+                    if (best.tri < 0 || t < best.t || (t == best.t && g < best.tri)) {
+                        if (best.tri >= 0) second = best.t;
+                        best.t = t; best.u = u; best.v = v; best.tri = g;
+                    } else if (t < second) {
+                        second = t;
+                    }
+                }
+            } else {
+                if (sp + 2 > 128) throw std::runtime_error("bvh stack overflow");
+                stack[sp++] = n.left;
+                stack[sp++] = n.right;
+            }
+        }
+    }
+
     SurfacePoint<T> MakePoint(int g, V2<T> bary, T dist) const { return MakePointMF(triMesh[g], triFace[g], bary, dist); }
     SurfacePoint<T> MakePointMF(int mesh, int f, V2<T> bary, T dist) const {
         const Mesh<T>& m = meshes[mesh];
@@ -848,8 +884,12 @@ struct PTParams {
     int numShadowRays, enableBsdfDI;
 };
 
+// RayTracerStats (rays, shadow rays) and ShadingStats (Shading/ShadingStats.cs:5-33): the material
+// calls counted where the reference's Notify* calls sit (GenericMaterial.cs:71,78,86,93;
+// DiffuseMaterial.cs:110,128,168 -- DiffuseMaterial.Sample also calls EvaluateWithCosine and Pdf).
 struct PathStats {
     uint64_t rays = 0, shadowRays = 0;
+    uint64_t matEval = 0, matSample = 0, matPdf = 0;
 };
 
 // Triangle.SampleUniformArea (Geometry/Triangle.cs:42-55)
@@ -944,6 +984,7 @@ template <class T> Rgb<T> RenderPixel(const Scene<T>& sc, const PTParams& P, uin
                     if (sc.LeavesScene(hit, bs.Direction)) {
                         Rgb<T> bsdfCos = me.EvaluateWithCosine(ctx, bs.Direction);
                         T pdfBsdf, pr; me.Pdf(ctx, bs.Direction, pdfBsdf, pr);
+                        if (stats) { stats->matEval++; stats->matPdf++; }
                         if (!(pdfBsdf == T(0) || bs.Pdf == T(0))) {
                             T mis = P.enableBsdfDI ? T(1) / (T(1) + pdfBsdf / (bs.Pdf * nShadow)) : T(1);
                             Rgb<T> contrib = bs.Weight * bsdfCos / nShadow;
@@ -967,6 +1008,7 @@ template <class T> Rgb<T> RenderPixel(const Scene<T>& sc, const PTParams& P, uin
                         Rgb<T> bsdfCos = me.EvaluateWithCosine(ctx, -l2s);
                         T pdfNE = light.invArea * selProb * nShadow;
                         T pdfBsdfSA, pr; me.Pdf(ctx, -l2s, pdfBsdfSA, pr);
+                        if (stats) { stats->matEval++; stats->matPdf++; }
                         T pdfBsdf = pdfBsdfSA * jac;
                         if (jac != T(0)) {
                             T ratio = pdfBsdf / pdfNE;
@@ -986,6 +1028,10 @@ template <class T> Rgb<T> RenderPixel(const Scene<T>& sc, const PTParams& P, uin
         T uc = T(rng.NextFloat());
         V2<float> up = rng.NextFloat2D();
         BsdfSample<T> bs = me.Sample(ctx, uc, V2<T>(T(up.x), T(up.y)));
+        if (stats) {
+            stats->matSample++;
+            if (mat.type != MAT_GENERIC) { stats->matEval++; stats->matPdf++; }
+        }
         if (bs.Pdf == T(0) || bs.Weight.IsBlack()) break;
         ray = Scene<T>::SpawnRay(hit, bs.Direction);
 

@@ -45,6 +45,7 @@ def lib():
         L.ora_render_pyramid.argtypes = [vp, ctypes.POINTER(PTParams), i, i, vp]
         L.ora_trace.argtypes = [vp, vp, i, vp, i]
         L.ora_trace_brute64.argtypes = [vp, vp, i, vp, vp]
+        L.ora_trace_two64.argtypes = [vp, vp, i, vp, vp, i]
         L.ora_camera_ray.argtypes = [vp, f, f, vp, vp]
         L.ora_material_eval.argtypes = [vp, i, vp, vp, vp, vp, vp, vp]
         L.ora_material_sample.argtypes = [vp, i, vp, vp, f, f, f, vp, vp, vp, vp]
@@ -180,9 +181,10 @@ class OracleScene:
         nthreads = nthreads or os.cpu_count() or 1
         if film is None:
             film = np.zeros((params.height, params.width, 3), np.float32)
-        stats = np.zeros(2, np.uint64)
+        stats = np.zeros(5, np.uint64)
         n = params.totalSpp - iter_first if iter_count is None else iter_count
         self.L.ora_render(self.h, ctypes.byref(params), _p(film), int(nthreads), _p(stats), int(iter_first), int(n))
+        self.last_shading_stats = {"NumMaterialEval": int(stats[2]), "NumMaterialSample": int(stats[3]), "NumMaterialPdf": int(stats[4])}
         return film, int(stats[0]), int(stats[1])
 
     def render_paths(self, params, sample_index, pixels, nthreads=None):
@@ -219,6 +221,17 @@ class OracleScene:
         hits = np.zeros((n, 4), np.float64)
         second = np.zeros(n, np.float64) if with_second else None
         self.L.ora_trace_brute64(self.h, _p(rays), n, _p(hits), _p(second))
+        return hits, second
+
+    def trace_two64(self, rays, nthreads=None):
+        """FP64 closest hit of FP32 rays (n x 8: org, tmin, dir, tmax) over the oracle's BVH, with the
+        distance of the runner-up surface.  Returns hits (n x 4 doubles: t, u, v, global triangle
+        id or -1) and the runner-up distances (tmax when there is none)."""
+        rays = np.ascontiguousarray(np.asarray(rays, np.float32).reshape(-1, 8), np.float64)
+        n = rays.shape[0]
+        hits = np.zeros((n, 4), np.float64)
+        second = np.zeros(n, np.float64)
+        self.L.ora_trace_two64(self.h, _p(rays), n, _p(hits), _p(second), int(nthreads or os.cpu_count() or 1))
         return hits, second
 
     def camera_ray(self, fx, fy):

@@ -61,7 +61,8 @@ class SstPathTracerParams(ctypes.Structure):
 class SstRenderStats(ctypes.Structure):
     _fields_ = [("renderTimeMs", ctypes.c_double), ("frameBufferTimeMs", ctypes.c_double), ("numIterations", ctypes.c_int32),
                 ("numKernelLaunches", ctypes.c_int32), ("numRays", ctypes.c_uint64), ("numShadowRays", ctypes.c_uint64),
-                ("numNanOrInf", ctypes.c_uint64), ("nanPixel", ctypes.c_int32 * 4), ("nanIteration", ctypes.c_int32 * 4)]
+                ("numNanOrInf", ctypes.c_uint64), ("nanPixel", ctypes.c_int32 * 4), ("nanIteration", ctypes.c_int32 * 4),
+                ("numMaterialEval", ctypes.c_uint64), ("numMaterialSample", ctypes.c_uint64), ("numMaterialPdf", ctypes.c_uint64)]
 
 
 class SstGradients(ctypes.Structure):
@@ -136,6 +137,7 @@ SIGNATURES = {
     "sst_set_tuning": [_vp, _P(SstTuning)],
     "sst_autotune": [_vp, _P(SstPathTracerParams), _i32, _P(SstTuning), _P(ctypes.c_double)],
     "sst_set_profiling": [_vp, _i32],
+    "sst_set_shading_stats": [_vp, _i32],
     "sst_get_kernel_times": [_vp, _vp, _vp, _vp, _i32],
     "sst_debug_material_eval": [_vp, _i32, _i32, _vp, _vp, _vp, _vp, _vp],
     "sst_debug_material_sample": [_vp, _i32, _i32, _vp, _vp, _vp, _vp, _vp, _vp],
@@ -222,6 +224,11 @@ KERNEL_CLASSES = ["camera", "trace_closest", "shade", "trace_shadow", "film_fold
 
 def set_profiling(ctx, enable):
     check(ctx.lib.sst_set_profiling(ctx.handle, int(bool(enable))))
+
+
+def set_shading_stats(ctx, enable):
+    """Counts the reference's material calls (ShadingStats) in the context's renders (sst_set_shading_stats)."""
+    check(ctx.lib.sst_set_shading_stats(ctx.handle, int(bool(enable))))
 
 
 def get_tuning(ctx):

@@ -200,7 +200,8 @@ struct sst_ctx {
     DevBuf adjA[3], adjB[3], neeG;
     int cap = 0, shCap = 0, neeSlots = 0;
     size_t sampleCap = 0;
-    DevBuf scratchIn, scratchOut, scratchOut2;
+    // ray queries (sst_trace, sst_occluded): split rays, queue counters, traversal records, results
+    DevBuf qRo, qRd, qCnt, qHits, qOut;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     int* pinnedCount = nullptr;
     // light paths (sst_trace_light_paths)
@@ -215,6 +216,8 @@ struct sst_ctx {
     int waveCapacity = 0;  // 0: the default
     int shadeBlocks = 8;   // resident blocks per SM of the forward shade kernel with GenericMaterials: 8 or 14
     int shadeOrder = 1;    // 1: each bounce's queue is shaded surface hits first (k_partition); 0: in queue order
+    // ShadingStats counting (sst_set_shading_stats)
+    bool shadingStats = false;
     // kernel timing (sst_set_profiling)
     bool profiling = false;
     std::vector<cudaEvent_t> evPool;

@@ -138,6 +138,21 @@ SST_D void outlierNotify(float* w, int* it, int& cnt, int n, float p, int iter) 
 // running mean: for iteration k (1-based) film = film * (k - 1) / k + v / k, non-finite
 // estimates logged and skipped (FrameBuffer.Splat/Normalize, Images/FrameBuffer.cs:166-191, 232).
 // =============================================================================================
+// FrameBuffer.Splat's NaN / Inf log (Images/FrameBuffer.cs:166-179): counts every non-finite estimate
+// and keeps the four smallest (iteration, pixel index) keys, the order in which a sequential render
+// would log them.  An atomicMax cascade over the complemented keys: slot k keeps the largest
+// complement that reaches it and passes the other value on, so slot k ends with the (k+1)-th smallest
+// key of all values logged, whatever the order of the atomics.
+__device__ __forceinline__ void logNan(DevStats* st, int iteration, int pixel) {
+    atomicAdd(&st->nanCount, 1ull);
+    unsigned long long v = ~(((unsigned long long)(unsigned)iteration << 32) | (unsigned)pixel);
+    for (int k = 0; k < 4; ++k) {
+        const unsigned long long old = atomicMax(&st->nanKey[k], v);
+        if (old == 0ull) break;
+        v = old < v ? old : v;
+    }
+}
+
 __global__ void k_film_fold(const DevJob* __restrict__ jobs, const WaveChunk* __restrict__ chunks, const WaveDesc* waves, int* curWave,
                             const float* samples, DevStats* st, int advance) {
     const WaveDesc wd = waves[*curWave];
@@ -186,10 +201,7 @@ __global__ void k_film_fold(const DevJob* __restrict__ jobs, const WaveChunk* __
             if (iter > 0) cur = cur * ((kf - 1.0f) / kf);
             float a = avg3(v);
             bool finite = isfinite(a);
-            if (!finite) {
-                unsigned long long k = atomicAdd(&st->nanCount, 1ull);
-                if (k < 4) { st->nanPixel[k] = (int)pix; st->nanIter[k] = (int)iter + 1; }
-            }
+            if (!finite) logNan(st, (int)iter + 1, (int)pix);
             bool used = finite || !cfg.ignoreNan;
             if (used) cur = cur + v / kf;
             if (finite && nOut > 0) outlierNotify(hw, hit, hcnt, nOut, a, (int)iter);
@@ -457,6 +469,37 @@ SST_D Ctx ctxFromPoint(const float* p, float3 outW) {
     c.out = c.f.toLocal(outW);
     c.uv = make_float2(p[9], p[10]);
     return c;
+}
+
+// TinyEmbree Hit wrapped as SurfacePoint (Geometry/SurfacePoint.cs:7-77) for sst_trace: the compact
+// traversal record (t, u, v, leaf triangle) expanded with the triangle's mesh, face, position, face
+// normal and error offset (Geometry/Mesh.cs:50-60), one thread per ray.
+__global__ void __launch_bounds__(256) k_hit_expand(DevScene sc, const float4* __restrict__ hits, int n, SstHitDev* out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float4 h = hits[i];
+    const int ti = __float_as_int(h.w);
+    SstHitDev r;
+    if (ti < 0) {
+        r.d = 0.f; r.u = 0.f; r.v = 0.f;
+        r.prim = -1; r.mesh = -1; r.eps = 0.f;
+        r.p[0] = r.p[1] = r.p[2] = 0.f;
+        r.n[0] = r.n[1] = r.n[2] = 0.f;
+    } else {
+        const float3 v1 = f3(__ldg(&sc.triv[3 * (size_t)ti])), v2 = f3(__ldg(&sc.triv[3 * (size_t)ti + 1])), v3 = f3(__ldg(&sc.triv[3 * (size_t)ti + 2]));
+        const float4 fn = __ldg(&sc.triN[ti]);
+        const int4 aux = __ldg(&sc.triAux[ti]);
+        const float3 p = baryPos(v1, v2, v3, h.y, h.z);
+        r.d = h.x; r.u = h.y; r.v = h.z;
+        r.prim = aux.z; r.mesh = aux.y;
+        r.eps = errorOffset(v1, v2, v3, h.y, h.z);
+        r.p[0] = p.x; r.p[1] = p.y; r.p[2] = p.z;
+        r.n[0] = fn.x; r.n[1] = fn.y; r.n[2] = fn.z;
+    }
+    out[i] = r;
+}
+void launch_hit_expand(const DevScene& sc, const float4* hits, int n, SstHitDev* out, cudaStream_t s) {
+    if (n > 0) k_hit_expand<<<(n + 255) / 256, 256, 0, s>>>(sc, hits, n, out);
 }
 
 __global__ void k_debug_material_eval(DevScene sc, int mat, int n, const float* pts, const float* outs, const float* ins, float* vals, float* pdfs) {

@@ -53,6 +53,8 @@ void launch_shade(int ns, bool adj, bool generic, int shadeBlocks, const DevJob*
 void launch_shade_pyramid(int ns, const DevJob* jobs, const PathBuf& A, const PathBuf& B, const float4* hits, float4* nee, int cap, float4* shRo,
                           float4* shRd, int* shTgt, uint32_t* shJob, const int* nIn, int* nOut, int* nSh, float* samples, DevStats* stats,
                           const PyrArgs& pyr, int maxItems, cudaStream_t s);
+// sst_trace's hit records: the compact traversal results expanded into SstHit (sst.h) layout.
+void launch_hit_expand(const DevScene& sc, const float4* hits, int n, SstHitDev* out, cudaStream_t s);
 void launch_debug_material_eval(const DevScene& sc, int mat, int n, const float* pts, const float* outs, const float* ins, float* vals, float* pdfs,
                                 cudaStream_t s);
 void launch_debug_material_sample(const DevScene& sc, int mat, int n, const float* pts, const float* outs, const float* us, float* dirs, float* pdfs,

@@ -11,74 +11,60 @@ const DevJob* jobTable(sst_scene* s) {
     return s->queryJob.as<DevJob>();
 }
 
+// Trace / IsOccluded over n rays.  The rays are split into origin and direction arrays and the
+// results written by the device (sst_trace: the SstHit records are expanded on the device from the
+// traversal's (t, u, v, triangle) records); host results come back in one copy.  The buffers are
+// the context's and only grow, so repeated queries of the same size allocate nothing.
 static void runQuery(sst_scene* s, const SstRay* rays, int n, SstHit* hits, int32_t* occl, int memory, bool anyHit) {
+    static_assert(sizeof(SstHit) == sizeof(SstHitDev), "hit layout");
     if (!s || (n > 0 && !rays) || n < 0) fail(SST_ERR_INVALID_ARGUMENT, "invalid query");
+    if (memory != SST_MEM_HOST && memory != SST_MEM_DEVICE) fail(SST_ERR_INVALID_ARGUMENT, "memory must be SST_MEM_HOST or SST_MEM_DEVICE");
     if (!s->committed) fail(SST_ERR_NOT_COMMITTED, "scene is not committed");
     if (n == 0) return;
     sst_ctx* c = s->ctx;
+    CUDA_CHECK(cudaSetDevice(c->device));
     cudaStream_t st = c->stream;
-    const float4* dr = reinterpret_cast<const float4*>(toDevice(c, c->scratchIn, rays, n, memory));
+    const cudaMemcpyKind in = memory == SST_MEM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+    const cudaMemcpyKind out = memory == SST_MEM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
     // separate origin / direction arrays (SstRay = org, tmin, dir, tmax = two float4)
-    DevBuf ro, rd;
-    ro.ensure(size_t(n) * 16);
-    rd.ensure(size_t(n) * 16);
-    CUDA_CHECK(cudaMemcpy2DAsync(ro.p, 16, dr, 32, 16, n, cudaMemcpyDeviceToDevice, st));
-    CUDA_CHECK(cudaMemcpy2DAsync(rd.p, 16, reinterpret_cast<const char*>(dr) + 16, 32, 16, n, cudaMemcpyDeviceToDevice, st));
-    DevBuf cnt, hitsBuf, occBuf;
-    cnt.ensure(sizeof(int) * 2);
-    int hostCnt[2] = {n, 0};
-    CUDA_CHECK(cudaMemcpyAsync(cnt.p, hostCnt, sizeof(hostCnt), cudaMemcpyHostToDevice, st));
+    c->qRo.ensure(size_t(n) * 16);
+    c->qRd.ensure(size_t(n) * 16);
+    CUDA_CHECK(cudaMemcpy2DAsync(c->qRo.p, 16, rays, 32, 16, size_t(n), in, st));
+    CUDA_CHECK(cudaMemcpy2DAsync(c->qRd.p, 16, reinterpret_cast<const char*>(rays) + 16, 32, 16, size_t(n), in, st));
+    c->qCnt.ensure(sizeof(int) * 2);
+    c->pinnedCount[0] = n;
+    c->pinnedCount[1] = 0;
+    CUDA_CHECK(cudaMemcpyAsync(c->qCnt.p, c->pinnedCount, sizeof(int) * 2, cudaMemcpyHostToDevice, st));
     c->stats.ensure(sizeof(DevStats));
     CUDA_CHECK(cudaMemsetAsync(c->stats.p, 0, sizeof(DevStats), st));
+    int* cnt = c->qCnt.as<int>();
     if (anyHit) {
-        occBuf.ensure(size_t(n) * 4);
-        launch_trace_query(c->trace, jobTable(s), ro.as<float4>(), rd.as<float4>(), cnt.as<int>(), cnt.as<int>() + 1, nullptr, occBuf.as<int>(),
-                           c->stats.as<DevStats>(), true, st);
-        CUDA_CHECK(cudaMemcpyAsync(occl, occBuf.p, size_t(n) * 4, memory == SST_MEM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, st));
-        CUDA_CHECK(cudaStreamSynchronize(st));
-        return;
-    }
-    hitsBuf.ensure(size_t(n) * 16);
-    launch_trace_query(c->trace, jobTable(s), ro.as<float4>(), rd.as<float4>(), cnt.as<int>(), cnt.as<int>() + 1, hitsBuf.as<float4>(), nullptr,
-                       c->stats.as<DevStats>(), false, st);
-    std::vector<float4> hh(n);
-    CUDA_CHECK(cudaMemcpyAsync(hh.data(), hitsBuf.p, size_t(n) * 16, cudaMemcpyDeviceToHost, st));
-    CUDA_CHECK(cudaStreamSynchronize(st));
-    // expand into SstHit on the host (the device result is the compact (t, u, v, tri) record)
-    std::vector<float4> tv(3), tn(1);
-    std::vector<int4> aux(1);
-    std::vector<SstHit> outHits(n);
-    for (int i = 0; i < n; ++i) {
-        SstHit& h = outHits[i];
-        std::memset(&h, 0, sizeof(h));
-        int ti;
-        std::memcpy(&ti, &hh[i].w, 4);
-        if (ti < 0) { h.meshId = -1; h.primId = -1; continue; }
-        CUDA_CHECK(cudaMemcpy(tv.data(), s->triv.as<float4>() + 3 * size_t(ti), 48, cudaMemcpyDeviceToHost));
-        CUDA_CHECK(cudaMemcpy(tn.data(), s->triN.as<float4>() + ti, 16, cudaMemcpyDeviceToHost));
-        CUDA_CHECK(cudaMemcpy(aux.data(), s->triAux.as<int4>() + ti, 16, cudaMemcpyDeviceToHost));
-        float u = hh[i].y, v = hh[i].z;
-        h.distance = hh[i].x;
-        h.u = u;
-        h.v = v;
-        h.meshId = aux[0].y;
-        h.primId = aux[0].z;
-        float w = 1.0f - u - v;
-        const float* a = &tv[0].x;
-        const float* b = &tv[1].x;
-        const float* cc = &tv[2].x;
-        float e[3];
-        for (int k = 0; k < 3; ++k) {
-            h.position[k] = u * b[k] + v * cc[k] + w * a[k];
-            e[k] = std::fabs(u * b[k]) + std::fabs(v * cc[k]) + std::fabs(w * a[k]);
+        int* dOcc = occl;
+        if (memory != SST_MEM_DEVICE) {
+            c->qOut.ensure(size_t(n) * 4);
+            dOcc = c->qOut.as<int>();
         }
-        h.errorOffset = std::sqrt(e[0] * e[0] + e[1] * e[1] + e[2] * e[2]) * 32.0f * 1.19209e-07f;
-        h.normal[0] = tn[0].x;
-        h.normal[1] = tn[0].y;
-        h.normal[2] = tn[0].z;
+        launch_trace_query(c->trace, jobTable(s), c->qRo.as<float4>(), c->qRd.as<float4>(), cnt, cnt + 1, nullptr, dOcc, c->stats.as<DevStats>(), true,
+                           st);
+        CUDA_CHECK(cudaGetLastError());
+        if (memory != SST_MEM_DEVICE) CUDA_CHECK(cudaMemcpyAsync(occl, dOcc, size_t(n) * 4, out, st));
+    } else {
+        c->qHits.ensure(size_t(n) * 16);
+        launch_trace_query(c->trace, jobTable(s), c->qRo.as<float4>(), c->qRd.as<float4>(), cnt, cnt + 1, c->qHits.as<float4>(), nullptr,
+                           c->stats.as<DevStats>(), false, st);
+        SstHitDev* dHits = reinterpret_cast<SstHitDev*>(hits);
+        if (memory != SST_MEM_DEVICE) {
+            c->qOut.ensure(size_t(n) * sizeof(SstHitDev));
+            dHits = c->qOut.as<SstHitDev>();
+        }
+        launch_hit_expand(s->dev, c->qHits.as<float4>(), n, dHits, st);
+        CUDA_CHECK(cudaGetLastError());
+        if (memory != SST_MEM_DEVICE) CUDA_CHECK(cudaMemcpyAsync(hits, dHits, size_t(n) * sizeof(SstHitDev), out, st));
     }
-    if (memory == SST_MEM_DEVICE) CUDA_CHECK(cudaMemcpy(hits, outHits.data(), sizeof(SstHit) * n, cudaMemcpyHostToDevice));
-    else std::memcpy(hits, outHits.data(), sizeof(SstHit) * n);
+    DevStats hs;
+    CUDA_CHECK(cudaMemcpyAsync(&hs, c->stats.p, sizeof(DevStats), cudaMemcpyDeviceToHost, st));
+    CUDA_CHECK(cudaStreamSynchronize(st));
+    if (hs.errorFlags & 1) fail(SST_ERR_DEVICE_LIMIT, "BVH traversal stack overflow");
 }
 
 static LightPathBuf bindLight(DevBuf* b, size_t cap) {

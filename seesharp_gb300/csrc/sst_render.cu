@@ -178,7 +178,8 @@ void renderJobs(sst_ctx* c, std::vector<JobIn>& jobs, SstRenderStats* out, bool 
         if (jobs[k].hasCam) hj[k].sc.cam = jobs[k].cam;
         hj[k].lay = jobs[k].lay;
         if (hj[k].lay.aovAlbedo) hj[k].lay.aovSamples = c->aovSamples.as<float>();
-        hj[k].cfg = PTConfig{P->width, P->height, P->maxDepth, P->minDepth, P->baseSeed, P->numShadowRays, P->enableBsdfDI, P->ignoreNanAndInf};
+        hj[k].cfg = PTConfig{P->width, P->height, P->maxDepth, P->minDepth, P->baseSeed, P->numShadowRays, P->enableBsdfDI, P->ignoreNanAndInf,
+                             (c->shadingStats && !replay) ? 1 : 0};
         hj[k].adj = jobs[k].adj;
     }
     std::vector<WaveChunk> chunks;
@@ -347,10 +348,14 @@ void renderJobs(sst_ctx* c, std::vector<JobIn>& jobs, SstRenderStats* out, bool 
         out->numShadowRays += hs.shadowRays;
         uint64_t prev = out->numNanOrInf;
         for (uint64_t k = 0; k < std::min<uint64_t>(hs.nanCount, 4) && prev + k < 4; ++k) {
-            out->nanPixel[prev + k] = hs.nanPixel[k];
-            out->nanIteration[prev + k] = hs.nanIter[k];
+            const unsigned long long key = ~hs.nanKey[k];
+            out->nanPixel[prev + k] = int(uint32_t(key & 0xFFFFFFFFull));
+            out->nanIteration[prev + k] = int(uint32_t(key >> 32));
         }
         out->numNanOrInf += hs.nanCount;
+        out->numMaterialEval += hs.matEvalPdf;
+        out->numMaterialPdf += hs.matEvalPdf;
+        out->numMaterialSample += hs.matSample;
     }
 }
 
@@ -863,6 +868,13 @@ int sst_render_batch(sst_ctx* ctx, const SstRenderJob* jobs, int32_t numJobs, Ss
         for (auto& j : in) it += j.done;
         total.numIterations = it;
         if (stats) *stats = total;
+    });
+}
+
+int sst_set_shading_stats(sst_ctx* ctx, int32_t enable) {
+    return guarded([&] {
+        if (!ctx) fail(SST_ERR_INVALID_ARGUMENT, "NULL context");
+        ctx->shadingStats = enable != 0;
     });
 }
 

@@ -111,6 +111,7 @@ __global__ void __launch_bounds__(128, MINB) k_shade(const DevJob* __restrict__ 
     float3 shC[2 * NS];
     uint32_t pend = 0;
     int queries = 0;
+    int nEvalPdf = 0, nSample = 0;  // ShadingStats (counted only with cfg.shadingStats)
     // adjoint state
     float3 adjLt = mk(0, 0, 0), adjDl = mk(0, 0, 0);
     int vBaseTgt = -1, vRoughTgt = -1;   // targets of this vertex (for the factor left pending)
@@ -175,6 +176,8 @@ __global__ void __launch_bounds__(128, MINB) k_shade(const DevJob* __restrict__ 
                 if (!(pm & (1u << k))) continue;
                 const float4 nv = A.neeIn[(size_t)k * cap + i];
                 radiance = radiance + f3(nv);
+                // a visible next-event sample: the reference evaluates the BSDF and its pdf
+                if (cfg.shadingStats && nv.w != 0.0f) ++nEvalPdf;
                 if (PYR && nv.w != 0.0f) {  // visible: the next-event sample of length `depth` counts
                     const float4 pg = A.pyrGIn[(size_t)k * cap + i];
                     pyrAdd(jobs[job], pyrPixel, (int)(dw & kDepthMask), true, f3(pg), pg.w);
@@ -305,11 +308,14 @@ __global__ void __launch_bounds__(128, MINB) k_shade(const DevJob* __restrict__ 
                                 envSample(sc.env, e1, e2, ed, epdf, ew);
                                 float pb;
                                 float3 bc = evalWithCos<GEN>(sc, m, lp, diffBase, c, ed, pb);
+                                float3 val = mk(0, 0, 0);
+                                bool use = false;
                                 if (!(pb == 0.0f || epdf == 0.0f)) {
                                     float mis = cfg.enableBsdfDI ? 1.0f / (1.0f + pb / (epdf * (float)cfg.numShadowRays)) : 1.0f;
                                     float3 contrib = ew * bc / (float)cfg.numShadowRays;
-                                    float3 val = neeScale * (mis * contrib) / surv;
+                                    val = neeScale * (mis * contrib) / surv;
                                     if (!isBlack(val)) {
+                                        use = true;
                                         int k = 2 * sIt;
                                         if (ADJ) {
                                             // d val / d(material): prefix * mis * weight / ns / surv * |cos| * df
@@ -326,15 +332,21 @@ __global__ void __launch_bounds__(128, MINB) k_shade(const DevJob* __restrict__ 
                                             const float3 pc = contrib * neeScale;
                                             shP[k] = make_float4(pc.x, pc.y, pc.z, mis);
                                         }
-                                        int q = aggAppend(nSh);
-                                        shJob[q] = job;
-                                        float3 o = offsetPoint(s.pos, s.n, s.eps, ed);
-                                        shRo[q] = make_float4(o.x, o.y, o.z, 0.0f);
-                                        shRd[q] = make_float4(ed.x, ed.y, ed.z, CUDART_INF_F);
-                                        shIdx[k] = q;
-                                        shC[k] = val;
-                                        pend |= 1u << k;
                                     }
+                                }
+                                // LeavesScene (PathTracer.cs:428): traced for a contributing sample, and for
+                                // every sample while shading statistics need its visibility (value zero)
+                                if (use || (!ADJ && cfg.shadingStats)) {
+                                    const int k = 2 * sIt;
+                                    if (PYR && !use) shP[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+                                    int q = aggAppend(nSh);
+                                    shJob[q] = job;
+                                    float3 o = offsetPoint(s.pos, s.n, s.eps, ed);
+                                    shRo[q] = make_float4(o.x, o.y, o.z, 0.0f);
+                                    shRd[q] = make_float4(ed.x, ed.y, ed.z, CUDART_INF_F);
+                                    shIdx[k] = q;
+                                    shC[k] = val;
+                                    pend |= 1u << k;
                                 }
                             }
                             if (sc.nEmitters > 0) {
@@ -359,13 +371,16 @@ __global__ void __launch_bounds__(128, MINB) k_shade(const DevJob* __restrict__ 
                                 float lpPdf = em.faceN.w;
                                 float pne = lpPdf * selProb * (float)cfg.numShadowRays;
                                 float pbA = pb * jac;
+                                float3 val = mk(0, 0, 0);
+                                bool use = false;
                                 if (jac != 0.0f) {
                                     float ratio = pbA / pne;
                                     float mis = cfg.enableBsdfDI ? 1.0f / (ratio + 1.0f) : 1.0f;
                                     float pdf = lpPdf / jac * selProb * (float)cfg.numShadowRays;
                                     float3 contrib = emis / pdf * bc;
-                                    float3 val = neeScale * (mis * contrib) / surv;
+                                    val = neeScale * (mis * contrib) / surv;
                                     if (!isBlack(val)) {
+                                        use = true;
                                         int k = 2 * sIt + 1;
                                         if (ADJ) {
                                             float3 coef = adjDl * neeScale * (mis * emis / pdf) / surv * fabsf(c.f.toLocal(-l2s).z);
@@ -382,18 +397,24 @@ __global__ void __launch_bounds__(128, MINB) k_shade(const DevJob* __restrict__ 
                                             const float3 pc = contrib * neeScale;
                                             shP[k] = make_float4(pc.x, pc.y, pc.z, mis);
                                         }
-                                        int q = aggAppend(nSh);
-                                        shJob[q] = job;
-                                        float3 dd = lpPos - s.pos;
-                                        float3 o = offsetPoint(s.pos, s.n, s.eps, dd);
-                                        float3 e = offsetPoint(lpPos, lpN, lpEps, -dd);
-                                        float3 sd = e - o;
-                                        shRo[q] = make_float4(o.x, o.y, o.z, 0.0f);
-                                        shRd[q] = make_float4(sd.x, sd.y, sd.z, 1.0f - 1e-5f);
-                                        shIdx[k] = q;
-                                        shC[k] = val;
-                                        pend |= 1u << k;
                                     }
+                                }
+                                // IsOccluded (PathTracer.cs:467): traced for a contributing sample, and for every
+                                // sample while shading statistics need its visibility (value zero)
+                                if (use || (!ADJ && cfg.shadingStats)) {
+                                    const int k = 2 * sIt + 1;
+                                    if (PYR && !use) shP[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+                                    int q = aggAppend(nSh);
+                                    shJob[q] = job;
+                                    float3 dd = lpPos - s.pos;
+                                    float3 o = offsetPoint(s.pos, s.n, s.eps, dd);
+                                    float3 e = offsetPoint(lpPos, lpN, lpEps, -dd);
+                                    float3 sd = e - o;
+                                    shRo[q] = make_float4(o.x, o.y, o.z, 0.0f);
+                                    shRd[q] = make_float4(sd.x, sd.y, sd.z, 1.0f - 1e-5f);
+                                    shIdx[k] = q;
+                                    shC[k] = val;
+                                    pend |= 1u << k;
                                 }
                             }
                         }
@@ -403,6 +424,11 @@ __global__ void __launch_bounds__(128, MINB) k_shade(const DevJob* __restrict__ 
                     float u1 = rng.nextFloat(), u2 = rng.nextFloat();
                     float3 dirW; float bpdf = 0.f; float3 bw = mk(0, 0, 0);
                     bool ok = sampleMaterial<GEN>(sc, m, lp, diffBase, c, uc, u1, u2, dirW, bpdf, bw);
+                    if (!ADJ && cfg.shadingStats) {
+                        // Material.Sample; DiffuseMaterial.Sample also evaluates and computes the pdf
+                        ++nSample;
+                        if (!(GEN && m.type == kGeneric)) ++nEvalPdf;
+                    }
                     if (!ok || bpdf == 0.0f || isBlack(bw)) {
                         // a finished path with queued NEE keeps its next length for the pyramid
                         if (pend) { cont = true; outDepth = kDoneFlag | (PYR ? depth + 1 : 0u); }
@@ -435,6 +461,11 @@ __global__ void __launch_bounds__(128, MINB) k_shade(const DevJob* __restrict__ 
     // shadow-query statistics (RayTracerStats.NumShadowRays semantics)
     int totq = __reduce_add_sync(0xffffffffu, queries);
     if ((threadIdx.x & 31) == 0 && totq) atomicAdd(&stats->shadowRays, (unsigned long long)totq);
+    if (!ADJ) {
+        const int te = __reduce_add_sync(0xffffffffu, nEvalPdf), ts = __reduce_add_sync(0xffffffffu, nSample);
+        if ((threadIdx.x & 31) == 0 && te) atomicAdd(&stats->matEvalPdf, (unsigned long long)te);
+        if ((threadIdx.x & 31) == 0 && ts) atomicAdd(&stats->matSample, (unsigned long long)ts);
+    }
 
     // K7: warp ballot / popc compaction into the next queue
     unsigned m = __ballot_sync(0xffffffffu, cont);

@@ -93,6 +93,7 @@ struct PTConfig {
     int numShadowRays;
     int enableBsdfDI;
     int ignoreNan;
+    int shadingStats;  // count material calls (every next-event shadow ray is traced)
 };
 
 // Path-replay adjoint buffers of a job (all NULL for a plain render).
@@ -121,6 +122,13 @@ struct LightPathBuf {  // structure of arrays of the light paths in flight
     float4* prevN;     // previous vertex face normal
     float4* ro;        // ray origin, w = tmin
     float4* rd;        // ray direction, w = tmax
+};
+struct SstHitDev {  // the layout of SstHit
+    float d, u, v;
+    int prim, mesh;
+    float eps;
+    float p[3];
+    float n[3];
 };
 struct SstPathVertexDev {  // the layout of SstPathVertex
     float p[16];
@@ -196,8 +204,11 @@ struct DevStats {
     unsigned long long rays;
     unsigned long long shadowRays;
     unsigned long long nanCount;
-    int nanPixel[4];
-    int nanIter[4];
+    // the four smallest keys (1-based iteration << 32 | pixel index) of the non-finite estimates,
+    // stored complemented (~key) in descending order, 0 for an unused entry (see logNan)
+    unsigned long long nanKey[4];
+    unsigned long long matEvalPdf;  // ShadingStats: material evaluations (each comes with a pdf here)
+    unsigned long long matSample;   // ShadingStats: material samples
     int errorFlags;  // bit 0: traversal stack overflow
     int pad[3];
 };

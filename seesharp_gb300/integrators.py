@@ -46,6 +46,11 @@ class PathTracer(Integrator):
         # with Open Image Denoise by default; the layers are computed on the GPU, the denoiser is
         # outside this library.
         self.EnableDenoiser = True
+        # ShadingStats (Shading/ShadingStats.cs): the reference counts every material call in every
+        # render.  Here counting is a switch (it traces the shadow rays of next-event samples that
+        # contribute nothing, whose visibility decides the reference's counts); with it on, Render
+        # writes FrameBuffer.MetaData["ShadingStats"] as PathTracer.cs:256 does.
+        self.CountShadingStats = False
         for k, v in kw.items():
             if not hasattr(self, k):
                 raise AttributeError(k)
@@ -96,6 +101,17 @@ class PathTracer(Integrator):
             fb.OutlierCache = OutlierReplayCache(fb.Width, fb.Height, fb.NumOutliersToTrack)
         oc = fb.OutlierCache
         outliers = (oc.weight, oc.iteration) if oc.nMax > 0 else None
+        if self.CountShadingStats:
+            _native.set_shading_stats(scene.native.ctx, True)
+        try:
+            stats = self._render(scene, p, film, var, albedo, normal, outliers, pyramid)
+        finally:
+            if self.CountShadingStats:
+                _native.set_shading_stats(scene.native.ctx, False)
+        self._finish(scene, stats, pyramid)
+
+    def _render(self, scene, p, film, var, albedo, normal, outliers, pyramid):
+        fb = scene.FrameBuffer
         if var is not None or fb.ReferenceImage is not None or albedo is not None or outliers is not None or pyramid is not None:
             ref = None if fb.ReferenceImage is None else fb.ReferenceImage.data
             stats, vimg, avg, err = scene.native.render_layers(p, film.ctypes.data, variance_state=None if var is None else var.state,
@@ -110,11 +126,18 @@ class PathTracer(Integrator):
                               for k in range(n)]
         else:
             stats = scene.native.render(p, film.ctypes.data)
+        return stats
+
+    def _finish(self, scene, stats, pyramid):
+        fb = scene.FrameBuffer
         fb.CurIteration = fb.CurIteration + stats.numIterations
         fb.MetaData["NumIterations"] = fb.CurIteration
         fb.MetaData["RenderTime"] = stats.renderTimeMs
         fb.MetaData["FrameBufferTime"] = stats.frameBufferTimeMs
         fb.MetaData["RayTracerStats"] = {"NumRays": int(stats.numRays), "NumShadowRays": int(stats.numShadowRays)}
+        if self.CountShadingStats:
+            fb.MetaData["ShadingStats"] = {"NumMaterialEval": int(stats.numMaterialEval), "NumMaterialSample": int(stats.numMaterialSample),
+                                           "NumMaterialPdf": int(stats.numMaterialPdf)}
         for k in range(min(4, int(stats.numNanOrInf))):
             px = stats.nanPixel[k]
             if px >= 0:

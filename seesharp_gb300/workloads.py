@@ -402,10 +402,38 @@ def validate_single_bounce(width=512, height=512):
     return sc, 10, 3
 
 
-def validate_environment(width=512, height=512, seed=5):
-    """Environment lighting (Validate_Environment.cs loads Data/Scenes/simplebackground.json with
-    Data/Scenes/sunsky.exr; the EXR cannot be decoded here, so a seeded procedural sky of the same
-    lat-long layout stands in).  10 spp, max depth 5."""
+def validate_single_bounce_glossy(width=512, height=512):
+    """Validate_SingleBounceGlossy.cs (32 spp, max depth 3): a rough (0.5) transmissive plane in
+    front of a rough reflector, lit by a 0.1-area quad of power 500 facing -z."""
+    sc = Scene()
+    a = Mesh([[-1, -1, 0], [1, -1, 0], [1, 1, 0], [-1, 1, 0]], [0, 1, 2, 0, 2, 3])
+    a.Material = GenericMaterial(GenericMaterial.Parameters(BaseColor=TextureRgb(RgbColor.White), Roughness=TextureMono(0.5),
+                                                           SpecularTransmittance=1.0))
+    b = Mesh([[-1, -1, 1], [1, -1, 1], [1, 1, 1], [-1, 1, 1]], [0, 1, 2, 0, 2, 3])
+    b.Material = GenericMaterial(GenericMaterial.Parameters(BaseColor=TextureRgb(RgbColor.White), Roughness=TextureMono(0.5)))
+    area = np.float32(0.1)
+    pos = float(np.sqrt(area) / np.float32(2))
+    l = Mesh([[-pos, -pos, 11], [pos, -pos, 11], [pos, pos, 11], [-pos, pos, 11]], [0, 1, 2, 0, 2, 3], shadingNormals=[[0, 0, -1]] * 4)
+    l.Material = _black()
+    sc.Meshes += [a, b, l]
+    radiance = float(np.float32(500) / (np.float32(math.pi) * area))
+    sc.Emitters.extend(DiffuseEmitter.MakeFromMesh(l, RgbColor.White * radiance))
+    sc.Camera = PerspectiveCamera(Matrix4x4.CreateLookAt([0, 0, -1], [0, 0, 0], [0, 1, 0]), 45)
+    sc.FrameBuffer = FrameBuffer(width, height)
+    return sc, 32, 3
+
+
+def validate_cornell_box(width=512, height=512, data_dir=None):
+    """Validate_CornellBox.cs: Data/Scenes/CornellBox/CornellBox.json, 512 x 512, 8 spp, max depth 5."""
+    from . import sceneio
+    sc = sceneio.load_json_scene(_scene_file(data_dir, "CornellBox/CornellBox.json"))
+    sc.FrameBuffer = FrameBuffer(width, height)
+    return sc, 8, 5
+
+
+def env_lit_box(width=512, height=512, seed=5):
+    """A diffuse ground and a GenericMaterial box lit only by a seeded procedural sky (lat-long
+    environment map, 128 x 64): an environment-lighting workload for the tests."""
     sc = Scene()
     g = Mesh([[-10, -1, -10], [10, -1, -10], [10, -1, 10], [-10, -1, 10]], [0, 2, 1, 0, 3, 2])
     g.Material = DiffuseMaterial(DiffuseMaterial.Parameters(BaseColor=TextureRgb(RgbColor(0.8, 0.8, 0.8))))
@@ -416,45 +444,46 @@ def validate_environment(width=512, height=512, seed=5):
     sc.Background = EnvironmentMap(RgbImage(procedural_sky(128, 64, seed=seed)))
     sc.Camera = PerspectiveCamera(Matrix4x4.CreateLookAt([0, 1, 4], [0, -0.3, 0], [0, 1, 0]), 45)
     sc.FrameBuffer = FrameBuffer(width, height)
-    return sc, 10, 5
+    return sc
 
 
-def validate_textures(width=512, height=512, seed=9):
-    """Textured materials (Validate_Textures.cs renders Data/Scenes/TextureTest; its PNG/OBJ
-    inputs cannot be decoded here, so a seeded checker texture on a quad stands in)."""
-    rng = np.random.default_rng(seed)
-    sc = Scene()
-    tex = np.zeros((64, 64, 3), np.float32)
-    ii, jj = np.meshgrid(np.arange(64), np.arange(64), indexing="ij")
-    chk = ((ii // 8 + jj // 8) % 2).astype(np.float32)
-    tex[..., 0] = 0.2 + 0.7 * chk
-    tex[..., 1] = 0.2 + 0.5 * (1 - chk)
-    tex[..., 2] = rng.uniform(0.1, 0.9, size=(64, 64)).astype(np.float32)
-    rough = MonochromeImage_from(rng.uniform(0.1, 0.9, size=(16, 16)).astype(np.float32))
-    q = Mesh([[-2, -2, -3], [2, -2, -3], [2, 2, -3], [-2, 2, -3]], [0, 1, 2, 0, 2, 3], textureCoordinates=[[0, 0], [1, 0], [1, 1], [0, 1]])
-    q.Material = GenericMaterial(GenericMaterial.Parameters(BaseColor=TextureRgb(RgbImage(tex)), Roughness=TextureMono(rough)))
-    f = Mesh([[-5, -2, 0], [5, -2, 0], [5, -2, -8], [-5, -2, -8]], [0, 1, 2, 0, 2, 3], textureCoordinates=[[0, 0], [3, 0], [3, 3], [0, 3]])
-    f.Material = DiffuseMaterial(DiffuseMaterial.Parameters(BaseColor=TextureRgb(RgbImage(tex[::-1].copy()))))
-    e = _small_emitter(-1.5, -1, (0.0, 1.5), 0.3)
-    e.Material = _black()
-    sc.Meshes += [q, f, e]
-    sc.Emitters.extend(DiffuseEmitter.MakeFromMesh(e, RgbColor(40, 40, 40)))
-    sc.Camera = PerspectiveCamera(Matrix4x4.CreateLookAt([0, 0, 1], [0, 0, -3], [0, 1, 0]), 50)
+def _scene_file(data_dir, rel):
+    import os
+    if data_dir is None:
+        raise ValueError(f"this Validation scene loads {rel}: pass data_dir, the directory that holds SeeSharp's Data/Scenes files")
+    return os.path.join(data_dir, rel)
+
+
+def validate_environment(width=512, height=512, data_dir=None):
+    """Validate_Environment.cs: Data/Scenes/simplebackground.json (lit by Data/Scenes/sunsky.exr),
+    512 x 512, 10 spp, max depth 5.  data_dir: the directory holding the reference's Data/Scenes files."""
+    from . import sceneio
+    sc = sceneio.load_json_scene(_scene_file(data_dir, "simplebackground.json"))
     sc.FrameBuffer = FrameBuffer(width, height)
     return sc, 10, 5
 
 
-def MonochromeImage_from(arr):
-    from .images import MonochromeImage
-    return MonochromeImage(arr)
+def validate_textures(width=700, height=500, data_dir=None):
+    """Validate_Textures.cs: Data/Scenes/TextureTest/TextureTest.json (an OBJ mesh with a PNG
+    texture), 700 x 500, 8 spp, max depth 5."""
+    from . import sceneio
+    sc = sceneio.load_json_scene(_scene_file(data_dir, "TextureTest/TextureTest.json"))
+    sc.FrameBuffer = FrameBuffer(width, height)
+    return sc, 8, 5
 
 
+# SeeSharp.Validation's factories (Validate_*.cs) by name.  Each takes (width, height) and returns
+# (scene, SamplesPerPixel, MaxDepth); the ones that load the reference's scene files also take
+# data_dir, the directory that holds SeeSharp's Data/Scenes files.
 VALIDATION_SCENES = {
     "DirectIllumination": validate_direct_illum,
     "DirectIllumTransmit": validate_direct_transmit,
     "MultiLight": validate_multi_light,
     "GlossyLight": validate_glossy_light,
     "SingleBounce": validate_single_bounce,
+    "SingleBounceGlossy": validate_single_bounce_glossy,
     "Environment": validate_environment,
-    "Textures": validate_textures,
+    "TextureTest": validate_textures,
+    "CornellBox": validate_cornell_box,
 }
+SCENE_FILE_VALIDATIONS = ("Environment", "TextureTest", "CornellBox")

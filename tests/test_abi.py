@@ -40,7 +40,7 @@ def test_struct_layouts_match_header():
     assert ctypes.sizeof(_native.SstHit) == 48
     assert ctypes.sizeof(_native.SstGenericMaterial) == 44
     assert ctypes.sizeof(_native.SstPathTracerParams) == 48
-    assert ctypes.sizeof(_native.SstRenderStats) == 80
+    assert ctypes.sizeof(_native.SstRenderStats) == 104
 
 
 def test_tuning_struct_matches_header():

@@ -7,6 +7,7 @@ functions, the oracle strict IEEE single precision; images by the reference's Va
 """
 import ctypes
 import math
+import os
 
 import numpy as np
 import pytest
@@ -17,6 +18,8 @@ from seesharp_gb300 import (DiffuseMaterial, FrameBuffer, GenericMaterial, Matri
 from seesharp_gb300 import _native
 
 pytestmark = pytest.mark.gpu
+
+SCENES = os.path.join(os.path.dirname(__file__), "golden", "scenes")
 
 
 def close(a, b, rtol=1e-4, atol=1e-6):
@@ -336,8 +339,10 @@ def test_cornell_box_image_mean():
 
 @pytest.mark.parametrize("name", list(workloads.VALIDATION_SCENES))
 def test_validation_scenes(name):
-    """SeeSharp.Validation scenes at reduced resolution: image means within 1%."""
-    sc, spp, depth = workloads.VALIDATION_SCENES[name](96, 96)
+    """SeeSharp.Validation scenes at reduced resolution: image means within 1%.  The factories that
+    load the reference's scene files read them from tests/golden/scenes."""
+    kw = {"data_dir": SCENES} if name in workloads.SCENE_FILE_VALIDATIONS else {}
+    sc, spp, depth = workloads.VALIDATION_SCENES[name](96, 96, **kw)
     sc.Prepare()
     g, _ = render_gpu(sc, spp, depth)
     r, _, _ = render_oracle(sc, spp, depth)
@@ -451,7 +456,7 @@ def _batch_scenes():
     out = []
     specs = [(workloads.cornell_box, (40, 30), 3, 5), (workloads.cornell_box, (17, 64), 5, 3),
              (lambda w, h: workloads.sphere_field(6, w, h, level=3), (48, 48), 4, 8),
-             (lambda w, h: workloads.validate_environment(w, h)[0], (33, 21), 2, 5),
+             (lambda w, h: workloads.env_lit_box(w, h), (33, 21), 2, 5),
              (lambda w, h: workloads.validate_glossy_light(w, h)[0], (50, 50), 6, 2)]
     for fn, (w, h), spp, depth in specs:
         sc = fn(w, h)

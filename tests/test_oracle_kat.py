@@ -399,3 +399,35 @@ def test_rng_nextint_lemire():
     vals, _ = O.rng_ints(0x1234567, 50, 1000)
     assert vals.max() < 50
     assert len(set(vals.tolist())) == 50
+
+
+# ---------------------------------------------------------------------------------------------
+# The FP64 BVH query that referees the GPU's intersection parity on the benchmark scenes
+# (tests/test_gpu_intersection.py) equals FP64 brute force: same closest triangle and distance, and
+# the runner-up distance equals the nearest hit among all other triangles.
+def test_oracle_bvh_two_hit_query_equals_brute_force():
+    rng = np.random.default_rng(4)
+    n = 400
+    c = rng.uniform(-5, 5, size=(n, 1, 3))
+    v = (c + rng.normal(scale=0.6, size=(n, 3, 3))).astype(np.float32)
+    sc = Scene()
+    m = Mesh(v.reshape(-1, 3), np.arange(3 * n, dtype=np.int32))
+    m.Material = DiffuseMaterial()
+    sc.Meshes.append(m)
+    sc.Emitters.extend(DiffuseEmitter.MakeFromMesh(m, RgbColor.White))
+    sc.Camera = PerspectiveCamera(Matrix4x4.CreateLookAt([0, 0, 12], [0, 0, 0], [0, 1, 0]), 40)
+    sc.FrameBuffer = FrameBuffer(8, 8)
+    o = O.OracleScene.from_scene(sc, fp64=True)
+    k = 1500
+    org = rng.uniform(-8, 8, size=(k, 3))
+    d = rng.uniform(-4, 4, size=(k, 3)) - org
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    rays = np.zeros((k, 8), np.float32)
+    rays[:, 0:3], rays[:, 4:7], rays[:, 7] = org, d, np.inf
+    hits, second = o.trace_two64(rays)
+    ref, ref2 = o.trace_brute64(rays[:, 0:3].astype(np.float64), rays[:, 4:7].astype(np.float64), with_second=True)
+    assert np.array_equal(hits[:, 3], ref[:, 3])
+    hit = ref[:, 3] >= 0
+    assert hit.sum() > k // 4
+    assert np.array_equal(hits[hit, 0], ref[hit, 0])
+    assert np.array_equal(second[hit], ref2[hit])

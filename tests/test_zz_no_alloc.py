@@ -80,3 +80,28 @@ def test_noalloc_rejects_more_rays_than_its_scratch_holds(scene):
     # the next call in range still works
     ok = scene.native.occluded_noalloc(rays[:100])
     assert np.array_equal(ok, scene.native.occluded(rays[:100]))
+
+
+def test_noalloc_allocates_no_device_memory(scene):
+    """The property the entry point exists for: after its first call on the device (which looks up
+    the scratch array's address), repeated calls leave the device's free memory unchanged.  The
+    same measurement sees the growth of sst_occluded's context buffers for a larger query, so it
+    would see an allocation."""
+    torch = pytest.importorskip("torch")
+    L, h = scene.native.lib, scene.native.handle
+    n = _native.SST_NOALLOC_MAX_RAYS
+    rays = _rays(n, seed=21)
+    out = np.zeros(n, np.int32)
+    _native.check(L.sst_occluded_noalloc(h, _p(rays), n, _p(out), _native.SST_MEM_HOST))
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    for k in range(20):
+        _native.check(L.sst_occluded_noalloc(h, _p(rays), n, _p(out), _native.SST_MEM_HOST))
+    free1, _ = torch.cuda.mem_get_info()
+    assert free1 == free0
+    # a query larger than any before grows the context buffers of sst_occluded by about 68 MB
+    big = np.tile(rays, (64, 1))
+    flags = np.zeros(big.shape[0], np.int32)
+    _native.check(L.sst_occluded(h, _p(big), big.shape[0], _p(flags), _native.SST_MEM_HOST))
+    free2, _ = torch.cuda.mem_get_info()
+    assert free2 < free1 - 32 * 2**20
