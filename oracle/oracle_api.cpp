@@ -481,6 +481,7 @@ int ora_adjoint(void* p, const PTParams* P, const float* dLdI, double* gTex, dou
             for (int col = 0; col < P->width; ++col) {
                 uint32_t pix = uint32_t(row * P->width + col);
                 const float* d = dLdI + 3 * size_t(pix);
+                if (d[0] == 0.0f && d[1] == 0.0f && d[2] == 0.0f) continue;  // every term is a multiple of dLoss/dPixel
                 Rgb<double> delta(double(d[0]) / P->totalSpp, double(d[1]) / P->totalSpp, double(d[2]) / P->totalSpp);
                 for (int s = 0; s < P->totalSpp; ++s) {
                     Rng rng(P->baseSeed, pix, uint32_t(s));

@@ -160,6 +160,9 @@ void renderJobs(sst_ctx* c, std::vector<JobIn>& jobs, SstRenderStats* out, bool 
     bool generic = false;
     for (auto& j : jobs)
         for (auto& m : j.s->materials) generic |= m.type == kGeneric;
+    // SST_SHADE_GENERIC=1 runs the generic build for every wave (the build a mixed batch uses)
+    const char* sg = getenv("SST_SHADE_GENERIC");
+    if (sg && std::string(sg) == "1") generic = true;
     // per-item samples of the denoiser feature layers (written by the first shade, read by the fold)
     bool anyAov = false, pyramid = false;
     for (auto& j : jobs) {

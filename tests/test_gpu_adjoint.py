@@ -64,6 +64,62 @@ def test_adjoint_matches_fp64_replay():
     assert np.linalg.norm(g["texture"]) > 0 and np.all(g["roughness"] != 0) and np.all(g["radiance"] != 0)
 
 
+def test_adjoint_matches_fp64_replay_at_the_differentiation_size():
+    """The differentiation configuration itself (512 x 512, 32 spp, depth 5, 256 x 256 texture)
+    against the FP64 replay, on every 64th pixel: dLoss/dImage is the L2 loss gradient there and
+    zero elsewhere, so the replay covers 4096 pixels x 32 paths."""
+    sc, dr, tex0, image, target = setup(512, 512, 32, 256)
+    loss, dldi = l2_loss(image, target)
+    mask = np.zeros(512 * 512, bool)
+    mask[::64] = True
+    dldi = np.where(mask.reshape(512, 512, 1), dldi, 0).astype(np.float32)
+    g = dr.backward(dldi)["raw"]
+    o = O.OracleScene.from_scene(sc, fp64=True)
+    ref = o.adjoint(o.params(512, 512, 32, 5, baseSeed=dr.params.baseSeed), dldi, dr.n_tex, dr.n_mat, dr.n_em)
+    for key in ("textures", "materialBaseColor", "materialRoughness", "emitterRadiance"):
+        assert np.all(np.isfinite(g[key])), key
+        if np.linalg.norm(ref[key]) > 0:
+            assert rel_l2(g[key], ref[key]) <= 0.02, (key, rel_l2(g[key], ref[key]))
+    assert np.count_nonzero(ref["textures"]) > 1000
+
+
+def test_adjoint_large_combined_shape_matches_fp64_replay():
+    """The large combined job's gradient shape at a reduced size: a 1024 x 1024 x 3 base-colour
+    texture on the terrain and the roughness of every icosphere (60 here, 2000 in the full job),
+    depth 10, against the FP64 replay of the same paths.  The texture gradient is compared in 4 x 4
+    texel blocks: a hit's texel is floor(uv * 1024), and the FP32 and FP64 interpolations of uv
+    differ by about 1e-7, which puts about 2e-4 of the lookups on the other side of a texel edge;
+    those paths credit the neighbouring texel, which a block sum absorbs."""
+    sc, tex, mats, cams = workloads.large_combined(96, 54, num_spheres=60, terrain_quads=64, tex_res=1024, num_lights=40, views=1)
+    sc.Prepare()
+    pt = PathTracer(TotalSpp=4, MaxDepth=10)
+    dr = DifferentiableRender(sc, pt, texture=tex, roughness_materials=mats)
+    rng = np.random.default_rng(8)
+    tex0 = tex.Image.data.copy()
+    r0 = np.array([m.MaterialParameters.Roughness.constColor for m in mats], np.float64)
+    dr.params.baseSeed = 0x5EED
+    target = dr.forward(np.clip(tex0 * (1 + 0.3 * rng.standard_normal(tex0.shape)), 0.02, 0.98).astype(np.float32),
+                        np.clip(r0 + 0.2 * rng.standard_normal(r0.shape), 0.05, 1.0), None)
+    dr.params.baseSeed = pt.BaseSeed
+    image = dr.forward(tex0, r0, None)
+    loss, dldi = l2_loss(image, target)
+    g = dr.backward(dldi)
+    o = O.OracleScene.from_scene(sc, fp64=True)
+    ref = o.adjoint(o.params(96, 54, 4, 10, baseSeed=dr.params.baseSeed), dldi, dr.n_tex, dr.n_mat, dr.n_em)
+    raw = g["raw"]
+
+    def blocks(t):
+        t = np.asarray(t, np.float64)[dr.tex_offset:dr.tex_offset + 1024 * 1024 * 3].reshape(256, 4, 256, 4, 3)
+        return t.sum(axis=(1, 3))
+
+    for key in ("textures", "materialRoughness"):
+        assert np.all(np.isfinite(raw[key])), key
+        assert np.linalg.norm(ref[key]) > 0, key
+    assert rel_l2(blocks(raw["textures"]), blocks(ref["textures"])) <= 0.02, rel_l2(blocks(raw["textures"]), blocks(ref["textures"]))
+    assert rel_l2(raw["materialRoughness"], ref["materialRoughness"]) <= 0.02, rel_l2(raw["materialRoughness"], ref["materialRoughness"])
+    assert np.count_nonzero(g["roughness"]) >= 30 and g["texture"].shape == (1024, 1024, 3)
+
+
 def _fd(dr, loss_of, theta, h):
     return (loss_of(theta + h) - loss_of(theta - h)) / (2 * h)
 

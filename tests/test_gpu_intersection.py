@@ -142,25 +142,38 @@ def _check_closest(sc, o, rays, offsets, label):
     return checked
 
 
-def _check_occluded(sc, o, rays, label):
-    occ = sc.native.occluded(rays)
+def _occlusion_reference(o, rays, tris):
+    """FP64 occlusion of each segment and whether the answer is robust to FP32 rounding: the first
+    surface along the segment's line is farther from the segment's end than the FP32 resolution of
+    its t (16 ulps of the segment's coordinates over the segment's length, divided by the cosine
+    between the segment and the surface normal, since a grazing hit's t moves with every ulp of the
+    other coordinates; at least a relative 1e-6), and an occluder in front of the end is at least
+    1e-4 (in barycentric terms) inside its triangle."""
     full = rays.copy()
     full[:, 7] = np.inf
-    ref, second = o.trace_two64(full)
-    checked = 0
-    for i in range(rays.shape[0]):
-        rt, ru, rv, rg = ref[i]
-        tmax = float(rays[i, 7])
-        if rg >= 0:
-            w = 1 - ru - rv
-            if abs(rt - tmax) <= 1e-4 * tmax or min(ru, rv, w) < 1e-4 or (second[i] - rt) < 1e-4 * rt:
-                continue
-            want = rt < tmax
-        else:
-            want = False
-        assert bool(occ[i]) == want, (label, i, occ[i], rt, tmax)
-        checked += 1
-    return checked
+    ref, _ = o.trace_two64(full)
+    org, d = rays[:, 0:3].astype(np.float64), rays[:, 4:7].astype(np.float64)
+    tmax = rays[:, 7].astype(np.float64)
+    span = np.maximum(np.maximum(np.abs(org).max(axis=1), np.abs(org + d).max(axis=1)), 1.0)
+    dl = np.linalg.norm(d, axis=1)
+    tri = tris[np.maximum(ref[:, 3], 0).astype(np.int64)]
+    nrm = np.cross(tri[:, 1] - tri[:, 0], tri[:, 2] - tri[:, 0])
+    cos = np.abs(np.sum(nrm * d, axis=1)) / np.maximum(np.linalg.norm(nrm, axis=1) * dl, 1e-300)
+    res = np.maximum(16 * 1.2e-7 * span / dl / np.maximum(cos, 1e-9), 1e-6 * tmax)
+    hit = ref[:, 3] >= 0
+    rt, ru, rv = ref[:, 0], ref[:, 1], ref[:, 2]
+    want = hit & (rt < tmax)
+    decisive = ~hit | (np.abs(rt - tmax) > res)
+    decisive &= ~(want & (np.minimum(np.minimum(ru, rv), 1 - ru - rv) < 1e-4))
+    return want, decisive
+
+
+def _check_occluded(sc, o, rays, label):
+    occ = sc.native.occluded(rays) != 0
+    want, decisive = _occlusion_reference(o, rays, _tri_table(sc))
+    bad = np.nonzero(decisive & (occ != want))[0]
+    assert bad.size == 0, (label, bad[:8], occ[bad[:8]], want[bad[:8]])
+    return int(decisive.sum())
 
 
 def _run(sc, seed, min_frac=0.5):

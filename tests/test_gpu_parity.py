@@ -469,14 +469,22 @@ def _batch_scenes():
 def test_batch_equals_individual_renders(capacity):
     """One shared wavefront over jobs of different sizes, spp and depths gives every job the film
     its own render gives (bitwise: per-path arithmetic and per-pixel fold order do not depend on
-    how waves are packed)."""
+    how waves are packed).  A wave with any GenericMaterial shades every path with the shade build
+    that has the generic code compiled in, so the single renders run that build too
+    (SST_SHADE_GENERIC=1): a diffuse-only render otherwise runs the lean build, whose arithmetic is
+    the same source compiled separately, and nvcc may contract it into fused multiply-adds
+    differently (test_shade_builds_agree_on_diffuse_scenes bounds that difference)."""
     import os
     pairs = _batch_scenes()
     singles = []
-    for sc, pt in pairs:
-        sc.FrameBuffer.Reset()
-        pt.Render(sc)
-        singles.append(sc.FrameBuffer.Image.data.copy())
+    os.environ["SST_SHADE_GENERIC"] = "1"
+    try:
+        for sc, pt in pairs:
+            sc.FrameBuffer.Reset()
+            pt.Render(sc)
+            singles.append(sc.FrameBuffer.Image.data.copy())
+    finally:
+        os.environ.pop("SST_SHADE_GENERIC", None)
     if capacity:
         os.environ["SST_WAVE_CAPACITY"] = capacity
     try:
@@ -488,6 +496,23 @@ def test_batch_equals_individual_renders(capacity):
         os.environ.pop("SST_WAVE_CAPACITY", None)
     for (sc, _), ref in zip(pairs, singles):
         assert np.array_equal(sc.FrameBuffer.Image.data, ref)
+
+
+def test_shade_builds_agree_on_diffuse_scenes():
+    """The lean shade build (no GenericMaterial code, used for waves without GenericMaterials) and
+    the generic build compile the same diffuse arithmetic separately; nvcc's fused multiply-add
+    contraction may differ between them by an ulp.  At 1 spp every pixel is one path: the two films
+    agree per path to a relative 1e-5, except where an ulp flips a discrete decision."""
+    import os
+    sc = workloads.cornell_box(128, 128)
+    sc.Prepare()
+    lean, _ = render_gpu(sc, 1, 5)
+    os.environ["SST_SHADE_GENERIC"] = "1"
+    try:
+        gen, _ = render_gpu(sc, 1, 5)
+    finally:
+        os.environ.pop("SST_SHADE_GENERIC", None)
+    assert per_path_agreement(gen, lean, 1e-5, 1e-7) >= 0.995
 
 
 def test_graph_replay_equals_plain_launches():
