@@ -184,8 +184,9 @@ typedef struct SstTuning {
     int32_t traceBlock;       /* threads per traversal block: 64, 128 (the default) or 256 */
     int32_t traceStackShared; /* traversal stack entries per thread kept in shared memory: 16, 24 (the default) or 32 */
     int32_t traceBlocksPerSM; /* resident traversal blocks per SM; 0 = as many as fit */
-    int32_t traceBvhWidth;    /* BVH traversed: 2 (binary) or 4 (4-wide, same leaves; the default) */
-    int32_t traceRefillIdle;  /* 4-wide traversal: a warp's finished rays are replaced once this many of its
+    int32_t traceBvhWidth;    /* BVH traversed: 2 (binary), 4 (4-wide, same leaves; the default) or 8 (8-wide, same leaves,
+                                 children in octant slots) */
+    int32_t traceRefillIdle;  /* 4- and 8-wide traversal: a warp's finished rays are replaced once this many of its
                                  32 lanes are idle (1..32; 32 = only when all are; the default is 20) */
     int32_t shadeBlocks;      /* resident 128-thread blocks per SM the forward shade kernel with GenericMaterials
                                  is built for: 8 (64 registers; the default) or 14 (32 registers, more
@@ -199,7 +200,7 @@ int sst_set_tuning(sst_ctx* ctx, const SstTuning* tuning);
 /* Chooses the setting for this scene and these parameters by timing trial renders into a scratch
  * film (the caller's films are not touched), keeping the fastest of two runs per candidate:
  * first the traversal variant (BVH width x block size x shared stack entries), then the refill
- * threshold of the 4-wide traversal, then the shade kernel's build, then the shade order, then
+ * threshold of the wide traversals, then the shade kernel's build, then the shade order, then
  * the resident blocks per SM, each with trials of at least trialIterations iterations and at least 2^21 paths; then the
  * wave capacity, with trials of about four waves of 2^22 paths (within the parameters' spp).  The
  * choice is applied to the scene's context and returned in `chosen`; bestTrialMs (may be NULL)
@@ -215,7 +216,7 @@ int sst_autotune(sst_scene* scene, const SstPathTracerParams* params, int32_t tr
  *  - a caller on a latency-bound loop (shadow or picking queries per frame): cudaFree waits for
  *    the whole device, and cudaMalloc may, which stalls every stream on the GPU, not just this one.
  * The scratch it uses (split ray arrays, queue counters, job record, ray statistics, result flags)
- * is one array of 2,360,320 bytes that is part of this library's device code.  Every GPU that
+ * is one array of 2,361,344 bytes that is part of this library's device code.  Every GPU that
  * loads the library holds it until the process exits.
  * Limits and rules:
  *  - n <= SST_NOALLOC_MAX_RAYS; a larger n returns SST_ERR_INVALID_ARGUMENT and does nothing.

@@ -686,3 +686,126 @@ int buildBvh4(const float4* nodes2, int nNodes2, float4* nodes4, void* scratch, 
     return 0;
 }
 }  // namespace sst
+
+// =============================================================================================
+// 8-wide BVH from the binary one, its children in octant slots.  Each node is made from a
+// binary inner node by opening its inner children, largest surface area first, until it has eight
+// children (or only leaves remain); leaves are the binary tree's leaves, unchanged.  The children
+// are then placed in the eight slots by the octant of their box centre relative to the node's
+// (slot bit 0: +x side, bit 1: +y, bit 2: +z), greedily, best-aligned (child, slot) pair first,
+// as in the octant ordering of Ylitie, Karras and Laine, "Efficient Incoherent Ray Traversal on
+// GPUs Through Compressed Wide BVHs" (HPG 2017).  A ray whose direction has the sign bits o
+// (bit set for a negative component) then visits the slots in the order s ^ o ascending, which
+// puts the children that lie first along its direction first, without a per-node sort.
+// Node layout (15 float4, 240 bytes): lo.x[8], hi.x[8], lo.y[8], hi.y[8], lo.z[8], hi.z[8] (two
+// float4 each), child references[8] (an 8-wide node index or a leaf reference), and
+// (valid-slot mask | inner-slot mask << 8, -, -, -).  Level-synchronous like the 4-wide build.
+// =============================================================================================
+namespace sst {
+namespace {
+__global__ void k_collapse8(const float4* nodes2, const int2* frontier, const int* nFront, float4* nodes8, int* nodeCounter, int2* next,
+                            int* nNext) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= *nFront) return;
+    int2 item = frontier[i];
+    Child4 c[8];
+    int cnt = 2;
+    readChildren(nodes2, (uint32_t)item.x, c[0], c[1]);
+    while (cnt < 8) {
+        int best = -1;
+        float bestA = -1.0f;
+        for (int k = 0; k < cnt; ++k)
+            if (!(c[k].ref & kLeafFlag)) {
+                float a = halfArea(c[k]);
+                if (a > bestA) { bestA = a; best = k; }
+            }
+        if (best < 0) break;
+        Child4 a, b;
+        readChildren(nodes2, c[best].ref, a, b);
+        c[best] = a;
+        c[cnt++] = b;
+    }
+    // node centre and the children's offsets from it
+    float lo[3] = {CUDART_INF_F, CUDART_INF_F, CUDART_INF_F}, hi[3] = {-CUDART_INF_F, -CUDART_INF_F, -CUDART_INF_F};
+    for (int k = 0; k < cnt; ++k)
+        for (int a = 0; a < 3; ++a) { lo[a] = fminf(lo[a], c[k].lo[a]); hi[a] = fmaxf(hi[a], c[k].hi[a]); }
+    float off[8][3];
+    for (int k = 0; k < cnt; ++k)
+        for (int a = 0; a < 3; ++a) off[k][a] = 0.5f * (c[k].lo[a] + c[k].hi[a]) - 0.5f * (lo[a] + hi[a]);
+    // greedy assignment: repeatedly the (child, slot) pair of largest alignment between the child's
+    // offset and the slot's octant direction among the unassigned ones (ties: lower child, slot)
+    int slotOf[8], childIn[8];
+    for (int k = 0; k < 8; ++k) { slotOf[k] = -1; childIn[k] = -1; }
+    for (int n = 0; n < cnt; ++n) {
+        float bestV = -CUDART_INF_F;
+        int bc = -1, bs = -1;
+        for (int k = 0; k < cnt; ++k) {
+            if (slotOf[k] >= 0) continue;
+            for (int s = 0; s < 8; ++s) {
+                if (childIn[s] >= 0) continue;
+                float v = ((s & 1) ? off[k][0] : -off[k][0]) + ((s & 2) ? off[k][1] : -off[k][1]) + ((s & 4) ? off[k][2] : -off[k][2]);
+                if (v > bestV) { bestV = v; bc = k; bs = s; }
+            }
+        }
+        slotOf[bc] = bs;
+        childIn[bs] = bc;
+    }
+    float v[6][8];
+    uint32_t refs[8];
+    uint32_t valid = 0, inner = 0;
+    for (int s = 0; s < 8; ++s) {
+        const int k = childIn[s];
+        if (k >= 0) {
+            for (int a = 0; a < 3; ++a) { v[2 * a][s] = c[k].lo[a]; v[2 * a + 1][s] = c[k].hi[a]; }
+            uint32_t r = c[k].ref;
+            valid |= 1u << s;
+            if (!(r & kLeafFlag)) {
+                int slot = atomicAdd(nodeCounter, 1);
+                next[atomicAdd(nNext, 1)] = make_int2((int)r, slot);
+                r = (uint32_t)slot;
+                inner |= 1u << s;
+            }
+            refs[s] = r;
+        } else {
+            for (int a = 0; a < 6; ++a) v[a][s] = 0.0f;
+            refs[s] = 0u;
+        }
+    }
+    float4* out = nodes8 + 15 * (size_t)item.y;
+    for (int a = 0; a < 6; ++a) {
+        out[2 * a] = make_float4(v[a][0], v[a][1], v[a][2], v[a][3]);
+        out[2 * a + 1] = make_float4(v[a][4], v[a][5], v[a][6], v[a][7]);
+    }
+    out[12] = make_float4(__uint_as_float(refs[0]), __uint_as_float(refs[1]), __uint_as_float(refs[2]), __uint_as_float(refs[3]));
+    out[13] = make_float4(__uint_as_float(refs[4]), __uint_as_float(refs[5]), __uint_as_float(refs[6]), __uint_as_float(refs[7]));
+    out[14] = make_float4(__uint_as_float(valid | (inner << 8)), 0.0f, 0.0f, 0.0f);
+}
+}  // namespace
+
+size_t bvh8ScratchBytes(int nNodes2) { return 2 * sizeof(int2) * (size_t)std::max(1, nNodes2) + 1024; }
+
+int buildBvh8(const float4* nodes2, int nNodes2, float4* nodes8, void* scratch, int* hostNodeCount, int* hostDepth, cudaStream_t st) {
+    *hostNodeCount = 0;
+    *hostDepth = 0;
+    if (nNodes2 <= 0) return 0;
+    char* p = static_cast<char*>(scratch);
+    int* counters = reinterpret_cast<int*>(p);  // [0] node counter, [1], [2] frontier sizes
+    int2* fr[2] = {reinterpret_cast<int2*>(p + 256), reinterpret_cast<int2*>(p + 256) + nNodes2};
+    k_collapse_root<<<1, 1, 0, st>>>(fr[0], counters + 1, counters);
+    int cur = 0, depth = 0, n = 1;
+    int hostCnt = 0;
+    while (n > 0) {
+        if (++depth > 4 * kMaxBvhDepth) return -2;
+        if (cudaMemsetAsync(counters + 2 - cur, 0, sizeof(int), st) != cudaSuccess) return -1;
+        k_collapse8<<<(n + 127) / 128, 128, 0, st>>>(nodes2, fr[cur], counters + 1 + cur, nodes8, counters, fr[1 - cur], counters + 2 - cur);
+        if (cudaMemcpyAsync(&n, counters + 2 - cur, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess) return -1;
+        if (cudaStreamSynchronize(st) != cudaSuccess) return -1;
+        cur = 1 - cur;
+    }
+    if (cudaMemcpyAsync(&hostCnt, counters, sizeof(int), cudaMemcpyDeviceToHost, st) != cudaSuccess) return -1;
+    if (cudaStreamSynchronize(st) != cudaSuccess) return -1;
+    *hostNodeCount = hostCnt;
+    *hostDepth = depth;
+    return 0;
+}
+}  // namespace sst

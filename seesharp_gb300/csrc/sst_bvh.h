@@ -24,6 +24,11 @@ int buildLbvh(const float4* tri, int n, float4* nodesOut, int* orderOut, void* s
 size_t bvh4ScratchBytes(int nNodes2);
 int buildBvh4(const float4* nodes2, int nNodes2, float4* nodes4, void* scratch, int* hostNodeCount, int* hostDepth, cudaStream_t st);
 
+// 8-wide BVH over the same leaves, children in octant slots: at most nNodes2 nodes of 15 float4
+// each are written to nodes8.  Returns 0 on success with the node count and the number of levels.
+size_t bvh8ScratchBytes(int nNodes2);
+int buildBvh8(const float4* nodes2, int nNodes2, float4* nodes8, void* scratch, int* hostNodeCount, int* hostDepth, cudaStream_t st);
+
 // Gathers per-triangle records into leaf order: out[t] = in[order[t]] (triv also stamps the
 // global id into v0.w).
 void launch_leaf_gather(const int* order, int n, const float4* trivG, const float4* triNG, const int4* auxG, const int4* vtxG, float4* triv,

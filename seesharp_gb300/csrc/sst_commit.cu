@@ -381,6 +381,18 @@ void commitScene(sst_scene* s, int W, int H) {
         int rc = buildBvh4(s->nodes.as<float4>(), s->nNodes, s->nodes4.as<float4>(), scratch4.p, &s->nNodes4, &s->bvh4Depth, st);
         if (rc != 0) fail(SST_ERR_CUDA, "4-wide BVH build failed (" + std::to_string(rc) + "): " + cudaGetErrorString(cudaGetLastError()));
     }
+    // 8-wide BVH over the same leaves, children in octant slots.  Its traversal stack packs a node
+    // index into 24 bits; a scene with more 8-wide nodes is traversed 4-wide instead.
+    s->nNodes8 = 0;
+    s->bvh8Depth = 0;
+    if (s->nNodes > 0) {
+        DevBuf& scratch8 = s->ctx->commitScratch8;
+        s->nodes8.ensure(sizeof(float4) * 15 * size_t(s->nNodes));
+        scratch8.ensure(bvh8ScratchBytes(s->nNodes));
+        int rc = buildBvh8(s->nodes.as<float4>(), s->nNodes, s->nodes8.as<float4>(), scratch8.p, &s->nNodes8, &s->bvh8Depth, st);
+        if (rc != 0) fail(SST_ERR_CUDA, "8-wide BVH build failed (" + std::to_string(rc) + "): " + cudaGetErrorString(cudaGetLastError()));
+        if (s->nNodes8 >= (1 << 24)) s->nNodes8 = 0;
+    }
     std::vector<float> vnrm, vuv;
     if (anyNormals) {
         vnrm.assign(3 * size_t(nv), 0.f);
@@ -460,6 +472,8 @@ void commitScene(sst_scene* s, int W, int H) {
     d.nNodes = s->nNodes;
     d.nodes4 = s->nNodes4 > 0 ? s->nodes4.as<float4>() : nullptr;
     d.nNodes4 = s->nNodes4;
+    d.nodes8 = s->nNodes8 > 0 ? s->nodes8.as<float4>() : nullptr;
+    d.nNodes8 = s->nNodes8;
     {
         // Scene.Prepare (Scene.cs:115-136): the mean of all vertices and the distance to the
         // furthest one, summed in single precision in mesh and vertex order

@@ -191,7 +191,7 @@ struct sst_ctx {
     // scene commit: pinned staging of the packed triangle records and the BVH build's temporaries
     // (kept across commits: no allocation or device-wide free per Scene.Prepare once they fit)
     PinnedBuf commitStage;
-    DevBuf commitTri[4], commitOrder, commitScratch, commitScratch4;
+    DevBuf commitTri[4], commitOrder, commitScratch, commitScratch4, commitScratch8;
     // wavefront buffers
     DevBuf pathA[9], pathB[9];
     DevBuf hits, nee, shRo, shRd, shTgt, shJob, counters, samples, stats, film;
@@ -290,9 +290,9 @@ struct sst_scene {
     bool committed = false;
     int W = 0, H = 0;
     // device
-    DevBuf nodes, nodes4, triv, triN, triAux, triVtx, vnrm, vuv, mats, texs, texData, ems, envImg, envRowCdf, envColCdf, envHasCol, envRowMarg, queryJob;
+    DevBuf nodes, nodes4, nodes8, triv, triN, triAux, triVtx, vnrm, vuv, mats, texs, texData, ems, envImg, envRowCdf, envColCdf, envHasCol, envRowMarg, queryJob;
     DevScene dev{};
-    int nTri = 0, nNodes = 0, bvhDepth = 0, nNodes4 = 0, bvh4Depth = 0;
+    int nTri = 0, nNodes = 0, bvhDepth = 0, nNodes4 = 0, bvh4Depth = 0, nNodes8 = 0, bvh8Depth = 0;
     // adjoint: per-path radiance of the last sst_forward and its settings
     DevBuf record, gTex, gMatBase, gMatRough, gEmitter, dLdI;
     bool recordValid = false;
@@ -351,4 +351,13 @@ void batchFilmsOut(sst_ctx* ctx, const SstRenderJob* jobs, int numJobs, const st
 SstRenderStats emptyStats();
 // sst_query.cu
 const DevJob* jobTable(sst_scene* s);
+// The context's traversal setting for rays of these scenes: the 8-wide BVH is not built for a
+// scene whose node indices do not fit its stack entries, which then traverses 4-wide.
+inline TraceTuning traceFor(const sst_ctx* c, const sst_scene* const* scenes, size_t n) {
+    TraceTuning t = c->trace;
+    if (t.width == 8)
+        for (size_t k = 0; k < n; ++k)
+            if (scenes[k]->nNodes > 0 && scenes[k]->nNodes8 == 0) t.width = 4;
+    return t;
+}
 

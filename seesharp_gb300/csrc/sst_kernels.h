@@ -20,13 +20,13 @@ void launch_film_fold(const DevJob* jobs, const WaveChunk* chunks, const WaveDes
                       int maxFold, int advance, cudaStream_t s);
 // Traversal launch configuration (sst_trace.cu): threads per block (64, 128 or 256), stack
 // entries per thread kept in shared memory (16, 24 or 32), resident blocks per SM (0: as many as
-// fit), BVH width (2 or 4; a scene without a 4-wide BVH is traversed binary).
+// fit), BVH width (2, 4 or 8; a scene without a wide BVH misses every ray).
 struct TraceTuning {
     int block = kTraceBlock;
     int smemStack = kSmemStack;
     int blocksPerSM = 0;
     int width = 4;  // BVH width: 2 (binary) or 4
-    // 4-wide traversal: finished rays of a warp are replaced once this many of its 32 lanes are
+    // 4- and 8-wide traversal: finished rays of a warp are replaced once this many of its 32 lanes are
     // idle (32: only when the whole warp is); the other lanes pause in place meanwhile
     int refillIdle = kTraceRefillIdle;
 };

@@ -44,13 +44,13 @@ static void runQuery(sst_scene* s, const SstRay* rays, int n, SstHit* hits, int3
             c->qOut.ensure(size_t(n) * 4);
             dOcc = c->qOut.as<int>();
         }
-        launch_trace_query(c->trace, jobTable(s), c->qRo.as<float4>(), c->qRd.as<float4>(), cnt, cnt + 1, nullptr, dOcc, c->stats.as<DevStats>(), true,
+        launch_trace_query(traceFor(c, &s, 1), jobTable(s), c->qRo.as<float4>(), c->qRd.as<float4>(), cnt, cnt + 1, nullptr, dOcc, c->stats.as<DevStats>(), true,
                            st);
         CUDA_CHECK(cudaGetLastError());
         if (memory != SST_MEM_DEVICE) CUDA_CHECK(cudaMemcpyAsync(occl, dOcc, size_t(n) * 4, out, st));
     } else {
         c->qHits.ensure(size_t(n) * 16);
-        launch_trace_query(c->trace, jobTable(s), c->qRo.as<float4>(), c->qRd.as<float4>(), cnt, cnt + 1, c->qHits.as<float4>(), nullptr,
+        launch_trace_query(traceFor(c, &s, 1), jobTable(s), c->qRo.as<float4>(), c->qRd.as<float4>(), cnt, cnt + 1, c->qHits.as<float4>(), nullptr,
                            c->stats.as<DevStats>(), false, st);
         SstHitDev* dHits = reinterpret_cast<SstHitDev*>(hits);
         if (memory != SST_MEM_DEVICE) {
@@ -142,7 +142,7 @@ int sst_trace_light_paths(sst_scene* s, uint32_t seed, uint32_t iteration, int32
             int* qIn = cnt + d;
             int* qOut = cnt + d + 1;
             int* work = cnt + (maxDepth + 2) + d;
-            launch_trace_closest(c->trace, job, nullptr, A.ro, A.rd, qIn, work, c->lightHits.as<float4>(), c->stats.as<DevStats>(), st);
+            launch_trace_closest(traceFor(c, &s, 1), job, nullptr, A.ro, A.rd, qIn, work, c->lightHits.as<float4>(), c->stats.as<DevStats>(), st);
             launch_light_walk(job, P, A, B, c->lightHits.as<float4>(), qIn, qOut, dv, dl, items, st);
             CUDA_CHECK(cudaGetLastError());
             std::swap(A, B);
@@ -173,15 +173,15 @@ int sst_trace_light_paths(sst_scene* s, uint32_t seed, uint32_t iteration, int32
 // in this library's device image, laid out as
 //   [0, 256)      queue length and work counter of the traversal kernel
 //   [256, 512)    DevStats (ray counts)
-//   [512, 1024)   DevJob (the scene record the traversal kernel reads)
+//   [512, 2048)   DevJob (the scene record the traversal kernel reads)
 //   then          ray origins (float4 x max rays), ray directions (float4 x max rays),
 //                 occlusion flags (int x max rays).
 // ---------------------------------------------------------------------------------------------
 namespace {
-constexpr size_t kNaCounters = 0, kNaStats = 256, kNaJob = 512, kNaHeader = 1024;
+constexpr size_t kNaCounters = 0, kNaStats = 256, kNaJob = 512, kNaHeader = 2048;
 constexpr size_t kNaMaxRays = SST_NOALLOC_MAX_RAYS;
 constexpr size_t kNaBytes = kNaHeader + 2 * 16 * kNaMaxRays + 4 * kNaMaxRays;
-static_assert(kNaBytes == 2360320, "the header states the scratch size");
+static_assert(kNaBytes == 2361344, "the header states the scratch size");
 static_assert(sizeof(DevStats) <= kNaJob - kNaStats && sizeof(DevJob) <= kNaHeader - kNaJob, "scratch header too small");
 static_assert(alignof(DevJob) <= 256 && alignof(DevStats) <= 256, "scratch header alignment");
 constexpr int kNaMaxDevices = 64;
@@ -236,7 +236,7 @@ extern "C" int sst_occluded_noalloc(sst_scene* s, const SstRay* rays, int32_t n,
         DevJob j{};
         j.sc = s->dev;
         CUDA_CHECK(cudaMemcpyAsync(job, &j, sizeof(DevJob), cudaMemcpyHostToDevice, st));
-        launch_trace_query(c->trace, job, ro, rd, cnt, cnt + 1, nullptr, occ, stats, true, st);
+        launch_trace_query(traceFor(c, &s, 1), job, ro, rd, cnt, cnt + 1, nullptr, occ, stats, true, st);
         CUDA_CHECK(cudaGetLastError());
         CUDA_CHECK(cudaMemcpyAsync(occluded, occ, size_t(n) * 4, out, st));
         CUDA_CHECK(cudaStreamSynchronize(st));

@@ -156,6 +156,9 @@ void renderJobs(sst_ctx* c, std::vector<JobIn>& jobs, SstRenderStats* out, bool 
         w.wb.b.adjL = c->adjB[0].as<float4>(); w.wb.b.adjD = c->adjB[1].as<float4>(); w.wb.b.adjP = c->adjB[2].as<float4>();
         w.wb.neeG = c->neeG.as<float4>();
     }
+    std::vector<const sst_scene*> jobScenes;
+    for (auto& j : jobs) jobScenes.push_back(j.s);
+    const TraceTuning trace = traceFor(c, jobScenes.data(), jobScenes.size());
     // any GenericMaterial in the wave's scenes (otherwise the shade kernel without generic code runs)
     bool generic = false;
     for (auto& j : jobs)
@@ -224,7 +227,7 @@ void renderJobs(sst_ctx* c, std::vector<JobIn>& jobs, SstRenderStats* out, bool 
         for (int d = 1; d <= maxDepth; ++d) {
             {
                 KTimer kt(c, 1);
-                launch_trace_closest(c->trace, dj, A.job, A.ro, A.rd, cnt + kCntQueue + d, cnt + kCntWork + 2 * d, w.wb.hits, dstats, st);
+                launch_trace_closest(trace, dj, A.job, A.ro, A.rd, cnt + kCntQueue + d, cnt + kCntWork + 2 * d, w.wb.hits, dstats, st);
             }
             {
                 KTimer kt(c, 2);
@@ -260,7 +263,7 @@ void renderJobs(sst_ctx* c, std::vector<JobIn>& jobs, SstRenderStats* out, bool 
             }
             {
                 KTimer kt(c, 3);
-                launch_trace_shadow(c->trace, dj, w.wb.shJob, w.wb.shRo, w.wb.shRd, w.wb.shTgt, cnt + kCntShadow + d, cnt + kCntWork + 2 * d + 1, curNee,
+                launch_trace_shadow(trace, dj, w.wb.shJob, w.wb.shRo, w.wb.shRd, w.wb.shTgt, cnt + kCntShadow + d, cnt + kCntWork + 2 * d + 1, curNee,
                                     dstats, st);
             }
             launches += c->shadeOrder ? 4 : 3;  // closest hit, shade order, shade, shadow rays
@@ -427,7 +430,7 @@ static TraceTuning toTrace(const SstTuning& t) { return TraceTuning{t.traceBlock
 
 static void checkTuning(const SstTuning& t) {
     if (!traceTuningValid(toTrace(t)))
-        fail(SST_ERR_INVALID_ARGUMENT, "traceBlock must be 64, 128 or 256, traceStackShared 16, 24 or 32, traceBvhWidth 2 or 4, and traceRefillIdle in [1, 32]");
+        fail(SST_ERR_INVALID_ARGUMENT, "traceBlock must be 64, 128 or 256, traceStackShared 16, 24 or 32, traceBvhWidth 2, 4 or 8, and traceRefillIdle in [1, 32]");
     if (t.waveCapacity != 0 && (t.waveCapacity < 1024 || t.waveCapacity > (1 << 24)))
         fail(SST_ERR_INVALID_ARGUMENT, "waveCapacity must be 0 or in [1024, 2^24]");
     if (t.traceBlocksPerSM < 0 || t.traceBlocksPerSM > 64) fail(SST_ERR_INVALID_ARGUMENT, "traceBlocksPerSM must be in [0, 64]");
@@ -605,7 +608,7 @@ int sst_autotune(sst_scene* s, const SstPathTracerParams* p, int32_t trialIterat
         const int kIters = (int)std::max<long long>(trialIterations, ((long long)defaultWaveCapacity() + tpix - 1) / tpix);
         try {
             // traversal variant
-            for (int wdt : {2, 4})
+            for (int wdt : {2, 4, 8})
                 for (int b : {64, 128, 256})
                     for (int k : {16, 24, 32}) {
                         SstTuning t = best;
@@ -616,8 +619,8 @@ int sst_autotune(sst_scene* s, const SstPathTracerParams* p, int32_t trialIterat
                         double ms = trial(t, kIters);
                         if (ms < bestMs) { bestMs = ms; best = t; }
                     }
-            // refill threshold of the 4-wide traversal
-            if (best.traceBvhWidth == 4)
+            // refill threshold of the wide traversals
+            if (best.traceBvhWidth != 2)
                 for (int ri : {32, 12, 24}) {
                     if (ri == best.traceRefillIdle) continue;
                     SstTuning t = best;

@@ -2,10 +2,11 @@
 // (Integrators/PathTracer.cs:319,428,467).
 //
 // Binary BVH with both child boxes stored in the parent (64-byte nodes read as four 128-bit
-// loads) or the 4-wide BVH over the same leaves (128-byte nodes), watertight ray/triangle test
-// (Woop, Benthin, Wald 2013), a per-thread traversal stack in shared memory with a local-memory
-// tail, and persistent warps: the binary kernel fetches 32 rays at a time, the 4-wide one replaces
-// finished rays once a set number of the warp's lanes are idle.
+// loads), or the 4-wide (128-byte nodes) or 8-wide (240-byte nodes, children in octant slots) BVH
+// over the same leaves, watertight ray/triangle test (Woop, Benthin, Wald 2013), a per-thread
+// traversal stack in shared memory with a local-memory tail, and persistent warps: the binary
+// kernel fetches 32 rays at a time, the wide ones replace finished rays once a set number of the
+// warp's lanes are idle.
 // The block size and the number of stack entries kept in shared memory are template parameters;
 // the autotuner picks one of the instantiated variants per context (TraceTuning).  The result of
 // a query does not depend on the variant: the traversal order is the same, and closest-hit ties
@@ -272,6 +273,156 @@ SST_D bool trav4Run(Trav4& s, int* sstack, int* lstack, int* errFlags, int pause
     }
 }
 
+// 8-wide traversal over the same leaves, children in octant slots (sst_bvh.cu).  A ray visits a
+// node's hit children in the order slot ^ o ascending, o the sign bits of its direction, which
+// approximates front to back without a sort.  A node visit tests the eight child boxes against the
+// near and far planes the direction selects (the near-plane arrays are read directly, so every
+// slab is one fused multiply-add).  It is the other widths' arithmetic: with a finite inverse
+// direction the near plane's t is the smaller of the two, so a box passes here exactly when it
+// passes there, and with an infinite one (a zero direction component) a NaN slab is ignored, which
+// passes at least the boxes the other widths pass.  The hit children become a bit mask in visiting
+// order.  The
+// traversal keeps one (node, remaining mask) group in registers; moving to an inner child pushes
+// the rest of the group as one stack entry (node << 8 | mask), and a leaf child is tested in
+// place.  SSTACK entries per thread in shared memory, the rest in local memory (the depth of the
+// tree bounds the stack).
+struct Bvh8 {
+    const float4* nodes8;
+    const float4* triv;
+    int nNodes8;
+};
+SST_D Bvh8 bvh8Of(const DevScene& sc) { return Bvh8{sc.nodes8, sc.triv, sc.nNodes8}; }
+
+struct Trav8 {
+    Bvh8 bvh;
+    float3 org, inv, oi;
+    RayPre pre;
+    float tmin;
+    TraceResult r;
+    int bestGid;
+    int sp;
+    uint32_t node;  // the group in registers: an 8-wide node ...
+    uint32_t mask;  // ... and its hit children not yet visited (bit j: slot j ^ oct)
+    uint32_t oct;   // sign bits of the direction (bit a set when inv[a] < 0)
+    bool done;
+};
+
+// Mask of the hit children of `node` in visiting order (bit j set: slot j ^ oct was hit).
+SST_D uint32_t visit8(const Trav8& s, uint32_t node) {
+    const float4* nd = s.bvh.nodes8 + 15 * (size_t)node;
+    const int ox = (int)(s.oct & 1u), oy = (int)((s.oct >> 1) & 1u), oz = (int)((s.oct >> 2) & 1u);
+    const uint32_t valid = __float_as_uint(__ldg(&nd[14].x)) & 0xFFu;
+    const float hitT = s.r.t * 1.0000004f;  // conservative far bound (box/triangle rounding)
+    uint32_t hm = 0;
+    // two halves of four children (24 box floats live at a time); near planes: lo for a positive
+    // direction component, hi for a negative one
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        const float4 nx = __ldg(nd + 2 * ox + h), fx = __ldg(nd + 2 - 2 * ox + h);
+        const float4 ny = __ldg(nd + 4 + 2 * oy + h), fy = __ldg(nd + 6 - 2 * oy + h);
+        const float4 nz = __ldg(nd + 8 + 2 * oz + h), fz = __ldg(nd + 10 - 2 * oz + h);
+        const float NX[4] = {nx.x, nx.y, nx.z, nx.w}, FX[4] = {fx.x, fx.y, fx.z, fx.w};
+        const float NY[4] = {ny.x, ny.y, ny.z, ny.w}, FY[4] = {fy.x, fy.y, fy.z, fy.w};
+        const float NZ[4] = {nz.x, nz.y, nz.z, nz.w}, FZ[4] = {fz.x, fz.y, fz.z, fz.w};
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const float tn = fmaxf(fmaxf(fmaf(NX[k], s.inv.x, s.oi.x), fmaf(NY[k], s.inv.y, s.oi.y)), fmaxf(fmaf(NZ[k], s.inv.z, s.oi.z), s.tmin));
+            const float tf = fminf(fminf(fmaf(FX[k], s.inv.x, s.oi.x), fmaf(FY[k], s.inv.y, s.oi.y)), fminf(fmaf(FZ[k], s.inv.z, s.oi.z), hitT));
+            hm |= (tn <= tf * 1.0000004f) ? (1u << (4 * h + k)) : 0u;
+        }
+    }
+    hm &= valid;
+    // slot k -> bit k ^ oct
+    if (s.oct & 1u) hm = ((hm & 0x55u) << 1) | ((hm >> 1) & 0x55u);
+    if (s.oct & 2u) hm = ((hm & 0x33u) << 2) | ((hm >> 2) & 0x33u);
+    if (s.oct & 4u) hm = ((hm & 0x0Fu) << 4) | ((hm >> 4) & 0x0Fu);
+    return hm;
+}
+
+SST_D void trav8Begin(Trav8& s, const Bvh8 bvh, float3 org, float3 dir, float tmin, float tmax) {
+    s.bvh = bvh;
+    s.org = org;
+    s.pre = rayPre(dir);
+    s.inv = mk(1.0f / dir.x, 1.0f / dir.y, 1.0f / dir.z);
+    s.oi = mk(-org.x * s.inv.x, -org.y * s.inv.y, -org.z * s.inv.z);
+    s.oct = (s.inv.x < 0.0f ? 1u : 0u) | (s.inv.y < 0.0f ? 2u : 0u) | (s.inv.z < 0.0f ? 4u : 0u);
+    s.tmin = tmin;
+    s.r = TraceResult{tmax, 0.f, 0.f, -1};
+    s.bestGid = 0x7FFFFFFF;
+    s.sp = 0;
+    s.node = 0;
+    s.done = bvh.nNodes8 == 0 || !(tmax > tmin);
+    s.mask = s.done ? 0u : visit8(s, 0u);  // the root's hit children
+    if (!s.done && s.mask == 0u) s.done = true;
+}
+
+// Traversal steps until the ray is finished (true, result in s.r) or, with pauseIdle > 0, until
+// pauseIdle lanes of the warp are outside this loop (false after at least one step; a later call
+// resumes).  lstack: this lane's local-memory stack tail.
+template <bool ANY, int BLOCK, int SSTACK>
+SST_D bool trav8Run(Trav8& s, int* sstack, int* lstack, int* errFlags, int pauseIdle) {
+    const int tid = threadIdx.x;
+    bool first = true;
+    for (;;) {
+        if (!first && pauseIdle > 0 && 32 - __popc(__activemask()) >= pauseIdle) return false;
+        first = false;
+        if (s.mask == 0u) {
+            if (s.sp == 0) return true;
+            --s.sp;
+            const uint32_t e = (uint32_t)(s.sp < SSTACK ? sstack[s.sp * BLOCK + tid] : lstack[s.sp - SSTACK]);
+            s.node = e >> 8;
+            s.mask = e & 0xFFu;
+        }
+        const uint32_t j = (uint32_t)(__ffs((int)s.mask) - 1);
+        s.mask &= s.mask - 1u;
+        const uint32_t slot = j ^ s.oct;
+        const uint32_t ref = __float_as_uint(__ldg(reinterpret_cast<const float*>(s.bvh.nodes8 + 15 * (size_t)s.node + 12) + slot));
+        if (!(ref & kLeafFlag)) {
+            if (s.mask) {
+                const int e = (int)((s.node << 8) | s.mask);
+                if (s.sp < SSTACK) sstack[s.sp * BLOCK + tid] = e;
+                else if (s.sp < kMaxStack) lstack[s.sp - SSTACK] = e;
+                else { atomicOr(errFlags, 1); return true; }
+                ++s.sp;
+            }
+            s.node = ref;
+            s.mask = visit8(s, ref);
+        } else {
+            const int firstTri = (int)(ref & kLeafFirstMask);
+            const int cnt = (int)((ref >> kLeafCountShift) & 0xF) + 1;
+            for (int k = 0; k < cnt; ++k) {
+                const int ti = firstTri + k;
+                const float4 a = __ldg(&s.bvh.triv[3 * (size_t)ti]), b = __ldg(&s.bvh.triv[3 * (size_t)ti + 1]), c = __ldg(&s.bvh.triv[3 * (size_t)ti + 2]);
+                float t, u, v;
+                // allow an equal distance so that ties can resolve to the smaller id
+                const float lim = ANY ? s.r.t : __uint_as_float(__float_as_uint(s.r.t) + (s.r.t < CUDART_INF_F ? 1u : 0u));
+                if (isectTri(s.org, s.pre, f3(a), f3(b), f3(c), s.tmin, lim, t, u, v)) {
+                    const int gid = __float_as_int(a.w);
+                    if (ANY) { s.r.t = t; s.r.u = u; s.r.v = v; s.r.tri = ti; return true; }
+                    if (t < s.r.t || (t == s.r.t && gid < s.bestGid)) { s.r.t = t; s.r.u = u; s.r.v = v; s.r.tri = ti; s.bestGid = gid; }
+                }
+            }
+        }
+    }
+}
+
+// The resumable traversals (4- and 8-wide) behind one interface for the kernel's refill loop.
+template <int W> struct WideTrav;
+template <> struct WideTrav<4> {
+    using State = Trav4;
+    static constexpr int kStack = kMaxStack4;
+    SST_D static void begin(State& s, const DevScene& sc, float3 o, float3 d, float tmin, float tmax) { trav4Begin(s, bvh4Of(sc), o, d, tmin, tmax); }
+    template <bool ANY, int BLOCK, int SSTACK>
+    SST_D static bool run(State& s, int* sstack, int* lstack, int* err, int pause) { return trav4Run<ANY, BLOCK, SSTACK>(s, sstack, lstack, err, pause); }
+};
+template <> struct WideTrav<8> {
+    using State = Trav8;
+    static constexpr int kStack = kMaxStack;
+    SST_D static void begin(State& s, const DevScene& sc, float3 o, float3 d, float tmin, float tmax) { trav8Begin(s, bvh8Of(sc), o, d, tmin, tmax); }
+    template <bool ANY, int BLOCK, int SSTACK>
+    SST_D static bool run(State& s, int* sstack, int* lstack, int* err, int pause) { return trav8Run<ANY, BLOCK, SSTACK>(s, sstack, lstack, err, pause); }
+};
+
 // mode 0: closest hit -> hits[i]; mode 1: shadow rays, zero nee[tgt[i]] when occluded;
 // mode 2: any hit -> occl[i] = 1/0.
 // Resident threads per SM the traversal kernels are compiled for (register budget); 0: no bound.
@@ -280,7 +431,7 @@ SST_D bool trav4Run(Trav4& s, int* sstack, int* lstack, int* errFlags, int pause
 #ifndef SST_TRACE_MIN_THREADS
 #define SST_TRACE_MIN_THREADS 1024
 #endif
-template <int MODE, int BLOCK, int SSTACK, bool WIDE>
+template <int MODE, int BLOCK, int SSTACK, int W>
 __global__ void __launch_bounds__(BLOCK, SST_TRACE_MIN_THREADS > 0 ? SST_TRACE_MIN_THREADS / BLOCK : 1) k_trace(const DevJob* __restrict__ jobs, const uint32_t* __restrict__ rayJob, const float4* ro,
                                                  const float4* rd, const int* count, int* work, float4* hits, const int* tgt, float4* nee,
                                                  int* occl, DevStats* stats, int countRays, int refillIdle) {
@@ -290,12 +441,13 @@ __global__ void __launch_bounds__(BLOCK, SST_TRACE_MIN_THREADS > 0 ? SST_TRACE_M
     if (countRays && blockIdx.x == 0 && threadIdx.x == 0) {
         if (MODE == 0) atomicAdd(&stats->rays, (unsigned long long)n);
     }
-    if constexpr (WIDE) {
+    if constexpr (W != 2) {
         // Lanes whose ray is finished take new rays together once refillIdle of the warp's lanes
         // are idle (32: once the whole warp is); the others pause in place and resume after the
-        // refill.  A scene without a 4-wide BVH has no triangles: every ray misses.
-        int lstack[kMaxStack4 - SSTACK];
-        Trav4 s;
+        // refill.  A scene without a wide BVH has no triangles: every ray misses.
+        using T = WideTrav<W>;
+        int lstack[T::kStack - SSTACK];
+        typename T::State s;
         int i = -1;
         bool exhausted = false;
         const int thr = refillIdle > 0 && refillIdle < 32 ? refillIdle : 32;
@@ -313,13 +465,13 @@ __global__ void __launch_bounds__(BLOCK, SST_TRACE_MIN_THREADS > 0 ? SST_TRACE_M
                         i = j;
                         const float4 o = ro[j], d = rd[j];
                         const uint32_t jb = rayJob ? rayJob[j] : 0u;
-                        trav4Begin(s, bvh4Of(jobs[jb].sc), f3(o), f3(d), o.w, d.w);
+                        T::begin(s, jobs[jb].sc, f3(o), f3(d), o.w, d.w);
                     }
                 }
             }
             if (__ballot_sync(0xffffffffu, i >= 0) == 0) break;  // every lane idle: the queue is drained
             if (i >= 0) {
-                const bool fin = s.done || trav4Run<MODE != 0, BLOCK, SSTACK>(s, sstack, lstack, &stats->errorFlags, exhausted ? 0 : thr);
+                const bool fin = s.done || T::template run<MODE != 0, BLOCK, SSTACK>(s, sstack, lstack, &stats->errorFlags, exhausted ? 0 : thr);
                 if (fin) {
                     const TraceResult& h = s.r;
                     if (MODE == 0) hits[i] = make_float4(h.t, h.u, h.v, __int_as_float(h.tri));
@@ -359,9 +511,9 @@ __global__ void __launch_bounds__(BLOCK, SST_TRACE_MIN_THREADS > 0 ? SST_TRACE_M
 using TraceKernel = void (*)(const DevJob*, const uint32_t*, const float4*, const float4*, const int*, int*, float4*, const int*, float4*, int*,
                              DevStats*, int, int);
 
-template <int BLOCK, int SSTACK, bool WIDE>
+template <int BLOCK, int SSTACK, int W>
 struct TraceVariant {
-    static constexpr TraceKernel k[3] = {k_trace<0, BLOCK, SSTACK, WIDE>, k_trace<1, BLOCK, SSTACK, WIDE>, k_trace<2, BLOCK, SSTACK, WIDE>};
+    static constexpr TraceKernel k[3] = {k_trace<0, BLOCK, SSTACK, W>, k_trace<1, BLOCK, SSTACK, W>, k_trace<2, BLOCK, SSTACK, W>};
 };
 
 static const int kBlocks[3] = {64, 128, 256};
@@ -373,34 +525,43 @@ static int indexOf(const int* a, int v) {
     return -1;
 }
 
-// Variant index: (width 2 or 4) x block x stack, 18 in all.
+// Variant index: (width 2, 4 or 8) x block x stack, 27 in all.
 static int variantOf(const TraceTuning& t) {
     int bi = indexOf(kBlocks, t.block), si = indexOf(kStacks, t.smemStack);
-    if (bi < 0 || si < 0 || (t.width != 2 && t.width != 4)) return -1;
-    return (t.width == 4 ? 9 : 0) + bi * 3 + si;
+    if (bi < 0 || si < 0 || (t.width != 2 && t.width != 4 && t.width != 8)) return -1;
+    return (t.width == 8 ? 18 : (t.width == 4 ? 9 : 0)) + bi * 3 + si;
 }
 
 static TraceKernel traceKernel(int mode, int variant) {
 #define SST_TV(B, S, W) TraceVariant<B, S, W>::k[mode]
     switch (variant) {
-        case 0: return SST_TV(64, 16, false);
-        case 1: return SST_TV(64, 24, false);
-        case 2: return SST_TV(64, 32, false);
-        case 3: return SST_TV(128, 16, false);
-        case 4: return SST_TV(128, 24, false);
-        case 5: return SST_TV(128, 32, false);
-        case 6: return SST_TV(256, 16, false);
-        case 7: return SST_TV(256, 24, false);
-        case 8: return SST_TV(256, 32, false);
-        case 9: return SST_TV(64, 16, true);
-        case 10: return SST_TV(64, 24, true);
-        case 11: return SST_TV(64, 32, true);
-        case 12: return SST_TV(128, 16, true);
-        case 13: return SST_TV(128, 24, true);
-        case 14: return SST_TV(128, 32, true);
-        case 15: return SST_TV(256, 16, true);
-        case 16: return SST_TV(256, 24, true);
-        default: return SST_TV(256, 32, true);
+        case 0: return SST_TV(64, 16, 2);
+        case 1: return SST_TV(64, 24, 2);
+        case 2: return SST_TV(64, 32, 2);
+        case 3: return SST_TV(128, 16, 2);
+        case 4: return SST_TV(128, 24, 2);
+        case 5: return SST_TV(128, 32, 2);
+        case 6: return SST_TV(256, 16, 2);
+        case 7: return SST_TV(256, 24, 2);
+        case 8: return SST_TV(256, 32, 2);
+        case 9: return SST_TV(64, 16, 4);
+        case 10: return SST_TV(64, 24, 4);
+        case 11: return SST_TV(64, 32, 4);
+        case 12: return SST_TV(128, 16, 4);
+        case 13: return SST_TV(128, 24, 4);
+        case 14: return SST_TV(128, 32, 4);
+        case 15: return SST_TV(256, 16, 4);
+        case 16: return SST_TV(256, 24, 4);
+        case 17: return SST_TV(256, 32, 4);
+        case 18: return SST_TV(64, 16, 8);
+        case 19: return SST_TV(64, 24, 8);
+        case 20: return SST_TV(64, 32, 8);
+        case 21: return SST_TV(128, 16, 8);
+        case 22: return SST_TV(128, 24, 8);
+        case 23: return SST_TV(128, 32, 8);
+        case 24: return SST_TV(256, 16, 8);
+        case 25: return SST_TV(256, 24, 8);
+        default: return SST_TV(256, 32, 8);
     }
 #undef SST_TV
 }
@@ -410,7 +571,7 @@ bool traceTuningValid(const TraceTuning& t) { return variantOf(t) >= 0 && t.bloc
 // Resident blocks per SM of a variant (occupancy), computed once per variant for the device that
 // first asks (the devices of one machine are identical).
 static int maxBlocksPerSM(int variant) {
-    static int cache[18] = {};
+    static int cache[27] = {};
     int& c = cache[variant];
     if (c == 0) {
         int bps = 0;

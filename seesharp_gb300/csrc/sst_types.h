@@ -65,6 +65,7 @@ struct DevCamera {
 struct DevScene {
     const float4* nodes;   // binary BVH: 4 float4 per node
     const float4* nodes4;  // 4-wide BVH over the same leaves: 8 float4 per node
+    const float4* nodes8;  // 8-wide BVH over the same leaves, octant slots: 15 float4 per node
     const float4* triv;    // 3 float4 per leaf-ordered triangle: v1 (w = global tri id), v2, v3
     const float4* triN;    // per leaf-ordered triangle: face normal, w = emitter index (int bits, -1)
     const int4* triAux;    // (material, mesh, local face, attribute flags: 1 normals, 2 uvs)
@@ -79,6 +80,7 @@ struct DevScene {
     int nTri;
     int nNodes;
     int nNodes4;
+    int nNodes8;
     int hasEnv;
     float3 sceneCenter;  // Scene.Center / Scene.Radius (Scene.cs:115-136)
     float sceneRadius;

@@ -26,7 +26,7 @@ from seesharp_gb300 import _native, workloads
 pytestmark = pytest.mark.gpu
 
 
-@pytest.fixture(params=[2, 4], ids=["bvh2", "bvh4"])
+@pytest.fixture(params=[2, 4, 8], ids=["bvh2", "bvh4", "bvh8"])
 def width(request):
     ctx = _native.default_context()
     base = _native.get_tuning(ctx)
