@@ -177,6 +177,39 @@ template <class T> static void matSample(const Scene<T>& sc, int mat, const floa
 }
 }  // namespace
 
+// Monte Carlo integral over directions with a 99% confidence interval, restating the estimator of
+// SeeSharp.Tests/Core/Shading/Material_SampleTransform.cs:40-69: 32 batches, batch i seeded
+// RNG(18273912, i, 1313), per sample a 2D primary sample, then one more number for the component
+// choice; zero-pdf samples are skipped; per-batch float sums of val / N and val^2 / N (added up in
+// batch order here, under a lock in any order there); variance = E[v^2] - E[v]^2, interval
+// mean +- 2.576 sqrt(variance / N).
+template <class F>
+static void mcInterval(int numSamples, F sampleFn, float* ci) {
+    const int numBatches = 32;
+    numSamples = (numSamples / numBatches) * numBatches;
+    const float invNum = 1.0f / float(numSamples);
+    float total = 0.0f, totalSquares = 0.0f;
+    for (int b = 0; b < numBatches; ++b) {
+        float result = 0.0f, squares = 0.0f;
+        Rng rng(18273912u, uint32_t(b), 1313u);
+        for (int j = 0; j < numSamples / numBatches; ++j) {
+            V2<float> primary = rng.NextFloat2D();
+            float u = rng.NextFloat();
+            float val;
+            if (!sampleFn(u, primary, val)) continue;
+            result += val * invNum;
+            squares += val * val * invNum;
+        }
+        total += result;
+        totalSquares += squares;
+    }
+    const float variance = totalSquares - total * total;
+    if (variance <= 0.0f) { ci[0] = ci[1] = total; return; }
+    const float off = std::sqrt(variance) / std::sqrt(float(numSamples));
+    ci[0] = total - 2.576f * off;
+    ci[1] = total + 2.576f * off;
+}
+
 extern "C" {
 
 void* ora_scene_create(int fp64) { auto* h = new Handle(); h->fp64 = fp64; return h; }
@@ -396,6 +429,51 @@ int ora_trace_two64(void* p, const double* rays, int n, double* hits, double* se
     return 0;
 }
 
+// Material_SampleTransform.cs:71-117 on the FP32 oracle: mode 0 integrates EvaluateWithCosine's
+// channel average with uniform-sphere directions, mode 1 the same with the material's own Sample,
+// mode 2 the material's pdf with uniform-sphere directions.  pt: the 11-float surface point.
+int ora_material_integrate(void* p, int mat, const float* pt, const float* outDir, int mode, int numSamples, float* ci) {
+    Handle* H = static_cast<Handle*>(p);
+    const Scene<float>& sc = H->s32;
+    if (mat < 0 || mat >= int(sc.materials.size()) || mode < 0 || mode > 2) return -1;
+    SurfacePoint<float> sp = PointFrom<float>(pt);
+    ShadingContext<float> ctx(sp, V3<float>(outDir[0], outDir[1], outDir[2]));
+    MaterialEval<float> me{sc, sc.materials[mat]};
+    mcInterval(numSamples, [&](float u, V2<float> primary, float& val) {
+        V3<float> dir;
+        float pdf;
+        if (mode == 1) {
+            BsdfSample<float> smp = me.Sample(ctx, u, primary);
+            dir = smp.Direction;
+            pdf = smp.Pdf;
+        } else {
+            DirectionSample<float> smp = ToUniformSphere(primary);
+            dir = smp.Direction;
+            pdf = smp.Pdf;
+        }
+        if (pdf == 0.0f) return false;
+        float f;
+        if (mode == 2) { float fwd, rev; me.Pdf(ctx, dir, fwd, rev); f = fwd; }
+        else f = me.EvaluateWithCosine(ctx, dir).Average();
+        val = f / pdf;
+        return true;
+    }, ci);
+    return 0;
+}
+
+// Material_SampleTransform.cs:285-303: the visible-normal pdf TrowbridgeReitzDistribution.Pdf(outDir, dir)
+// integrated over uniform-sphere directions.
+void ora_ggx_pdf_integrate(float ax, float ay, const float* outDir, int numSamples, float* ci) {
+    GGX<float> ndf{ax, ay};
+    V3<float> o(outDir[0], outDir[1], outDir[2]);
+    mcInterval(numSamples, [&](float, V2<float> primary, float& val) {
+        DirectionSample<float> smp = ToUniformSphere(primary);
+        if (smp.Pdf == 0.0f) return false;
+        val = ndf.Pdf(o, smp.Direction) / smp.Pdf;
+        return true;
+    }, ci);
+}
+
 int ora_camera_ray(void* p, float fx, float fy, float* org, float* dir) {
     Handle* H = static_cast<Handle*>(p);
     if (H->fp64) {
@@ -582,6 +660,47 @@ float ora_fresnel_dielectric(float c, float ei, float et) { return FresnelDielec
 
 // Emitter/mesh sampling at the scene level: sample emitter e with primary (u1, u2); out = pos 3,
 // normal 3, shading normal 3, pdf.
+// Emitter.SampleRay followed by Emitter.SampleRayInverse (DiffuseEmitter.cs:44-79,
+// GlossyEmitter.cs:47-86): the inverse maps the sampled point back through
+// SampleWarp.FromUniformTriangle (:16-22) and the direction, in the shading frame of the point,
+// through FromCosHemisphere (:139-145) or FromCosineLobe(exponent + 1) (:184-190).
+// out: posPrimary (2), dirPrimary (2), point (3), direction (3), pdf, weight (3).
+int ora_emitter_ray_roundtrip(void* p, int e, const float* primPos, const float* primDir, float* out) {
+    Handle* H = static_cast<Handle*>(p);
+    const Scene<float>& sc = H->s32;
+    if (e < 0 || e >= int(sc.emitters.size())) return -1;
+    const Emitter<float>& em = sc.emitters[e];
+    EmitterRaySample<float> r = EmitterSampleRay(sc, em, V2<float>(primPos[0], primPos[1]), V2<float>(primDir[0], primDir[1]));
+    V2<float> posP = FromUniformTriangle(r.point.bary);
+    V3<float> n = r.point.shadingNormal, t, b;
+    ComputeBasisVectors(n, t, b);
+    V3<float> local(dot(t, r.dir), dot(b, r.dir), dot(n, r.dir));
+    V2<float> dirP;
+    if (!em.glossy()) {
+        dirP = FromCosHemisphere(local);
+    } else {
+        V2<float> sph = CartesianToSpherical(local);
+        float x = sph.x / (2.0f * PI<float>());
+        float c = std::cos(sph.y);
+        dirP = V2<float>(x, std::pow(c, (em.exponent + 1.0f) + 1.0f));
+    }
+    out[0] = posP.x; out[1] = posP.y; out[2] = dirP.x; out[3] = dirP.y;
+    out[4] = r.point.position.x; out[5] = r.point.position.y; out[6] = r.point.position.z;
+    out[7] = r.dir.x; out[8] = r.dir.y; out[9] = r.dir.z;
+    out[10] = r.pdf; out[11] = r.weight.r; out[12] = r.weight.g; out[13] = r.weight.b;
+    return 0;
+}
+
+// Mesh.ComputeShadingNormal (Geometry/Mesh.cs) of a face at barycentrics (u, v).
+int ora_mesh_shading_normal(void* p, int mesh, int face, float u, float v, float* out) {
+    Handle* H = static_cast<Handle*>(p);
+    const Scene<float>& sc = H->s32;
+    if (mesh < 0 || mesh >= int(sc.meshes.size()) || face < 0 || face >= sc.meshes[mesh].numFaces()) return -1;
+    V3<float> n = sc.meshes[mesh].ShadingNormal(face, V2<float>(u, v));
+    out[0] = n.x; out[1] = n.y; out[2] = n.z;
+    return 0;
+}
+
 int ora_emitter_sample(void* p, int e, float u1, float u2, float* out) {
     Handle* H = static_cast<Handle*>(p);
     const Scene<float>& sc = H->s32;

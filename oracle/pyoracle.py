@@ -46,6 +46,10 @@ def lib():
         L.ora_trace.argtypes = [vp, vp, i, vp, i]
         L.ora_trace_brute64.argtypes = [vp, vp, i, vp, vp]
         L.ora_trace_two64.argtypes = [vp, vp, i, vp, vp, i]
+        L.ora_material_integrate.argtypes = [vp, i, vp, vp, i, i, vp]
+        L.ora_emitter_ray_roundtrip.argtypes = [vp, i, vp, vp, vp]
+        L.ora_mesh_shading_normal.argtypes = [vp, i, i, f, f, vp]
+        L.ora_ggx_pdf_integrate.argtypes = [f, f, vp, i, vp]
         L.ora_camera_ray.argtypes = [vp, f, f, vp, vp]
         L.ora_material_eval.argtypes = [vp, i, vp, vp, vp, vp, vp, vp]
         L.ora_material_sample.argtypes = [vp, i, vp, vp, f, f, f, vp, vp, vp, vp]
@@ -234,6 +238,30 @@ class OracleScene:
         self.L.ora_trace_two64(self.h, _p(rays), n, _p(hits), _p(second), int(nthreads or os.cpu_count() or 1))
         return hits, second
 
+    def material_integrate(self, mat, point, out_dir, mode, n=1_000_000):
+        """99% confidence interval of a Monte Carlo integral over directions (the estimator of
+        Material_SampleTransform.cs:40-69): mode 0 the albedo with uniform-sphere sampling, 1 the
+        albedo with the material's own sampling, 2 the integral of its pdf."""
+        pt, od = f32(point, (11,)), f32(out_dir, (3,))
+        ci = np.zeros(2, np.float32)
+        if self.L.ora_material_integrate(self.h, int(mat), _p(pt), _p(od), int(mode), int(n), _p(ci)) != 0:
+            raise ValueError("invalid material or mode")
+        return float(ci[0]), float(ci[1])
+
+    def emitter_ray_roundtrip(self, e, prim_pos, prim_dir):
+        """Emitter.SampleRay then SampleRayInverse: (posPrimary, dirPrimary, point, direction, pdf, weight)."""
+        out = np.zeros(14, np.float32)
+        pp, pd = f32(prim_pos, (2,)), f32(prim_dir, (2,))  # kept alive across the call
+        if self.L.ora_emitter_ray_roundtrip(self.h, int(e), _p(pp), _p(pd), _p(out)) != 0:
+            raise ValueError("no such emitter")
+        return out[0:2], out[2:4], out[4:7], out[7:10], float(out[10]), out[11:14]
+
+    def mesh_shading_normal(self, mesh, face, u, v):
+        out = np.zeros(3, np.float32)
+        if self.L.ora_mesh_shading_normal(self.h, int(mesh), int(face), float(u), float(v), _p(out)) != 0:
+            raise ValueError("no such face")
+        return out
+
     def camera_ray(self, fx, fy):
         o = np.zeros(3, np.float32)
         d = np.zeros(3, np.float32)
@@ -347,28 +375,33 @@ def rng_ints(seed, mx, n):
 
 
 def ggx_D(ax, ay, n):
-    return float(lib().ora_ggx_D(ax, ay, _p(f32(n, (3,)))))
+    n = f32(n, (3,))  # a named array: the pointer must outlive the call
+    return float(lib().ora_ggx_D(ax, ay, _p(n)))
 
 
 def ggx_pdf(ax, ay, o, n):
-    return float(lib().ora_ggx_pdf(ax, ay, _p(f32(o, (3,))), _p(f32(n, (3,)))))
+    o, n = f32(o, (3,)), f32(n, (3,))
+    return float(lib().ora_ggx_pdf(ax, ay, _p(o), _p(n)))
 
 
 def ggx_sample(ax, ay, o, u1, u2):
     out = np.zeros(3, np.float32)
-    lib().ora_ggx_sample(ax, ay, _p(f32(o, (3,))), u1, u2, _p(out))
+    o = f32(o, (3,))
+    lib().ora_ggx_sample(ax, ay, _p(o), u1, u2, _p(out))
     return out
 
 
 def world_to_shading(n, d):
     out = np.zeros(3, np.float32)
-    lib().ora_world_to_shading(_p(f32(n, (3,))), _p(f32(d, (3,))), _p(out))
+    n, d = f32(n, (3,)), f32(d, (3,))
+    lib().ora_world_to_shading(_p(n), _p(d), _p(out))
     return out
 
 
 def shading_to_world(n, d):
     out = np.zeros(3, np.float32)
-    lib().ora_shading_to_world(_p(f32(n, (3,))), _p(f32(d, (3,))), _p(out))
+    n, d = f32(n, (3,)), f32(d, (3,))
+    lib().ora_shading_to_world(_p(n), _p(d), _p(out))
     return out
 
 
@@ -408,6 +441,13 @@ def warp_disc(u1, u2):
     p = np.zeros(2, np.float32)
     lib().ora_warp_disc(u1, u2, _p(p))
     return p
+
+
+def ggx_pdf_integrate(ax, ay, out_dir, n=1_000_000):
+    od = f32(out_dir, (3,))
+    ci = np.zeros(2, np.float32)
+    lib().ora_ggx_pdf_integrate(float(ax), float(ay), _p(od), int(n), _p(ci))
+    return float(ci[0]), float(ci[1])
 
 
 def fresnel_dielectric(c, ei, et):

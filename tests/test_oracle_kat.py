@@ -431,3 +431,103 @@ def test_oracle_bvh_two_hit_query_equals_brute_force():
     assert hit.sum() > k // 4
     assert np.array_equal(hits[hit, 0], ref[hit, 0])
     assert np.array_equal(second[hit], ref2[hit])
+
+
+# ---- Material_SampleTransform.cs:119-304: albedo by BSDF sampling against uniform-sphere sampling,
+# and the pdf integrating to one, 1M samples each, 99% confidence intervals that must overlap ----
+def _sampling_cases():
+    white = TextureRgb(RgbColor(1, 1, 1))
+    diffuse = lambda: DiffuseMaterial(DiffuseMaterial.Parameters(BaseColor=white, Transmitter=True))
+    rough = lambda: GenericMaterial(GenericMaterial.Parameters(BaseColor=white, Roughness=TextureMono(0.9), IndexOfRefraction=1.1))
+    glossy = lambda: GenericMaterial(GenericMaterial.Parameters(BaseColor=white, Roughness=TextureMono(0.2), Metallic=0.6))
+    glass = lambda: GenericMaterial(GenericMaterial.Parameters(Roughness=TextureMono(0.1), Anisotropic=0.0, IndexOfRefraction=1.45, Metallic=0.0,
+                                                               SpecularTintStrength=0.0, SpecularTransmittance=1.0))
+    return [
+        ("Diffuse_AlbedoShouldMatch", diffuse, (1, 0, 0.1), "albedo"),                              # :119-126
+        ("Diffuse_PDFShouldBeDensity", diffuse, (1, 0, 0.1), "pdf"),                                # :128-135
+        ("GenericRough_AlbedoShouldMatch", rough, (0, 0, 1), "albedo"),                             # :137-145
+        ("GenericRough_PDFShouldBeDensity", rough, (0, 0, 1), "pdf"),                               # :147-155
+        ("GenericGlossy_AlongNormal_AlbedoShouldMatch", glossy, (0, 0, 1), "albedo"),               # :157-165
+        ("GenericGlossy_AlongNormal_PDFShouldBeDensity", glossy, (0, 0, 1), "pdf"),                 # :167-175
+        ("GenericGlossy_AlongNormal_Underneath_AlbedoShouldMatch", glossy, (0, 0, -1), "albedo"),   # :177-185
+        ("GenericGlossy_AlongNormal_Underneath_PDFShouldBeDensity", glossy, (0, 0, -1), "pdf"),     # :187-195
+        ("GenericGlossy_GrazingAngle_AlbedoShouldMatch", glossy, (1, 0, 0.01), "albedo"),           # :197-205
+        ("GenericGlossy_GrazingAngle_PDFShouldBeDensity", glossy, (1, 0, 0.01), "pdf"),             # :207-215
+        ("GenericGlass_AlongNormal_AlbedoShouldMatch", glass, (0, 0, 1), "albedo"),                 # :217-228
+        ("GenericGlass_GrazingAngle_AlbedoShouldMatch", glass, (1, 0, 0.01), "albedo"),             # :230-241
+        ("GenericGlass_GrazingAngle_PDFShouldBeDensity", glass, (1, 0, 0.01), "pdf"),               # :243-254
+        ("GenericGlass_GrazingAngle_Underneath_AlbedoShouldMatch", glass, (1, 0, -1.1), "albedo"),  # :256-267
+        ("GenericGlass_GrazingAngle_Underneath_PDFShouldBeDensity", glass, (1, 0, -1.1), "pdf"),    # :269-280
+    ]
+
+
+SAMPLING_CASES = _sampling_cases()
+# MakeDummyHit (:11-23): the quad at z = -2 hit from the origin straight down; face normal +z and no
+# shading normals, so the shading normal is +z too.
+SAMPLING_HIT = np.array([0, 0, -2, 0, 0, 1, 0, 0, 1, 0.25, 0.25], np.float32)
+
+
+def overlap(a, b):
+    """Material_SampleTransform.cs:94: two intervals overlap."""
+    return b[0] < a[1] and b[1] > a[0]
+
+
+@pytest.mark.parametrize("name,make,out,kind", SAMPLING_CASES, ids=[c[0] for c in SAMPLING_CASES])
+def test_material_sample_transform(name, make, out, kind):
+    o = material_scene(make())
+    od = norm(out)
+    if kind == "albedo":  # IntegrateBSDF :96-117
+        uni = o.material_integrate(0, SAMPLING_HIT, od, 0)
+        imp = o.material_integrate(0, SAMPLING_HIT, od, 1)
+        assert overlap(uni, imp), (uni, imp)
+    else:  # IntegratePdf :71-88
+        ci = o.material_integrate(0, SAMPLING_HIT, od, 2)
+        assert overlap(ci, (1.0, 1.0)), ci
+
+
+@pytest.mark.parametrize("rough,ox,oy,oz", [(0.9, 1, 0, 0.1), (0.1, 1, 0, 0.1), (0.9, 1, 0, 1), (0.1, 1, 0, 1)])
+def test_trowbridge_reitz_pdf_is_a_density(rough, ox, oy, oz):
+    """TrowbridgeReitzDistribution_ShouldBeValidPDF :282-303."""
+    a = max(0.001, np.float32(rough) * np.float32(rough))
+    ci = O.ggx_pdf_integrate(a, a, norm((ox, oy, oz)))
+    assert overlap(ci, (1.0, 1.0)), ci
+
+
+# ---- Mesh_Attributes.cs:9-75: shading-normal interpolation and the CCW face-normal default ----
+def _one_mesh_scene(mesh):
+    sc = Scene()
+    mesh.Material = DiffuseMaterial()
+    sc.Meshes.append(mesh)
+    return O.OracleScene.from_scene(sc, commit=False)
+
+
+def test_mesh_shading_normals_should_be_set():
+    """ShadingNormals_ShouldBeSet :9-47."""
+    V = [[-1, 0, -1], [1, 0, -1], [1, 0, 1], [-1, 0, -1], [1, 0, -1], [-1, 0, 1]]
+    N = [[1, 0, 0]] * 3 + [[1, 0, -1]] * 3
+    o = _one_mesh_scene(Mesh(V, [0, 1, 2, 3, 4, 5], shadingNormals=N))
+    n1, n2 = o.mesh_shading_normal(0, 0, 0.5, 0.5), o.mesh_shading_normal(0, 1, 0.5, 0.5)
+    assert eq(n1[0], 1, 3) and eq(n1[1], 0, 3) and eq(n1[2], 0, 3)
+    assert eq(n2[0], 1 / math.sqrt(2), 3) and eq(n2[1], 0, 3) and eq(n2[2], -1 / math.sqrt(2), 3)
+
+
+def test_mesh_shading_normals_default_to_the_ccw_face_normal():
+    """ShadingNormals_ShouldBeInitialized_CCW :49-74."""
+    o = _one_mesh_scene(Mesh([[-1, 0, -1], [1, 0, -1], [1, 0, 1], [-1, 0, 1]], [0, 1, 2, 0, 2, 3]))
+    for uv in ((0.5, 0.25), (0.25, 0.5)):
+        n = o.mesh_shading_normal(0, 0, *uv)
+        assert eq(n[0], 0, 3) and eq(n[1], -1, 3) and eq(n[2], 0, 3)
+
+
+# ---- Emitter_Diffuse.cs:205-233, Emitter_Glossy.cs:7-34: SampleRay inverted by SampleRayInverse ----
+@pytest.mark.parametrize("glossy", [False, True], ids=["diffuse", "glossy"])
+def test_emitted_rays_sample_inverse(glossy):
+    m = Mesh([[-1, 10, -1], [1, 10, -1], [1, 10, 1], [-1, 10, 1]], [0, 1, 2, 0, 2, 3], shadingNormals=[[0, 1, 0]] * 4)
+    m.Material = DiffuseMaterial()
+    sc = Scene()
+    sc.Meshes.append(m)
+    sc.Emitters.extend(GlossyEmitter.MakeFromMesh(m, RgbColor.White, 50) if glossy else DiffuseEmitter.MakeFromMesh(m, RgbColor.White))
+    o = O.OracleScene.from_scene(sc, commit=False)
+    pos_p, dir_p, _, _, _, _ = o.emitter_ray_roundtrip(0, (0.3, 0.8), (0.56, 0.03))
+    assert eq(pos_p[0], 0.3, 3) and eq(pos_p[1], 0.8, 3)
+    assert eq(dir_p[0], 0.56, 3) and eq(dir_p[1], 0.03, 3)
