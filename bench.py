@@ -541,7 +541,8 @@ def run_ours(args, cfg):
     ws, rank, local = dist_info()
     if ws > 1:
         import torch.distributed as dist
-        dist.init_process_group("nccl", device_id=torch.device("cuda", local)) if False else dist.init_process_group("gloo")
+        # replicas: the only cross-rank traffic is the barrier and the max over ranks of the step time
+        dist.init_process_group("gloo")
     torch.cuda.set_device(local)
     from seesharp_gb300 import PathTracer, _native
 

@@ -14,6 +14,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <mutex>
 
 #include "sst_device.cuh"
 #include "sst_kernels.h"
@@ -178,6 +179,7 @@ struct Trav4 {
     int bestGid;
     int sp;
     uint32_t ref;
+    uint32_t oct;  // sign bits of the inverse direction: which plane of each slab is the near one
     bool done;
 };
 
@@ -187,6 +189,7 @@ SST_D void trav4Begin(Trav4& s, const Bvh4 bvh, float3 org, float3 dir, float tm
     s.pre = rayPre(dir);
     s.inv = mk(1.0f / dir.x, 1.0f / dir.y, 1.0f / dir.z);
     s.oi = mk(-org.x * s.inv.x, -org.y * s.inv.y, -org.z * s.inv.z);
+    s.oct = (s.inv.x < 0.0f ? 1u : 0u) | (s.inv.y < 0.0f ? 2u : 0u) | (s.inv.z < 0.0f ? 4u : 0u);
     s.tmin = tmin;
     s.r = TraceResult{tmax, 0.f, 0.f, -1};
     s.bestGid = 0x7FFFFFFF;
@@ -212,22 +215,26 @@ SST_D bool trav4Run(Trav4& s, int* sstack, int* lstack, int* errFlags, int pause
         const uint32_t ref = s.ref;
         if (!(ref & kLeafFlag)) {
             const float4* nd = sc.nodes4 + 8 * (size_t)ref;
-            float4 lx = __ldg(nd), hx = __ldg(nd + 1), ly = __ldg(nd + 2), hy = __ldg(nd + 3), lz = __ldg(nd + 4), hz = __ldg(nd + 5);
-            float4 rf = __ldg(nd + 6), meta = __ldg(nd + 7);
+            // the near plane of each slab is lo for a positive direction component and hi for a
+            // negative one; its t is then the smaller of the two (fma rounding is monotonic), so
+            // reading the near and far planes directly gives the min / max of both without computing
+            // them.  With an infinite inverse (a zero component) a NaN slab is ignored, which keeps
+            // at least the boxes the min / max form keeps.
+            const int ox = (int)(s.oct & 1u), oy = (int)((s.oct >> 1) & 1u), oz = (int)((s.oct >> 2) & 1u);
+            const float4 nx = __ldg(nd + ox), fx = __ldg(nd + 1 - ox), ny = __ldg(nd + 2 + oy), fy = __ldg(nd + 3 - oy);
+            const float4 nz = __ldg(nd + 4 + oz), fz = __ldg(nd + 5 - oz);
+            const float4 rf = __ldg(nd + 6), meta = __ldg(nd + 7);
             const int cnt = __float_as_int(meta.x);
             const float hitT = s.r.t * 1.0000004f;  // conservative far bound (box/triangle rounding)
             float key[4];
             uint32_t cr[4];
-            const float* LX = &lx.x; const float* HX = &hx.x; const float* LY = &ly.x; const float* HY = &hy.x;
-            const float* LZ = &lz.x; const float* HZ = &hz.x; const float* RF = &rf.x;
+            const float* NX = &nx.x; const float* FX = &fx.x; const float* NY = &ny.x; const float* FY = &fy.x;
+            const float* NZ = &nz.x; const float* FZ = &fz.x; const float* RF = &rf.x;
             int nh = 0;
 #pragma unroll
             for (int k = 0; k < 4; ++k) {
-                float a = fmaf(LX[k], s.inv.x, s.oi.x), b = fmaf(HX[k], s.inv.x, s.oi.x);
-                float c = fmaf(LY[k], s.inv.y, s.oi.y), d = fmaf(HY[k], s.inv.y, s.oi.y);
-                float e = fmaf(LZ[k], s.inv.z, s.oi.z), f = fmaf(HZ[k], s.inv.z, s.oi.z);
-                float tn = fmaxf(fmaxf(fminf(a, b), fminf(c, d)), fmaxf(fminf(e, f), s.tmin));
-                float tf = fminf(fminf(fmaxf(a, b), fmaxf(c, d)), fminf(fmaxf(e, f), hitT));
+                float tn = fmaxf(fmaxf(fmaf(NX[k], s.inv.x, s.oi.x), fmaf(NY[k], s.inv.y, s.oi.y)), fmaxf(fmaf(NZ[k], s.inv.z, s.oi.z), s.tmin));
+                float tf = fminf(fminf(fmaf(FX[k], s.inv.x, s.oi.x), fmaf(FY[k], s.inv.y, s.oi.y)), fminf(fmaf(FZ[k], s.inv.z, s.oi.z), hitT));
                 bool hit = k < cnt && tn <= tf * 1.0000004f;
                 key[k] = hit ? tn : CUDART_INF_F;
                 cr[k] = __float_as_uint(RF[k]);
@@ -431,8 +438,14 @@ template <> struct WideTrav<8> {
 #ifndef SST_TRACE_MIN_THREADS
 #define SST_TRACE_MIN_THREADS 1024
 #endif
+// The 8-wide traversal keeps more per-ray state: at 64 registers it spills; 896 resident threads
+// per SM give it 72.
+#ifndef SST_TRACE8_MIN_THREADS
+#define SST_TRACE8_MIN_THREADS 896
+#endif
 template <int MODE, int BLOCK, int SSTACK, int W>
-__global__ void __launch_bounds__(BLOCK, SST_TRACE_MIN_THREADS > 0 ? SST_TRACE_MIN_THREADS / BLOCK : 1) k_trace(const DevJob* __restrict__ jobs, const uint32_t* __restrict__ rayJob, const float4* ro,
+__global__ void __launch_bounds__(BLOCK, (W == 8 ? SST_TRACE8_MIN_THREADS : SST_TRACE_MIN_THREADS) > 0
+                                             ? (W == 8 ? SST_TRACE8_MIN_THREADS : SST_TRACE_MIN_THREADS) / BLOCK : 1) k_trace(const DevJob* __restrict__ jobs, const uint32_t* __restrict__ rayJob, const float4* ro,
                                                  const float4* rd, const int* count, int* work, float4* hits, const int* tgt, float4* nee,
                                                  int* occl, DevStats* stats, int countRays, int refillIdle) {
     __shared__ int sstack[SSTACK * BLOCK];
@@ -568,11 +581,23 @@ static TraceKernel traceKernel(int mode, int variant) {
 
 bool traceTuningValid(const TraceTuning& t) { return variantOf(t) >= 0 && t.blocksPerSM >= 0 && t.refillIdle >= 1 && t.refillIdle <= 32; }
 
-// Resident blocks per SM of a variant (occupancy), computed once per variant for the device that
-// first asks (the devices of one machine are identical).
+// Resident blocks per SM of a variant (occupancy) and the SM count, per device (the current one
+// at the launch), computed on first use under a lock and kept.
+constexpr int kTraceDevices = 64;
+static std::mutex g_occLock;
+static int g_occ[kTraceDevices][27];
+static int g_sms[kTraceDevices];
+
+static int currentDevice() {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    return dev >= 0 && dev < kTraceDevices ? dev : 0;
+}
+
 static int maxBlocksPerSM(int variant) {
-    static int cache[27] = {};
-    int& c = cache[variant];
+    const int dev = currentDevice();
+    std::lock_guard<std::mutex> lock(g_occLock);
+    int& c = g_occ[dev][variant];
     if (c == 0) {
         int bps = 0;
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, traceKernel(0, variant), kBlocks[(variant % 9) / 3], 0);
@@ -582,10 +607,10 @@ static int maxBlocksPerSM(int variant) {
 }
 
 static int numSMs() {
-    static int sms = 0;
+    const int dev = currentDevice();
+    std::lock_guard<std::mutex> lock(g_occLock);
+    int& sms = g_sms[dev];
     if (sms == 0) {
-        int dev = 0;
-        cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         if (sms <= 0) sms = 1;
     }
