@@ -189,8 +189,8 @@ typedef struct SstTuning {
     int32_t traceRefillIdle;  /* 4- and 8-wide traversal: a warp's finished rays are replaced once this many of its
                                  32 lanes are idle (1..32; 32 = only when all are; the default is 20) */
     int32_t shadeBlocks;      /* resident 128-thread blocks per SM the forward shade kernel with GenericMaterials
-                                 is built for: 8 (64 registers; the default) or 14 (32 registers, more
-                                 warps, more spilling; one shadow ray per technique only) */
+                                 is built for: 8 (64 registers; the default), 10, 12 or 14 (48, 40 or 32
+                                 registers: more warps, more spilling; one shadow ray per technique only) */
     int32_t shadeOrder;       /* 1 (the default): each bounce's paths are shaded surface hits first, misses and
                                  finished paths after them; 0: in queue order */
 } SstTuning;
@@ -200,7 +200,7 @@ int sst_set_tuning(sst_ctx* ctx, const SstTuning* tuning);
 /* Chooses the setting for this scene and these parameters by timing trial renders into a scratch
  * film (the caller's films are not touched), keeping the fastest of two runs per candidate:
  * first the traversal variant (BVH width x block size x shared stack entries), then the refill
- * threshold of the wide traversals, then the shade kernel's build, then the shade order, then
+ * threshold of the wide traversals, then the shade kernel's build (8, 10, 12 or 14 blocks), then the shade order, then
  * the resident blocks per SM, each with trials of at least trialIterations iterations and at least 2^21 paths; then the
  * wave capacity, with trials of about four waves of 2^22 paths (within the parameters' spp).  The
  * choice is applied to the scene's context and returned in `chosen`; bestTrialMs (may be NULL)

@@ -214,7 +214,7 @@ struct sst_ctx {
     // launch configuration (sst_set_tuning / sst_autotune)
     TraceTuning trace;
     int waveCapacity = 0;  // 0: the default
-    int shadeBlocks = 8;   // resident blocks per SM of the forward shade kernel with GenericMaterials: 8 or 14
+    int shadeBlocks = 8;   // resident blocks per SM of the forward shade kernel with GenericMaterials: 8, 10, 12 or 14
     int shadeOrder = 1;    // 1: each bounce's queue is shaded surface hits first (k_partition); 0: in queue order
     // ShadingStats counting (sst_set_shading_stats)
     bool shadingStats = false;

@@ -420,8 +420,7 @@ void launch_partition(const uint32_t* depth, const float4* hits, const int* nIn,
     k_partition<<<grid, 256, 0, s>>>(depth, hits, nIn, order, counts);
 }
 
-int shadeDenseBlocks() { return SST_SHADE_GEN_DENSE_BLOCKS; }
-bool shadeBlocksValid(int b) { return b == SST_SHADE_GEN_MIN_BLOCKS || b == SST_SHADE_GEN_DENSE_BLOCKS; }
+bool shadeBlocksValid(int b) { return b == SST_SHADE_GEN_MIN_BLOCKS || b == 10 || b == 12 || b == SST_SHADE_GEN_DENSE_BLOCKS; }
 
 void launch_shade(int ns, bool adj, bool generic, int shadeBlocks, const DevJob* jobs, const PathBuf& A, const PathBuf& B, const float4* hits,
                   float4* nee, float4* neeG, int cap, float4* shRo, float4* shRd, int* shTgt, uint32_t* shJob, const int* nIn, int* nOut, int* nSh,
@@ -432,9 +431,8 @@ void launch_shade(int ns, bool adj, bool generic, int shadeBlocks, const DevJob*
         k_shade<1, false, false><<<grid, 128, 0, s>>>(jobs, A, B, hits, nee, neeG, cap, shRo, shRd, shTgt, shJob, nIn, nOut, nSh, samples, stats, PyrArgs{});
         return;
     }
-    if (generic && !adj && ns == 1 && shadeBlocks == SST_SHADE_GEN_DENSE_BLOCKS) {
-        k_shade<1, false, true, false, SST_SHADE_GEN_DENSE_BLOCKS><<<grid, 128, 0, s>>>(jobs, A, B, hits, nee, neeG, cap, shRo, shRd, shTgt, shJob, nIn, nOut,
-                                                                                     nSh, samples, stats, PyrArgs{});
+    if (generic && !adj && ns == 1 && shadeBlocks != SST_SHADE_GEN_MIN_BLOCKS) {
+        launch_shade_generic_occ(shadeBlocks, grid, jobs, A, B, hits, nee, cap, shRo, shRd, shTgt, shJob, nIn, nOut, nSh, samples, stats, s);
         return;
     }
 #define SST_SHADE_CASE(N)                                                                                                                    \

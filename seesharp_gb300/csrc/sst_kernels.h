@@ -40,12 +40,15 @@ void launch_trace_shadow(const TraceTuning& t, const DevJob* jobs, const uint32_
 void launch_trace_query(const TraceTuning& t, const DevJob* jobs, const float4* ro, const float4* rd, const int* count, int* work, float4* hits,
                         int* occl, DevStats* stats, bool anyHit, cudaStream_t s);
 // shadeBlocks: the resident blocks per SM of the forward variant with GenericMaterials: the
-// default build (8) or the dense one (shadeDenseBlocks()); one shadow ray per technique has both
-// builds, more shadow rays the default one.
-int shadeDenseBlocks();
+// default build (8, 64 registers) or a denser one (10, 12 or 14: 48, 40 or 32 registers, more warps,
+// more spilling); one shadow ray per technique has every build, more shadow rays the default one.
+// The denser builds live in sst_shade_occ.cu.
 // Writes the shade order of a bounce's queue (surface hits first) into order[0, *nIn).
 void launch_partition(const uint32_t* depth, const float4* hits, const int* nIn, int* order, int* counts, int maxItems, cudaStream_t s);
 bool shadeBlocksValid(int blocks);
+void launch_shade_generic_occ(int blocks, int grid, const DevJob* jobs, const PathBuf& A, const PathBuf& B, const float4* hits, float4* nee, int cap,
+                              float4* shRo, float4* shRd, int* shTgt, uint32_t* shJob, const int* nIn, int* nOut, int* nSh, float* samples,
+                              DevStats* stats, cudaStream_t s);
 void launch_shade(int ns, bool adj, bool generic, int shadeBlocks, const DevJob* jobs, const PathBuf& A, const PathBuf& B, const float4* hits,
                   float4* nee, float4* neeG, int cap, float4* shRo, float4* shRd, int* shTgt, uint32_t* shJob, const int* nIn, int* nOut, int* nSh,
                   float* samples, DevStats* stats, int maxItems, cudaStream_t s);

@@ -436,7 +436,7 @@ static void checkTuning(const SstTuning& t) {
     if (t.traceBlocksPerSM < 0 || t.traceBlocksPerSM > 64) fail(SST_ERR_INVALID_ARGUMENT, "traceBlocksPerSM must be in [0, 64]");
     if (t.shadeOrder != 0 && t.shadeOrder != 1) fail(SST_ERR_INVALID_ARGUMENT, "shadeOrder must be 0 or 1");
     if (!shadeBlocksValid(t.shadeBlocks))
-        fail(SST_ERR_INVALID_ARGUMENT, "shadeBlocks must be 8 or " + std::to_string(shadeDenseBlocks()));
+        fail(SST_ERR_INVALID_ARGUMENT, "shadeBlocks must be 8, 10, 12 or 14");
 }
 
 static SstTuning currentTuning(const sst_ctx* c) {
@@ -630,10 +630,14 @@ int sst_autotune(sst_scene* s, const SstPathTracerParams* p, int32_t trialIterat
                 }
             // occupancy build of the shade kernel with GenericMaterials
             {
-                SstTuning t = best;
-                t.shadeBlocks = best.shadeBlocks == 8 ? shadeDenseBlocks() : 8;
-                double ms = trial(t, kIters);
-                if (ms < bestMs) { bestMs = ms; best = t; }
+                const SstTuning base = best;
+                for (int sb : {8, 10, 12, 14}) {
+                    if (sb == base.shadeBlocks) continue;
+                    SstTuning t = base;
+                    t.shadeBlocks = sb;
+                    double ms = trial(t, kIters);
+                    if (ms < bestMs) { bestMs = ms; best = t; }
+                }
             }
             // shade order: surface hits first, or queue order
             {
