@@ -193,7 +193,7 @@ struct sst_ctx {
     PinnedBuf commitStage;
     DevBuf commitTri[4], commitOrder, commitScratch, commitScratch4, commitScratch8;
     // wavefront buffers
-    DevBuf pathA[9], pathB[9];
+    DevBuf pathA[10], pathB[10];
     DevBuf hits, nee, shRo, shRd, shTgt, shJob, counters, samples, stats, film;
     DevBuf shadeOrderBuf;  // k_partition's shade order of the current queue (cap ints)
     DevBuf jobsBuf, chunksBuf, wavesBuf, curWave;

@@ -12,6 +12,7 @@ static void bindPath(DevBuf* bufs, PathBuf& p, int cap) {
     size_t c = size_t(cap);
     for (int k = 0; k < 4; ++k) bufs[k].ensure(c * 4);
     for (int k = 4; k < 9; ++k) bufs[k].ensure(c * 16);
+    bufs[9].ensure(c * 4);
     p.job = bufs[0].as<uint32_t>();
     p.pix = bufs[1].as<uint32_t>();
     p.rng = bufs[2].as<uint32_t>();
@@ -21,6 +22,7 @@ static void bindPath(DevBuf* bufs, PathBuf& p, int cap) {
     p.prev = bufs[6].as<float4>();
     p.ro = bufs[7].as<float4>();
     p.rd = bufs[8].as<float4>();
+    p.neeFrom = bufs[9].as<uint32_t>();
     p.order = nullptr;
     p.neeIn = p.neeGIn = p.pyrGIn = nullptr;
 }

@@ -107,9 +107,7 @@ __global__ void __launch_bounds__(128, MINB) k_shade(const DevJob* __restrict__ 
     float nTmax = CUDART_INF_F;
     uint32_t pix = 0;
     Rng rng{0};
-    int shIdx[2 * NS];
-    float3 shC[2 * NS];
-    uint32_t pend = 0;
+    uint32_t pend = 0;  // next-event slots queued at this vertex (written at once, at this path's queue index)
     int queries = 0;
     int nEvalPdf = 0, nSample = 0;  // ShadingStats (counted only with cfg.shadingStats)
     // adjoint state
@@ -117,8 +115,6 @@ __global__ void __launch_bounds__(128, MINB) k_shade(const DevJob* __restrict__ 
     int vBaseTgt = -1, vRoughTgt = -1;   // targets of this vertex (for the factor left pending)
     float4 fP[3] = {};                   // d ln f_c / d theta of this vertex's sampled BSDF factor
     bool factorPending = false;
-    float4 shG[ADJ ? 2 * NS : 1][3];
-    float4 shP[PYR ? 2 * NS : 1];        // technique pyramid: queued NEE contribution and MIS weight
     int pyrPixel = 0;
 
     if (valid) {
@@ -140,8 +136,10 @@ __global__ void __launch_bounds__(128, MINB) k_shade(const DevJob* __restrict__ 
             pyrPixel = ck.pixStart + ((int)pix - ck.itemOffset) % ck.pixCount;
         }
         const DevAdj& adj = jobs[job].adj;
-        // resolve the NEE of the previous bounce (PathTracer.cs:363) in slot order
+        // resolve the NEE of the previous bounce (PathTracer.cs:363) in slot order; the previous bounce
+        // wrote them at the path's index in its own queue, which the compaction kept in neeFrom
         uint32_t pm = (dw >> kNeeShift) & 0xFFu;
+        const size_t nf = pm ? (size_t)A.neeFrom[i] : 0;
         if (ADJ) {
             float4 l4 = A.adjL[i], d4 = A.adjD[i];
             adjLt = f3(l4);
@@ -149,7 +147,7 @@ __global__ void __launch_bounds__(128, MINB) k_shade(const DevJob* __restrict__ 
 #pragma unroll
             for (int k = 0; k < 2 * NS; ++k) {
                 if (!(pm & (1u << k))) continue;
-                size_t slot = (size_t)k * cap + i;
+                size_t slot = (size_t)k * cap + nf;
                 float4 nv = A.neeIn[slot];
                 if (nv.w == 0.0f) continue;  // occluded
                 radiance = radiance + f3(nv);
@@ -174,12 +172,12 @@ __global__ void __launch_bounds__(128, MINB) k_shade(const DevJob* __restrict__ 
 #pragma unroll
             for (int k = 0; k < 2 * NS; ++k) {
                 if (!(pm & (1u << k))) continue;
-                const float4 nv = A.neeIn[(size_t)k * cap + i];
+                const float4 nv = A.neeIn[(size_t)k * cap + nf];
                 radiance = radiance + f3(nv);
                 // a visible next-event sample: the reference evaluates the BSDF and its pdf
                 if (cfg.shadingStats && nv.w != 0.0f) ++nEvalPdf;
                 if (PYR && nv.w != 0.0f) {  // visible: the next-event sample of length `depth` counts
-                    const float4 pg = A.pyrGIn[(size_t)k * cap + i];
+                    const float4 pg = A.pyrGIn[(size_t)k * cap + nf];
                     pyrAdd(jobs[job], pyrPixel, (int)(dw & kDepthMask), true, f3(pg), pg.w);
                 }
             }
@@ -316,21 +314,21 @@ __global__ void __launch_bounds__(128, MINB) k_shade(const DevJob* __restrict__ 
                                     val = neeScale * (mis * contrib) / surv;
                                     if (!isBlack(val)) {
                                         use = true;
-                                        int k = 2 * sIt;
+                                        const size_t sl = (size_t)(2 * sIt) * cap + i;
                                         if (ADJ) {
                                             // d val / d(material): prefix * mis * weight / ns / surv * |cos| * df
                                             float3 coef = adjDl * neeScale * (mis * ew / (float)cfg.numShadowRays) / surv * fabsf(c.f.toLocal(ed).z);
                                             Dl3 df = bsdfDeriv(m, baseV, roughV, c, ed);
-                                            shG[k][0] = make_float4(__int_as_float(vBaseTgt), coef.x * df.x.d[0] + coef.y * df.y.d[0] + coef.z * df.z.d[0],
-                                                                    coef.x * df.x.d[1] + coef.y * df.y.d[1] + coef.z * df.z.d[1],
-                                                                    coef.x * df.x.d[2] + coef.y * df.y.d[2] + coef.z * df.z.d[2]);
-                                            shG[k][1] = make_float4(__int_as_float(vRoughTgt), coef.x * df.x.d[3] + coef.y * df.y.d[3] + coef.z * df.z.d[3],
-                                                                    __int_as_float(-1), 0.f);
-                                            shG[k][2] = make_float4(0.f, 0.f, 0.f, 0.f);
+                                            neeG[3 * sl] = make_float4(__int_as_float(vBaseTgt), coef.x * df.x.d[0] + coef.y * df.y.d[0] + coef.z * df.z.d[0],
+                                                                       coef.x * df.x.d[1] + coef.y * df.y.d[1] + coef.z * df.z.d[1],
+                                                                       coef.x * df.x.d[2] + coef.y * df.y.d[2] + coef.z * df.z.d[2]);
+                                            neeG[3 * sl + 1] = make_float4(__int_as_float(vRoughTgt), coef.x * df.x.d[3] + coef.y * df.y.d[3] + coef.z * df.z.d[3],
+                                                                           __int_as_float(-1), 0.f);
+                                            neeG[3 * sl + 2] = make_float4(0.f, 0.f, 0.f, 0.f);
                                         }
                                         if (PYR) {
                                             const float3 pc = contrib * neeScale;
-                                            shP[k] = make_float4(pc.x, pc.y, pc.z, mis);
+                                            pyrA.pyrG[sl] = make_float4(pc.x, pc.y, pc.z, mis);
                                         }
                                     }
                                 }
@@ -338,14 +336,15 @@ __global__ void __launch_bounds__(128, MINB) k_shade(const DevJob* __restrict__ 
                                 // every sample while shading statistics need its visibility (value zero)
                                 if (use || (!ADJ && cfg.shadingStats)) {
                                     const int k = 2 * sIt;
-                                    if (PYR && !use) shP[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+                                    const size_t sl = (size_t)k * cap + i;
+                                    if (PYR && !use) pyrA.pyrG[sl] = make_float4(0.f, 0.f, 0.f, 0.f);
                                     int q = aggAppend(nSh);
                                     shJob[q] = job;
                                     float3 o = offsetPoint(s.pos, s.n, s.eps, ed);
                                     shRo[q] = make_float4(o.x, o.y, o.z, 0.0f);
                                     shRd[q] = make_float4(ed.x, ed.y, ed.z, CUDART_INF_F);
-                                    shIdx[k] = q;
-                                    shC[k] = val;
+                                    shTgt[q] = (int)sl;
+                                    nee[sl] = make_float4(val.x, val.y, val.z, 1.f);
                                     pend |= 1u << k;
                                 }
                             }
@@ -381,21 +380,21 @@ __global__ void __launch_bounds__(128, MINB) k_shade(const DevJob* __restrict__ 
                                     val = neeScale * (mis * contrib) / surv;
                                     if (!isBlack(val)) {
                                         use = true;
-                                        int k = 2 * sIt + 1;
+                                        const size_t sl = (size_t)(2 * sIt + 1) * cap + i;
                                         if (ADJ) {
                                             float3 coef = adjDl * neeScale * (mis * emis / pdf) / surv * fabsf(c.f.toLocal(-l2s).z);
                                             Dl3 df = bsdfDeriv(m, baseV, roughV, c, -l2s);
                                             float3 ge = adjDl * neeScale * (mis * emittedScale(em, lpSn, l2s) / pdf) * bc / surv;
-                                            shG[k][0] = make_float4(__int_as_float(vBaseTgt), coef.x * df.x.d[0] + coef.y * df.y.d[0] + coef.z * df.z.d[0],
-                                                                    coef.x * df.x.d[1] + coef.y * df.y.d[1] + coef.z * df.z.d[1],
-                                                                    coef.x * df.x.d[2] + coef.y * df.y.d[2] + coef.z * df.z.d[2]);
-                                            shG[k][1] = make_float4(__int_as_float(vRoughTgt), coef.x * df.x.d[3] + coef.y * df.y.d[3] + coef.z * df.z.d[3],
-                                                                    __int_as_float(idx), 0.f);
-                                            shG[k][2] = make_float4(ge.x, ge.y, ge.z, 0.f);
+                                            neeG[3 * sl] = make_float4(__int_as_float(vBaseTgt), coef.x * df.x.d[0] + coef.y * df.y.d[0] + coef.z * df.z.d[0],
+                                                                       coef.x * df.x.d[1] + coef.y * df.y.d[1] + coef.z * df.z.d[1],
+                                                                       coef.x * df.x.d[2] + coef.y * df.y.d[2] + coef.z * df.z.d[2]);
+                                            neeG[3 * sl + 1] = make_float4(__int_as_float(vRoughTgt), coef.x * df.x.d[3] + coef.y * df.y.d[3] + coef.z * df.z.d[3],
+                                                                           __int_as_float(idx), 0.f);
+                                            neeG[3 * sl + 2] = make_float4(ge.x, ge.y, ge.z, 0.f);
                                         }
                                         if (PYR) {
                                             const float3 pc = contrib * neeScale;
-                                            shP[k] = make_float4(pc.x, pc.y, pc.z, mis);
+                                            pyrA.pyrG[sl] = make_float4(pc.x, pc.y, pc.z, mis);
                                         }
                                     }
                                 }
@@ -403,7 +402,8 @@ __global__ void __launch_bounds__(128, MINB) k_shade(const DevJob* __restrict__ 
                                 // sample while shading statistics need its visibility (value zero)
                                 if (use || (!ADJ && cfg.shadingStats)) {
                                     const int k = 2 * sIt + 1;
-                                    if (PYR && !use) shP[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+                                    const size_t sl = (size_t)k * cap + i;
+                                    if (PYR && !use) pyrA.pyrG[sl] = make_float4(0.f, 0.f, 0.f, 0.f);
                                     int q = aggAppend(nSh);
                                     shJob[q] = job;
                                     float3 dd = lpPos - s.pos;
@@ -412,8 +412,8 @@ __global__ void __launch_bounds__(128, MINB) k_shade(const DevJob* __restrict__ 
                                     float3 sd = e - o;
                                     shRo[q] = make_float4(o.x, o.y, o.z, 0.0f);
                                     shRd[q] = make_float4(sd.x, sd.y, sd.z, 1.0f - 1e-5f);
-                                    shIdx[k] = q;
-                                    shC[k] = val;
+                                    shTgt[q] = (int)sl;
+                                    nee[sl] = make_float4(val.x, val.y, val.z, 1.f);
                                     pend |= 1u << k;
                                 }
                             }
@@ -493,20 +493,8 @@ __global__ void __launch_bounds__(128, MINB) k_shade(const DevJob* __restrict__ 
         B.adjP[3 * (size_t)j + 1] = fP[1];
         B.adjP[3 * (size_t)j + 2] = fP[2];
     }
-#pragma unroll
-    for (int k = 0; k < 2 * NS; ++k) {
-        if (pend & (1u << k)) {
-            int slot = k * cap + j;
-            shTgt[shIdx[k]] = slot;
-            nee[slot] = make_float4(shC[k].x, shC[k].y, shC[k].z, 1.f);
-            if (PYR) pyrA.pyrG[slot] = shP[k];
-            if (ADJ) {
-                neeG[3 * (size_t)slot] = shG[k][0];
-                neeG[3 * (size_t)slot + 1] = shG[k][1];
-                neeG[3 * (size_t)slot + 2] = shG[k][2];
-            }
-        }
-    }
+    // the next-event slots of this vertex were written at this path's index in the current queue
+    if (pend) B.neeFrom[j] = (uint32_t)i;
 }
 
 }  // namespace sst

@@ -226,6 +226,8 @@ struct PathBuf {
     float4* prev;      // previous hit position
     float4* ro;        // ray origin, tmin
     float4* rd;        // ray direction, tmax
+    uint32_t* neeFrom; // the path's index in the previous queue: its pending next-event slots are at
+                       // slot * cap + neeFrom (read only when the depth word has pending slots)
     // adjoint replay only (NULL otherwise)
     float4* adjL;      // path radiance from the forward pass, w = base-colour target (int bits)
     float4* adjD;      // dLoss/dSample per channel, w = roughness target (int bits)
