@@ -73,7 +73,7 @@ class SstGradients(ctypes.Structure):
 class SstTuning(ctypes.Structure):
     _fields_ = [("waveCapacity", ctypes.c_int32), ("traceBlock", ctypes.c_int32), ("traceStackShared", ctypes.c_int32),
                 ("traceBlocksPerSM", ctypes.c_int32), ("traceBvhWidth", ctypes.c_int32), ("traceRefillIdle", ctypes.c_int32),
-                ("shadeBlocks", ctypes.c_int32), ("shadeOrder", ctypes.c_int32)]
+                ("shadeBlocks", ctypes.c_int32), ("shadeOrder", ctypes.c_int32), ("shadeSplit", ctypes.c_int32)]
 
     def as_dict(self):
         return {k: int(getattr(self, k)) for k, _ in self._fields_}

@@ -18,7 +18,7 @@ CSRC = os.path.join(HERE, "csrc")
 ROOT = os.path.dirname(HERE)
 OUT = os.path.join(HERE, "libsst.so")
 BUILD = os.path.join(HERE, "_build")
-UNITS = ["sst_api.cu", "sst_commit.cu", "sst_render.cu", "sst_adjoint_api.cu", "sst_query.cu", "sst_kernels.cu", "sst_shade_occ.cu", "sst_pyramid.cu",
+UNITS = ["sst_api.cu", "sst_commit.cu", "sst_render.cu", "sst_adjoint_api.cu", "sst_query.cu", "sst_kernels.cu", "sst_shade_occ.cu", "sst_shade_split.cu", "sst_pyramid.cu",
          "sst_trace.cu", "sst_light.cu", "sst_bvh.cu"]
 HEADERS = ["sst_host.h", "sst_types.h", "sst_device.cuh", "sst_adjoint.cuh", "sst_shade.cuh", "sst_kernels.h", "sst_bvh.h", os.path.join("..", "..", "include", "sst.h")]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]

@@ -195,7 +195,8 @@ struct sst_ctx {
     // wavefront buffers
     DevBuf pathA[10], pathB[10];
     DevBuf hits, nee, shRo, shRd, shTgt, shJob, counters, samples, stats, film;
-    DevBuf shadeOrderBuf;  // k_partition's shade order of the current queue (cap ints)
+    DevBuf shadeOrderBuf;
+    DevBuf shadeRec;       // the split shade form's hand-over record (kShadeRec * cap float4)  // k_partition's shade order of the current queue (cap ints)
     DevBuf jobsBuf, chunksBuf, wavesBuf, curWave;
     DevBuf adjA[3], adjB[3], neeG;
     int cap = 0, shCap = 0, neeSlots = 0;
@@ -215,7 +216,8 @@ struct sst_ctx {
     TraceTuning trace;
     int waveCapacity = 0;  // 0: the default
     int shadeBlocks = 8;   // resident blocks per SM of the forward shade kernel with GenericMaterials: 8, 10, 12 or 14
-    int shadeOrder = 1;    // 1: each bounce's queue is shaded surface hits first (k_partition); 0: in queue order
+    int shadeOrder = 1;
+    int shadeSplit = 0;    // 1: the forward shade kernel runs as two kernels per bounce (sst_shade_split.cu)    // 1: each bounce's queue is shaded surface hits first (k_partition); 0: in queue order
     // ShadingStats counting (sst_set_shading_stats)
     bool shadingStats = false;
     // kernel timing (sst_set_profiling)

@@ -23,6 +23,7 @@ static void bindPath(DevBuf* bufs, PathBuf& p, int cap) {
     p.ro = bufs[7].as<float4>();
     p.rd = bufs[8].as<float4>();
     p.neeFrom = bufs[9].as<uint32_t>();
+    p.rec = nullptr;
     p.order = nullptr;
     p.neeIn = p.neeGIn = p.pyrGIn = nullptr;
 }
@@ -178,6 +179,9 @@ void renderJobs(sst_ctx* c, std::vector<JobIn>& jobs, SstRenderStats* out, bool 
     if (pyramid && replay) fail(SST_ERR_UNSUPPORTED, "the technique pyramid is not available in the adjoint replay");
     // technique pyramid: the payload of every NEE slot
     if (pyramid) c->pyrG.ensure(2 * size_t(w.wb.cap) * 16 * 2 * ns);
+    // the split shade form: forward renders with one shadow ray per technique
+    const bool split = c->shadeSplit && !replay && !pyramid && ns == 1;
+    if (split) c->shadeRec.ensure(size_t(kShadeRec) * size_t(w.wb.cap) * 16);
     // job table
     std::vector<DevJob> hj(jobs.size());
     for (size_t k = 0; k < jobs.size(); ++k) {
@@ -234,6 +238,7 @@ void renderJobs(sst_ctx* c, std::vector<JobIn>& jobs, SstRenderStats* out, bool 
             {
                 KTimer kt(c, 2);
                 PathBuf Ao = A;
+                if (split) Ao.rec = c->shadeRec.as<float4>();
                 if (c->shadeOrder) {
                     launch_partition(A.depth, w.wb.hits, cnt + kCntQueue + d, w.wb.order, cnt + kCntPart + 2 * d, maxItems, st);
                     Ao.order = w.wb.order;
@@ -268,7 +273,7 @@ void renderJobs(sst_ctx* c, std::vector<JobIn>& jobs, SstRenderStats* out, bool 
                 launch_trace_shadow(trace, dj, w.wb.shJob, w.wb.shRo, w.wb.shRd, w.wb.shTgt, cnt + kCntShadow + d, cnt + kCntWork + 2 * d + 1, curNee,
                                     dstats, st);
             }
-            launches += c->shadeOrder ? 4 : 3;  // closest hit, shade order, shade, shadow rays
+            launches += (c->shadeOrder ? 4 : 3) + (split ? 1 : 0);  // closest hit, shade order, shade (one or two), shadow rays
             std::swap(A, B);
             if (allowEarlyExit && d >= 6 && d < maxDepth) {
                 // stop early once the queue is empty (long MaxDepth with Russian roulette)
@@ -437,6 +442,7 @@ static void checkTuning(const SstTuning& t) {
         fail(SST_ERR_INVALID_ARGUMENT, "waveCapacity must be 0 or in [1024, 2^24]");
     if (t.traceBlocksPerSM < 0 || t.traceBlocksPerSM > 64) fail(SST_ERR_INVALID_ARGUMENT, "traceBlocksPerSM must be in [0, 64]");
     if (t.shadeOrder != 0 && t.shadeOrder != 1) fail(SST_ERR_INVALID_ARGUMENT, "shadeOrder must be 0 or 1");
+    if (t.shadeSplit != 0 && t.shadeSplit != 1) fail(SST_ERR_INVALID_ARGUMENT, "shadeSplit must be 0 or 1");
     if (!shadeBlocksValid(t.shadeBlocks))
         fail(SST_ERR_INVALID_ARGUMENT, "shadeBlocks must be 8, 10, 12 or 14");
 }
@@ -451,6 +457,7 @@ static SstTuning currentTuning(const sst_ctx* c) {
     t.traceRefillIdle = c->trace.refillIdle;
     t.shadeBlocks = c->shadeBlocks;
     t.shadeOrder = c->shadeOrder;
+    t.shadeSplit = c->shadeSplit;
     return t;
 }
 
@@ -563,6 +570,7 @@ int sst_set_tuning(sst_ctx* c, const SstTuning* t) {
         c->waveCapacity = t->waveCapacity;
         c->shadeBlocks = t->shadeBlocks;
         c->shadeOrder = t->shadeOrder;
+        c->shadeSplit = t->shadeSplit;
     });
 }
 
@@ -587,6 +595,7 @@ int sst_autotune(sst_scene* s, const SstPathTracerParams* p, int32_t trialIterat
             c->waveCapacity = t.waveCapacity;
             c->shadeBlocks = t.shadeBlocks;
             c->shadeOrder = t.shadeOrder;
+            c->shadeSplit = t.shadeSplit;
             double best = 1e300;
             for (int r = 0; r < 2; ++r) {
                 std::vector<JobIn> jobs(1);
@@ -648,6 +657,13 @@ int sst_autotune(sst_scene* s, const SstPathTracerParams* p, int32_t trialIterat
                 double ms = trial(t, kIters);
                 if (ms < bestMs) { bestMs = ms; best = t; }
             }
+            // shade form: one fused kernel, or the split pair
+            {
+                SstTuning t = best;
+                t.shadeSplit = 1 - best.shadeSplit;
+                double ms = trial(t, kIters);
+                if (ms < bestMs) { bestMs = ms; best = t; }
+            }
             // resident traversal blocks per SM
             int m = traceMaxBlocksPerSM(toTrace(best));
             for (int bps : {m / 2, (3 * m) / 4}) {
@@ -681,6 +697,7 @@ int sst_autotune(sst_scene* s, const SstPathTracerParams* p, int32_t trialIterat
             c->waveCapacity = start.waveCapacity;
             c->shadeBlocks = start.shadeBlocks;
             c->shadeOrder = start.shadeOrder;
+            c->shadeSplit = start.shadeSplit;
             c->profiling = prof;
             throw;
         }
@@ -689,6 +706,7 @@ int sst_autotune(sst_scene* s, const SstPathTracerParams* p, int32_t trialIterat
         c->waveCapacity = best.waveCapacity;
         c->shadeBlocks = best.shadeBlocks;
         c->shadeOrder = best.shadeOrder;
+        c->shadeSplit = best.shadeSplit;
         if (chosen) *chosen = best;
         if (bestTrialMs) *bestTrialMs = bestMs;
     });

@@ -86,8 +86,12 @@ SST_D int aggAppend(int* counter) {
 // the kernel's instruction footprint small).
 // PYR = true: the technique pyramids (PathTracer.RenderTechniquePyramid) are filled as well.
 // MINB: the resident blocks per SM the variant is compiled for.
+// SPLIT = true (forward only): the first of two kernels.  It stops before BSDF sampling and leaves
+// the shading point and the path's updated state in A.rec (kShadeRec float4 per queued path, see
+// k_shade_sample); k_shade_sample then samples the direction and compacts the queue.  Each half holds
+// less state and less code than the fused kernel.
 template <int NS, bool ADJ, bool GEN, bool PYR = false,
-          int MINB = (ADJ ? SST_SHADE_ADJ_MIN_BLOCKS : (GEN ? SST_SHADE_GEN_MIN_BLOCKS : SST_SHADE_MIN_BLOCKS))>
+          int MINB = (ADJ ? SST_SHADE_ADJ_MIN_BLOCKS : (GEN ? SST_SHADE_GEN_MIN_BLOCKS : SST_SHADE_MIN_BLOCKS)), bool SPLIT = false>
 __global__ void __launch_bounds__(128, MINB) k_shade(const DevJob* __restrict__ jobs, PathBuf A, PathBuf B,
                                                                    const float4* __restrict__ hits, float4* nee, float4* neeG, int cap,
                                                                    float4* shRo, float4* shRd, int* shTgt, uint32_t* shJob, const int* nIn,
@@ -110,6 +114,7 @@ __global__ void __launch_bounds__(128, MINB) k_shade(const DevJob* __restrict__ 
     uint32_t pend = 0;  // next-event slots queued at this vertex (written at once, at this path's queue index)
     int queries = 0;
     int nEvalPdf = 0, nSample = 0;  // ShadingStats (counted only with cfg.shadingStats)
+    bool sampled = false;           // SPLIT: the path goes on to k_shade_sample
     // adjoint state
     float3 adjLt = mk(0, 0, 0), adjDl = mk(0, 0, 0);
     int vBaseTgt = -1, vRoughTgt = -1;   // targets of this vertex (for the factor left pending)
@@ -419,6 +424,16 @@ __global__ void __launch_bounds__(128, MINB) k_shade(const DevJob* __restrict__ 
                             }
                         }
                     }
+                    if constexpr (SPLIT) {
+                        // hand the shading point and the path's state to k_shade_sample
+                        const size_t cp = (size_t)cap;
+                        A.rec[i] = make_float4(s.pos.x, s.pos.y, s.pos.z, s.eps);
+                        A.rec[cp + i] = make_float4(s.n.x, s.n.y, s.n.z, __int_as_float(s.mat));
+                        A.rec[2 * cp + i] = make_float4(s.sn.x, s.sn.y, s.sn.z, s.uv.x);
+                        A.rec[3 * cp + i] = make_float4(s.uv.y, surv, __uint_as_float(rng.s), __uint_as_float(kRecSample | pend));
+                        A.rec[4 * cp + i] = make_float4(radiance.x, radiance.y, radiance.z, 0.f);
+                        sampled = true;
+                    } else {
                     // SampleDirection (PathTracer.cs:526-530)
                     float uc = rng.nextFloat();
                     float u1 = rng.nextFloat(), u2 = rng.nextFloat();
@@ -452,11 +467,15 @@ __global__ void __launch_bounds__(128, MINB) k_shade(const DevJob* __restrict__ 
                         nRd = dirW;
                     }
                     outDepth |= pend << kNeeShift;
+                    }  // !SPLIT
                 }
             }
         }
         if (terminate && !ADJ) splat(samples, pix, radiance);
         if (!cont) pend = 0;
+        // the first kernel of the split form: a path that does not go on to sampling is finished
+        // here (terminated, or a finished path whose queued next-event samples were resolved)
+        if (SPLIT && !sampled) A.rec[3 * (size_t)cap + i] = make_float4(0.f, 0.f, 0.f, 0.f);
     }
     // shadow-query statistics (RayTracerStats.NumShadowRays semantics)
     int totq = __reduce_add_sync(0xffffffffu, queries);
@@ -466,6 +485,7 @@ __global__ void __launch_bounds__(128, MINB) k_shade(const DevJob* __restrict__ 
         if ((threadIdx.x & 31) == 0 && te) atomicAdd(&stats->matEvalPdf, (unsigned long long)te);
         if ((threadIdx.x & 31) == 0 && ts) atomicAdd(&stats->matSample, (unsigned long long)ts);
     }
+    if constexpr (SPLIT) return;  // k_shade_sample compacts the queue
 
     // K7: warp ballot / popc compaction into the next queue
     unsigned m = __ballot_sync(0xffffffffu, cont);
@@ -494,6 +514,112 @@ __global__ void __launch_bounds__(128, MINB) k_shade(const DevJob* __restrict__ 
         B.adjP[3 * (size_t)j + 2] = fP[2];
     }
     // the next-event slots of this vertex were written at this path's index in the current queue
+    if (pend) B.neeFrom[j] = (uint32_t)i;
+}
+
+
+// The second kernel of the split form (forward only): SampleDirection (PathTracer.cs:526-530) for the
+// paths that k_shade<..., SPLIT = true> left in A.rec with kRecSample, then the queue compaction of
+// the fused kernel.  The shading context, the GenericMaterial parameters and the RNG state are
+// rebuilt from the record by the same arithmetic as in the fused kernel, so the path goes on
+// exactly as there.
+template <bool GEN, int MINB>
+__global__ void __launch_bounds__(128, MINB) k_shade_sample(const DevJob* __restrict__ jobs, PathBuf A, PathBuf B, int cap, const int* nIn,
+                                                           int* nOut, float* samples, DevStats* stats) {
+    const int n = *nIn;
+    if ((int)(blockIdx.x * blockDim.x) >= n) return;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const bool valid = t < n;
+    const int i = (valid && A.order) ? A.order[t] : t;
+    bool cont = false;
+    uint32_t job = 0, pix = 0, outDepth = 0;
+    float3 prefix = mk(1, 1, 1), radiance = mk(0, 0, 0), hitPos = mk(0, 0, 0), nRo = mk(0, 0, 0), nRd = mk(0, 0, 0);
+    float prevPdfOut = 0.f;
+    Rng rng{0};
+    uint32_t pend = 0;
+    int nEvalPdf = 0, nSample = 0;
+    if (valid) {
+        const size_t cp = (size_t)cap;
+        const float4 r3 = A.rec[3 * cp + i];
+        const uint32_t fl = __float_as_uint(r3.w);
+        if (fl & kRecSample) {
+            job = A.job[i];
+            pix = A.pix[i];
+            const DevScene& sc = jobs[job].sc;
+            const PTConfig& cfg = jobs[job].cfg;
+            const uint32_t depth = A.depth[i] & kDepthMask;
+            prefix = f3(A.pw[i]);
+            const float3 rdir = f3(A.rd[i]);
+            const float4 r0 = A.rec[i], r1 = A.rec[cp + i], r2 = A.rec[2 * cp + i], r4 = A.rec[4 * cp + i];
+            Surf s;
+            s.pos = f3(r0);
+            s.eps = r0.w;
+            s.n = f3(r1);
+            s.mat = __float_as_int(r1.w);
+            s.sn = f3(r2);
+            s.uv = make_float2(r2.w, r3.x);
+            const float surv = r3.y;
+            rng.s = __float_as_uint(r3.z);
+            pend = fl & 0xFFu;
+            radiance = f3(r4);
+            hitPos = s.pos;
+            Ctx c;
+            c.f.n = s.sn;
+            basis(c.f.n, c.f.t, c.f.b);
+            c.outW = -rdir;
+            c.out = c.f.toLocal(c.outW);
+            c.faceN = s.n;
+            c.uv = s.uv;
+            const DevMaterial& m = sc.mats[s.mat];
+            Lp lp = {};
+            float3 diffBase = mk(0, 0, 0);
+            if (GEN && m.type == kGeneric) lp = localParams(sc, m, s.uv);
+            else diffBase = lookupRgb(sc, m.baseTex, m.base, s.uv);
+            // SampleDirection (PathTracer.cs:526-530)
+            float uc = rng.nextFloat();
+            float u1 = rng.nextFloat(), u2 = rng.nextFloat();
+            float3 dirW; float bpdf = 0.f; float3 bw = mk(0, 0, 0);
+            bool ok = sampleMaterial<GEN>(sc, m, lp, diffBase, c, uc, u1, u2, dirW, bpdf, bw);
+            if (cfg.shadingStats) {
+                ++nSample;
+                if (!(GEN && m.type == kGeneric)) ++nEvalPdf;
+            }
+            if (!ok || bpdf == 0.0f || isBlack(bw)) {
+                if (pend) { cont = true; outDepth = kDoneFlag; }
+                else splat(samples, pix, radiance);
+            } else {
+                cont = true;
+                prefix = prefix * (bw / surv);  // PathTracer.cs:372-378
+                prevPdfOut = bpdf * surv;
+                outDepth = depth + 1;
+                nRo = offsetPoint(s.pos, s.n, s.eps, dirW);
+                nRd = dirW;
+            }
+            outDepth |= pend << kNeeShift;
+        }
+        if (!cont) pend = 0;
+    }
+    const int te = __reduce_add_sync(0xffffffffu, nEvalPdf), ts = __reduce_add_sync(0xffffffffu, nSample);
+    if ((threadIdx.x & 31) == 0 && te) atomicAdd(&stats->matEvalPdf, (unsigned long long)te);
+    if ((threadIdx.x & 31) == 0 && ts) atomicAdd(&stats->matSample, (unsigned long long)ts);
+    // warp ballot / popc compaction into the next queue
+    unsigned msk = __ballot_sync(0xffffffffu, cont);
+    if (msk == 0) return;
+    const int lane = threadIdx.x & 31;
+    int base = 0;
+    if (lane == 0) base = atomicAdd(nOut, __popc(msk));
+    base = __shfl_sync(0xffffffffu, base, 0);
+    if (!cont) return;
+    const int j = base + __popc(msk & ((1u << lane) - 1u));
+    B.job[j] = job;
+    B.pix[j] = pix;
+    B.rng[j] = rng.s;
+    B.depth[j] = outDepth;
+    B.pw[j] = make_float4(prefix.x, prefix.y, prefix.z, prevPdfOut);
+    B.rad[j] = make_float4(radiance.x, radiance.y, radiance.z, 0.f);
+    B.prev[j] = make_float4(hitPos.x, hitPos.y, hitPos.z, 0.f);
+    B.ro[j] = make_float4(nRo.x, nRo.y, nRo.z, 0.f);
+    B.rd[j] = make_float4(nRd.x, nRd.y, nRd.z, (outDepth & kDoneFlag) ? -1.0f : CUDART_INF_F);
     if (pend) B.neeFrom[j] = (uint32_t)i;
 }
 

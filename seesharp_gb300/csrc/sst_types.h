@@ -228,6 +228,8 @@ struct PathBuf {
     float4* rd;        // ray direction, tmax
     uint32_t* neeFrom; // the path's index in the previous queue: its pending next-event slots are at
                        // slot * cap + neeFrom (read only when the depth word has pending slots)
+    float4* rec;       // split shade form only: per queued path, what the first kernel hands the second
+                       // (kShadeRec float4 planes of the queue's capacity); NULL otherwise
     // adjoint replay only (NULL otherwise)
     float4* adjL;      // path radiance from the forward pass, w = base-colour target (int bits)
     float4* adjD;      // dLoss/dSample per channel, w = roughness target (int bits)
@@ -244,6 +246,8 @@ struct PathBuf {
 };
 
 constexpr uint32_t kDepthMask = 0xFFFFu;
+constexpr int kShadeRec = 5;                  // float4 planes of PathBuf.rec (the split shade form)
+constexpr uint32_t kRecSample = 0x80000000u;  // PathBuf.rec flag: the path goes on to BSDF sampling
 constexpr int kNeeShift = 16;
 constexpr uint32_t kDoneFlag = 0x80000000u;
 constexpr uint32_t kAdjFactorFlag = 0x40000000u;  // adjoint: a BSDF-factor gradient is pending

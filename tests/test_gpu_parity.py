@@ -551,12 +551,13 @@ def test_tuning_and_autotune_leave_images_and_queries_unchanged():
         hits0, occ0 = sc.native.trace(rays), sc.native.occluded(rays)
         assert st0.numKernelLaunches > 0
         for t in [dict(traceBlock=64, traceStackShared=16, traceBlocksPerSM=1, waveCapacity=4096, traceBvhWidth=2, traceRefillIdle=20, shadeBlocks=14, shadeOrder=0),
-                  dict(traceBlock=256, traceStackShared=32, traceBlocksPerSM=0, waveCapacity=0, traceBvhWidth=4, traceRefillIdle=32, shadeBlocks=8, shadeOrder=1),
+                  dict(traceBlock=256, traceStackShared=32, traceBlocksPerSM=0, waveCapacity=0, traceBvhWidth=4, traceRefillIdle=32, shadeBlocks=8, shadeOrder=1, shadeSplit=1),
                   dict(traceBlock=64, traceStackShared=16, traceBlocksPerSM=3, waveCapacity=8192, traceBvhWidth=4, traceRefillIdle=1, shadeBlocks=10, shadeOrder=1),
                   dict(traceBlock=128, traceStackShared=24, traceBlocksPerSM=2, waveCapacity=1 << 20, traceBvhWidth=4, traceRefillIdle=12, shadeBlocks=8, shadeOrder=0),
                   dict(traceBlock=128, traceStackShared=24, traceBlocksPerSM=2, waveCapacity=1 << 20, traceBvhWidth=2, traceRefillIdle=8, shadeBlocks=12, shadeOrder=1),
-                  dict(traceBlock=256, traceStackShared=16, traceBlocksPerSM=0, waveCapacity=0, traceBvhWidth=8, traceRefillIdle=20, shadeBlocks=8, shadeOrder=1),
+                  dict(traceBlock=256, traceStackShared=16, traceBlocksPerSM=0, waveCapacity=0, traceBvhWidth=8, traceRefillIdle=20, shadeBlocks=14, shadeOrder=1, shadeSplit=1),
                   dict(traceBlock=64, traceStackShared=32, traceBlocksPerSM=3, waveCapacity=8192, traceBvhWidth=8, traceRefillIdle=32, shadeBlocks=14, shadeOrder=0)]:
+            t.setdefault("shadeSplit", 0)
             _native.set_tuning(ctx, **t)
             assert _native.get_tuning(ctx) == t
             img, _ = render_gpu(sc, 4, 6)
@@ -571,7 +572,7 @@ def test_tuning_and_autotune_leave_images_and_queries_unchanged():
         img, _ = render_gpu(sc, 4, 6)
         assert np.array_equal(img, ref)
         for bad in (dict(traceBlock=96), dict(traceStackShared=20), dict(waveCapacity=100), dict(traceBlocksPerSM=-1), dict(traceBvhWidth=6),
-                    dict(traceRefillIdle=0), dict(traceRefillIdle=33), dict(shadeBlocks=9),
+                    dict(traceRefillIdle=0), dict(traceRefillIdle=33), dict(shadeBlocks=9), dict(shadeSplit=2),
                     dict(shadeOrder=2)):
             with pytest.raises(_native.SstError):
                 _native.set_tuning(ctx, **bad)
