@@ -177,8 +177,13 @@ int sst_trace(sst_scene* scene, const SstRay* rays, int32_t n, SstHit* hits, int
 int sst_occluded(sst_scene* scene, const SstRay* rays, int32_t n, int32_t* occluded, int32_t memory);
 
 /* ---- launch configuration and autotuner (no counterpart in the reference) ---------------------
- * The wavefront's queue capacity and the traversal kernels' launch shape.  None of them changes
- * a result: films and query results are bitwise the same under every valid setting. */
+ * The wavefront's queue capacity, the traversal kernels' launch shape and the shade kernel's build.
+ * None of them changes a result: films and query results are bitwise the same under every valid
+ * setting, except shadeSplit, whose two kernels compile the shading arithmetic separately from the
+ * fused kernel (and, with shadeSplit = 1, shadeBlocks 14 against the other values, which select a
+ * separately compiled build of the split kernels), so the compiler may fuse a multiply-add
+ * differently and move a path's estimate by an ulp (or, rarely, flip a decision that the ulp
+ * decides). */
 typedef struct SstTuning {
     int32_t waveCapacity;     /* paths in flight per wave; 0 = the default (2^21) */
     int32_t traceBlock;       /* threads per traversal block: 64, 128 (the default) or 256 */
@@ -193,9 +198,10 @@ typedef struct SstTuning {
                                  registers: more warps, more spilling; one shadow ray per technique only) */
     int32_t shadeOrder;       /* 1 (the default): each bounce's paths are shaded surface hits first, misses and
                                  finished paths after them; 0: in queue order */
-    int32_t shadeSplit;       /* 1: forward renders with one shadow ray per technique shade each bounce with two
-                                 kernels (hit, emitter MIS, Russian roulette and next-event estimation; then
-                                 BSDF sampling and the queue compaction); 0 (the default): one fused kernel */
+    int32_t shadeSplit;       /* 1: forward renders with GenericMaterials and one shadow ray per technique shade each
+                                 bounce with two kernels (hit, emitter MIS, Russian roulette and next-event
+                                 estimation; then BSDF sampling and the queue compaction), built for 8 blocks, or
+                                 for 14 when shadeBlocks is 14; 0 (the default): one fused kernel */
 } SstTuning;
 int sst_get_tuning(sst_ctx* ctx, SstTuning* out);
 /* Invalid values return SST_ERR_INVALID_ARGUMENT and leave the setting unchanged. */

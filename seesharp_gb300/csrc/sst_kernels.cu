@@ -427,8 +427,8 @@ void launch_shade(int ns, bool adj, bool generic, int shadeBlocks, const DevJob*
                   float* samples, DevStats* stats, int maxItems, cudaStream_t s) {
     int grid = (maxItems + 127) / 128;
     if (grid == 0) return;
-    if (!adj && ns == 1 && A.rec) {
-        launch_shade_split(generic, shadeBlocks, grid, jobs, A, B, hits, nee, cap, shRo, shRd, shTgt, shJob, nIn, nOut, nSh, samples, stats, s);
+    if (generic && !adj && ns == 1 && A.rec) {
+        launch_shade_split(shadeBlocks, grid, jobs, A, B, hits, nee, cap, shRo, shRd, shTgt, shJob, nIn, nOut, nSh, samples, stats, s);
         return;
     }
     if (!generic && !adj && ns == 1) {

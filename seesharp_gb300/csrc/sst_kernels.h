@@ -46,10 +46,10 @@ void launch_trace_query(const TraceTuning& t, const DevJob* jobs, const float4* 
 // Writes the shade order of a bounce's queue (surface hits first) into order[0, *nIn).
 void launch_partition(const uint32_t* depth, const float4* hits, const int* nIn, int* order, int* counts, int maxItems, cudaStream_t s);
 bool shadeBlocksValid(int blocks);
-// The split form (sst_shade_split.cu), forward, one shadow ray per technique: two kernels per bounce,
-// A.rec must hold kShadeRec * cap float4.  blocks: 14 selects the dense build of both kernels, any
-// other value the 8-block one.
-void launch_shade_split(bool generic, int blocks, int grid, const DevJob* jobs, const PathBuf& A, const PathBuf& B, const float4* hits, float4* nee,
+// The split form (sst_shade_split.cu), forward, GenericMaterials, one shadow ray per technique: two
+// kernels per bounce, A.rec must hold kShadeRec * cap float4.  blocks: 14 selects the dense build of
+// both kernels, any other value the 8-block one.
+void launch_shade_split(int blocks, int grid, const DevJob* jobs, const PathBuf& A, const PathBuf& B, const float4* hits, float4* nee,
                         int cap, float4* shRo, float4* shRd, int* shTgt, uint32_t* shJob, const int* nIn, int* nOut, int* nSh, float* samples,
                         DevStats* stats, cudaStream_t s);
 void launch_shade_generic_occ(int blocks, int grid, const DevJob* jobs, const PathBuf& A, const PathBuf& B, const float4* hits, float4* nee, int cap,

@@ -180,7 +180,7 @@ void renderJobs(sst_ctx* c, std::vector<JobIn>& jobs, SstRenderStats* out, bool 
     // technique pyramid: the payload of every NEE slot
     if (pyramid) c->pyrG.ensure(2 * size_t(w.wb.cap) * 16 * 2 * ns);
     // the split shade form: forward renders with one shadow ray per technique
-    const bool split = c->shadeSplit && !replay && !pyramid && ns == 1;
+    const bool split = c->shadeSplit && generic && !replay && !pyramid && ns == 1;
     if (split) c->shadeRec.ensure(size_t(kShadeRec) * size_t(w.wb.cap) * 16);
     // job table
     std::vector<DevJob> hj(jobs.size());
@@ -639,16 +639,23 @@ int sst_autotune(sst_scene* s, const SstPathTracerParams* p, int32_t trialIterat
                     double ms = trial(t, kIters);
                     if (ms < bestMs) { bestMs = ms; best = t; }
                 }
-            // occupancy build of the shade kernel with GenericMaterials
-            {
+            // the shade kernel with GenericMaterials: fused, built for 8, 10, 12 or 14 blocks, or split
+            // into two kernels, built for 8 or 14 (the split form's register budget changes which build
+            // wins, so the two choices are tried together); a scene without one runs neither
+            bool generic = false;
+            for (auto& m : s->materials) generic |= m.type == kGeneric;
+            if (generic) {
                 const SstTuning base = best;
-                for (int sb : {8, 10, 12, 14}) {
-                    if (sb == base.shadeBlocks) continue;
-                    SstTuning t = base;
-                    t.shadeBlocks = sb;
-                    double ms = trial(t, kIters);
-                    if (ms < bestMs) { bestMs = ms; best = t; }
-                }
+                for (int split : {0, 1})
+                    for (int sb : {8, 10, 12, 14}) {
+                        if (split && (sb == 10 || sb == 12)) continue;
+                        if (sb == base.shadeBlocks && split == base.shadeSplit) continue;
+                        SstTuning t = base;
+                        t.shadeBlocks = sb;
+                        t.shadeSplit = split;
+                        double ms = trial(t, kIters);
+                        if (ms < bestMs) { bestMs = ms; best = t; }
+                    }
             }
             // shade order: surface hits first, or queue order
             {
@@ -657,13 +664,7 @@ int sst_autotune(sst_scene* s, const SstPathTracerParams* p, int32_t trialIterat
                 double ms = trial(t, kIters);
                 if (ms < bestMs) { bestMs = ms; best = t; }
             }
-            // shade form: one fused kernel, or the split pair
-            {
-                SstTuning t = best;
-                t.shadeSplit = 1 - best.shadeSplit;
-                double ms = trial(t, kIters);
-                if (ms < bestMs) { bestMs = ms; best = t; }
-            }
+
             // resident traversal blocks per SM
             int m = traceMaxBlocksPerSM(toTrace(best));
             for (int bps : {m / 2, (3 * m) / 4}) {

@@ -1,6 +1,7 @@
 // The split form of the forward shade kernel: k_shade<..., SPLIT = true> (hit, emitter MIS, Russian
 // roulette, next-event estimation) followed by k_shade_sample (BSDF sampling and the queue
-// compaction), for one shadow ray per technique.  Each half keeps less state live and holds less
+// compaction), for GenericMaterials and one shadow ray per technique (with DiffuseMaterials only the
+// fused kernel, which then needs no material dispatch, is faster).  Each half keeps less state live and holds less
 // code than the fused kernel; the launch tuning (SstTuning.shadeSplit) picks the form.  A
 // translation unit of its own, so that these instances compile in parallel with the others.
 #include <cuda_runtime.h>
@@ -10,14 +11,10 @@
 
 namespace sst {
 
-void launch_shade_split(bool generic, int blocks, int grid, const DevJob* jobs, const PathBuf& A, const PathBuf& B, const float4* hits, float4* nee,
+void launch_shade_split(int blocks, int grid, const DevJob* jobs, const PathBuf& A, const PathBuf& B, const float4* hits, float4* nee,
                         int cap, float4* shRo, float4* shRd, int* shTgt, uint32_t* shJob, const int* nIn, int* nOut, int* nSh, float* samples,
                         DevStats* stats, cudaStream_t s) {
-    if (!generic) {
-        k_shade<1, false, false, false, SST_SHADE_MIN_BLOCKS, true><<<grid, 128, 0, s>>>(jobs, A, B, hits, nee, nullptr, cap, shRo, shRd, shTgt,
-                                                                                        shJob, nIn, nOut, nSh, samples, stats, PyrArgs{});
-        k_shade_sample<false, SST_SHADE_MIN_BLOCKS><<<grid, 128, 0, s>>>(jobs, A, B, cap, nIn, nOut, samples, stats);
-    } else if (blocks == SST_SHADE_GEN_DENSE_BLOCKS) {
+    if (blocks == SST_SHADE_GEN_DENSE_BLOCKS) {
         k_shade<1, false, true, false, SST_SHADE_GEN_DENSE_BLOCKS, true><<<grid, 128, 0, s>>>(jobs, A, B, hits, nee, nullptr, cap, shRo, shRd, shTgt,
                                                                                              shJob, nIn, nOut, nSh, samples, stats, PyrArgs{});
         k_shade_sample<true, SST_SHADE_GEN_DENSE_BLOCKS><<<grid, 128, 0, s>>>(jobs, A, B, cap, nIn, nOut, samples, stats);

@@ -515,6 +515,50 @@ def test_shade_builds_agree_on_diffuse_scenes():
     assert per_path_agreement(gen, lean, 1e-5, 1e-7) >= 0.995
 
 
+def test_split_shade_agrees_with_the_fused_kernel():
+    """The split shade form (SstTuning.shadeSplit = 1: hit, emitter MIS, Russian roulette and
+    next-event estimation in one kernel, BSDF sampling and the queue compaction in a second) computes
+    what the fused kernel computes, from the same random numbers, in separately compiled code: at
+    1 spp every pixel is one path, and paths agree to a relative 1e-5 except where nvcc's multiply-add
+    contraction moves an ulp that flips a discrete decision.  The split form's 8- and 14-block builds
+    are compiled separately from each other as well (ptxas may contract a multiply and an add under
+    one register budget and not under the other) and agree the same way; under one build the film is
+    bitwise the same for every launch shape (wave capacity, traversal variant, shade order).  A scene
+    with DiffuseMaterials only is not affected by the setting at all."""
+    ctx = _native.default_context()
+    base = _native.get_tuning(ctx)
+    sc = workloads.sphere_field(40, 192, 160, level=3)
+    sc.Prepare()
+    try:
+        _native.set_tuning(ctx, **dict(base, shadeSplit=0))
+        fused, stf = render_gpu(sc, 1, 8)
+        _native.set_tuning(ctx, **dict(base, shadeSplit=1, shadeBlocks=8))
+        split, sts = render_gpu(sc, 1, 8)
+        assert sts.numKernelLaunches > stf.numKernelLaunches
+        assert per_path_agreement(split, fused, 1e-5, 1e-7) >= 0.995
+        assert abs(int(sts.numRays) - int(stf.numRays)) <= 1e-3 * int(stf.numRays)
+        for t in (dict(shadeBlocks=8, waveCapacity=4096, traceBvhWidth=2, shadeOrder=1 - base["shadeOrder"]),
+                  dict(shadeBlocks=10, traceBvhWidth=8, traceBlock=64)):
+            _native.set_tuning(ctx, **dict(base, shadeSplit=1, **t))
+            img, _ = render_gpu(sc, 1, 8)
+            assert np.array_equal(img, split), t
+        _native.set_tuning(ctx, **dict(base, shadeSplit=1, shadeBlocks=14))
+        dense, _ = render_gpu(sc, 1, 8)
+        assert per_path_agreement(dense, split, 1e-5, 1e-7) >= 0.995
+        _native.set_tuning(ctx, **dict(base, shadeSplit=1, shadeBlocks=14, waveCapacity=8192, traceBvhWidth=2))
+        img, _ = render_gpu(sc, 1, 8)
+        assert np.array_equal(img, dense)
+        cb = workloads.cornell_box(64, 64)
+        cb.Prepare()
+        _native.set_tuning(ctx, **dict(base, shadeSplit=0))
+        a, _ = render_gpu(cb, 2, 5)
+        _native.set_tuning(ctx, **dict(base, shadeSplit=1))
+        b, _ = render_gpu(cb, 2, 5)
+        assert np.array_equal(a, b)
+    finally:
+        _native.set_tuning(ctx, **base)
+
+
 def test_graph_replay_equals_plain_launches():
     import os
     sc = workloads.cornell_box(64, 64)
@@ -534,7 +578,8 @@ def test_tuning_and_autotune_leave_images_and_queries_unchanged():
     """Wave capacity, traversal block size, shared stack entries, resident traversal blocks, the
     refill threshold of the 4-wide traversal, the shade kernel's occupancy build and the shade order
     change the launch shape and the order in which rays and paths are processed only: the film and
-    the query results stay bitwise the same."""
+    the query results stay bitwise the same.  (The split shade form is compiled separately and has
+    its own test; the autotuner's choice is compared with a film of the same form.)"""
     from seesharp_gb300 import autotune
     sc = workloads.sphere_field(12, 96, 80, level=3)
     sc.Prepare()
@@ -551,11 +596,11 @@ def test_tuning_and_autotune_leave_images_and_queries_unchanged():
         hits0, occ0 = sc.native.trace(rays), sc.native.occluded(rays)
         assert st0.numKernelLaunches > 0
         for t in [dict(traceBlock=64, traceStackShared=16, traceBlocksPerSM=1, waveCapacity=4096, traceBvhWidth=2, traceRefillIdle=20, shadeBlocks=14, shadeOrder=0),
-                  dict(traceBlock=256, traceStackShared=32, traceBlocksPerSM=0, waveCapacity=0, traceBvhWidth=4, traceRefillIdle=32, shadeBlocks=8, shadeOrder=1, shadeSplit=1),
+                  dict(traceBlock=256, traceStackShared=32, traceBlocksPerSM=0, waveCapacity=0, traceBvhWidth=4, traceRefillIdle=32, shadeBlocks=8, shadeOrder=1),
                   dict(traceBlock=64, traceStackShared=16, traceBlocksPerSM=3, waveCapacity=8192, traceBvhWidth=4, traceRefillIdle=1, shadeBlocks=10, shadeOrder=1),
                   dict(traceBlock=128, traceStackShared=24, traceBlocksPerSM=2, waveCapacity=1 << 20, traceBvhWidth=4, traceRefillIdle=12, shadeBlocks=8, shadeOrder=0),
                   dict(traceBlock=128, traceStackShared=24, traceBlocksPerSM=2, waveCapacity=1 << 20, traceBvhWidth=2, traceRefillIdle=8, shadeBlocks=12, shadeOrder=1),
-                  dict(traceBlock=256, traceStackShared=16, traceBlocksPerSM=0, waveCapacity=0, traceBvhWidth=8, traceRefillIdle=20, shadeBlocks=14, shadeOrder=1, shadeSplit=1),
+                  dict(traceBlock=256, traceStackShared=16, traceBlocksPerSM=0, waveCapacity=0, traceBvhWidth=8, traceRefillIdle=20, shadeBlocks=14, shadeOrder=1),
                   dict(traceBlock=64, traceStackShared=32, traceBlocksPerSM=3, waveCapacity=8192, traceBvhWidth=8, traceRefillIdle=32, shadeBlocks=14, shadeOrder=0)]:
             t.setdefault("shadeSplit", 0)
             _native.set_tuning(ctx, **t)
@@ -570,7 +615,14 @@ def test_tuning_and_autotune_leave_images_and_queries_unchanged():
         chosen, ms = autotune(sc, PathTracer(TotalSpp=4, MaxDepth=6))
         assert chosen == _native.get_tuning(ctx) and ms > 0
         img, _ = render_gpu(sc, 4, 6)
-        assert np.array_equal(img, ref)
+        if chosen["shadeSplit"]:
+            # the same film as the chosen split build renders under the default launch shape
+            _native.set_tuning(ctx, **dict(base, shadeSplit=1, shadeBlocks=chosen["shadeBlocks"]))
+            ref_split, _ = render_gpu(sc, 4, 6)
+            _native.set_tuning(ctx, **chosen)
+            assert np.array_equal(img, ref_split)
+        else:
+            assert np.array_equal(img, ref)
         for bad in (dict(traceBlock=96), dict(traceStackShared=20), dict(waveCapacity=100), dict(traceBlocksPerSM=-1), dict(traceBvhWidth=6),
                     dict(traceRefillIdle=0), dict(traceRefillIdle=33), dict(shadeBlocks=9), dict(shadeSplit=2),
                     dict(shadeOrder=2)):
