@@ -190,7 +190,9 @@ typedef struct SstTuning {
     int32_t traceStackShared; /* traversal stack entries per thread kept in shared memory: 16, 24 (the default) or 32 */
     int32_t traceBlocksPerSM; /* resident traversal blocks per SM; 0 = as many as fit */
     int32_t traceBvhWidth;    /* BVH traversed: 2 (binary), 4 (4-wide, same leaves; the default) or 8 (8-wide, same leaves,
-                                 children in octant slots) */
+                                 children in octant slots; built for a scene by the first render or query that
+                                 traverses it with this setting, and until then sst_occluded_noalloc, which
+                                 allocates nothing, traverses the scene 4-wide) */
     int32_t traceRefillIdle;  /* 4- and 8-wide traversal: a warp's finished rays are replaced once this many of its
                                  32 lanes are idle (1..32; 32 = only when all are; the default is 20) */
     int32_t shadeBlocks;      /* resident 128-thread blocks per SM the forward shade kernel with GenericMaterials

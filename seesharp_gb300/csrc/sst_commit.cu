@@ -381,18 +381,10 @@ void commitScene(sst_scene* s, int W, int H) {
         int rc = buildBvh4(s->nodes.as<float4>(), s->nNodes, s->nodes4.as<float4>(), scratch4.p, &s->nNodes4, &s->bvh4Depth, st);
         if (rc != 0) fail(SST_ERR_CUDA, "4-wide BVH build failed (" + std::to_string(rc) + "): " + cudaGetErrorString(cudaGetLastError()));
     }
-    // 8-wide BVH over the same leaves, children in octant slots.  Its traversal stack packs a node
-    // index into 24 bits; a scene with more 8-wide nodes is traversed 4-wide instead.
+    // the 8-wide BVH is built on first use (ensureBvh8)
     s->nNodes8 = 0;
     s->bvh8Depth = 0;
-    if (s->nNodes > 0) {
-        DevBuf& scratch8 = s->ctx->commitScratch8;
-        s->nodes8.ensure(sizeof(float4) * 15 * size_t(s->nNodes));
-        scratch8.ensure(bvh8ScratchBytes(s->nNodes));
-        int rc = buildBvh8(s->nodes.as<float4>(), s->nNodes, s->nodes8.as<float4>(), scratch8.p, &s->nNodes8, &s->bvh8Depth, st);
-        if (rc != 0) fail(SST_ERR_CUDA, "8-wide BVH build failed (" + std::to_string(rc) + "): " + cudaGetErrorString(cudaGetLastError()));
-        if (s->nNodes8 >= (1 << 24)) s->nNodes8 = 0;
-    }
+    s->bvh8Built = false;
     std::vector<float> vnrm, vuv;
     if (anyNormals) {
         vnrm.assign(3 * size_t(nv), 0.f);
@@ -521,3 +513,22 @@ void commitScene(sst_scene* s, int W, int H) {
     s->committed = true;
 }
 
+// 8-wide BVH over the committed scene's leaves, children in octant slots, built when a traversal
+// first asks for it (the launch tuning's traceBvhWidth = 8): the default 4-wide traversal never
+// pays its build time or its memory.  Its traversal stack packs a node index into 24 bits; a scene
+// with more 8-wide nodes is traversed 4-wide instead.
+void ensureBvh8(sst_scene* s) {
+    if (s->bvh8Built || !s->committed || s->nNodes == 0) return;
+    cudaStream_t st = s->ctx->stream;
+    DevBuf& scratch8 = s->ctx->commitScratch8;
+    s->nodes8.ensure(sizeof(float4) * 15 * size_t(s->nNodes));
+    scratch8.ensure(bvh8ScratchBytes(s->nNodes));
+    int n8 = 0, depth8 = 0;
+    int rc = buildBvh8(s->nodes.as<float4>(), s->nNodes, s->nodes8.as<float4>(), scratch8.p, &n8, &depth8, st);
+    if (rc != 0) fail(SST_ERR_CUDA, "8-wide BVH build failed (" + std::to_string(rc) + "): " + cudaGetErrorString(cudaGetLastError()));
+    s->bvh8Built = true;
+    s->nNodes8 = n8 >= (1 << 24) ? 0 : n8;
+    s->bvh8Depth = depth8;
+    s->dev.nodes8 = s->nNodes8 > 0 ? s->nodes8.as<float4>() : nullptr;
+    s->dev.nNodes8 = s->nNodes8;
+}

@@ -295,6 +295,7 @@ struct sst_scene {
     DevBuf nodes, nodes4, nodes8, triv, triN, triAux, triVtx, vnrm, vuv, mats, texs, texData, ems, envImg, envRowCdf, envColCdf, envHasCol, envRowMarg, queryJob;
     DevScene dev{};
     int nTri = 0, nNodes = 0, bvhDepth = 0, nNodes4 = 0, bvh4Depth = 0, nNodes8 = 0, bvh8Depth = 0;
+    bool bvh8Built = false;  // the 8-wide BVH of the committed geometry exists (ensureBvh8)
     // adjoint: per-path radiance of the last sst_forward and its settings
     DevBuf record, gTex, gMatBase, gMatRough, gEmitter, dLdI;
     bool recordValid = false;
@@ -353,13 +354,22 @@ void batchFilmsOut(sst_ctx* ctx, const SstRenderJob* jobs, int numJobs, const st
 SstRenderStats emptyStats();
 // sst_query.cu
 const DevJob* jobTable(sst_scene* s);
-// The context's traversal setting for rays of these scenes: the 8-wide BVH is not built for a
-// scene whose node indices do not fit its stack entries, which then traverses 4-wide.
+// sst_commit.cu: builds the scene's 8-wide BVH if it has not been built since the last commit.
+void ensureBvh8(sst_scene* s);
+// The context's traversal setting for rays of these scenes: a scene without an 8-wide BVH (not
+// built yet, or with node indices that do not fit its stack entries) traverses 4-wide.
 inline TraceTuning traceFor(const sst_ctx* c, const sst_scene* const* scenes, size_t n) {
     TraceTuning t = c->trace;
     if (t.width == 8)
         for (size_t k = 0; k < n; ++k)
             if (scenes[k]->nNodes > 0 && scenes[k]->nNodes8 == 0) t.width = 4;
     return t;
+}
+// The same, building the 8-wide BVHs first when the setting asks for them.  Call it before the
+// scenes' DevScene records are copied into a job table.
+inline TraceTuning traceForBuilding(sst_ctx* c, sst_scene* const* scenes, size_t n) {
+    if (c->trace.width == 8)
+        for (size_t k = 0; k < n; ++k) ensureBvh8(scenes[k]);
+    return traceFor(c, scenes, n);
 }
 

@@ -44,14 +44,15 @@ static void runQuery(sst_scene* s, const SstRay* rays, int n, SstHit* hits, int3
             c->qOut.ensure(size_t(n) * 4);
             dOcc = c->qOut.as<int>();
         }
-        launch_trace_query(traceFor(c, &s, 1), jobTable(s), c->qRo.as<float4>(), c->qRd.as<float4>(), cnt, cnt + 1, nullptr, dOcc, c->stats.as<DevStats>(), true,
-                           st);
+        const TraceTuning tt = traceForBuilding(c, &s, 1);
+        launch_trace_query(tt, jobTable(s), c->qRo.as<float4>(), c->qRd.as<float4>(), cnt, cnt + 1, nullptr, dOcc, c->stats.as<DevStats>(), true, st);
         CUDA_CHECK(cudaGetLastError());
         if (memory != SST_MEM_DEVICE) CUDA_CHECK(cudaMemcpyAsync(occl, dOcc, size_t(n) * 4, out, st));
     } else {
         c->qHits.ensure(size_t(n) * 16);
-        launch_trace_query(traceFor(c, &s, 1), jobTable(s), c->qRo.as<float4>(), c->qRd.as<float4>(), cnt, cnt + 1, c->qHits.as<float4>(), nullptr,
-                           c->stats.as<DevStats>(), false, st);
+        const TraceTuning tt = traceForBuilding(c, &s, 1);
+        launch_trace_query(tt, jobTable(s), c->qRo.as<float4>(), c->qRd.as<float4>(), cnt, cnt + 1, c->qHits.as<float4>(), nullptr, c->stats.as<DevStats>(),
+                           false, st);
         SstHitDev* dHits = reinterpret_cast<SstHitDev*>(hits);
         if (memory != SST_MEM_DEVICE) {
             c->qOut.ensure(size_t(n) * sizeof(SstHitDev));
@@ -129,6 +130,7 @@ int sst_trace_light_paths(sst_scene* s, uint32_t seed, uint32_t iteration, int32
         CUDA_CHECK(cudaMemsetAsync(cnt, 0, sizeof(int) * 2 * (size_t(maxDepth) + 3), st));
         c->stats.ensure(sizeof(DevStats));
         CUDA_CHECK(cudaMemsetAsync(c->stats.p, 0, sizeof(DevStats), st));
+        const TraceTuning tt = traceForBuilding(c, &s, 1);
         const DevJob* job = jobTable(s);
         LightParams P{numPaths, maxDepth, seed, iteration};
         CUDA_CHECK(cudaEventRecord(c->ev0, st));
@@ -142,7 +144,7 @@ int sst_trace_light_paths(sst_scene* s, uint32_t seed, uint32_t iteration, int32
             int* qIn = cnt + d;
             int* qOut = cnt + d + 1;
             int* work = cnt + (maxDepth + 2) + d;
-            launch_trace_closest(traceFor(c, &s, 1), job, nullptr, A.ro, A.rd, qIn, work, c->lightHits.as<float4>(), c->stats.as<DevStats>(), st);
+            launch_trace_closest(tt, job, nullptr, A.ro, A.rd, qIn, work, c->lightHits.as<float4>(), c->stats.as<DevStats>(), st);
             launch_light_walk(job, P, A, B, c->lightHits.as<float4>(), qIn, qOut, dv, dl, items, st);
             CUDA_CHECK(cudaGetLastError());
             std::swap(A, B);

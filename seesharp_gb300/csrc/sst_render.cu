@@ -159,9 +159,9 @@ void renderJobs(sst_ctx* c, std::vector<JobIn>& jobs, SstRenderStats* out, bool 
         w.wb.b.adjL = c->adjB[0].as<float4>(); w.wb.b.adjD = c->adjB[1].as<float4>(); w.wb.b.adjP = c->adjB[2].as<float4>();
         w.wb.neeG = c->neeG.as<float4>();
     }
-    std::vector<const sst_scene*> jobScenes;
+    std::vector<sst_scene*> jobScenes;
     for (auto& j : jobs) jobScenes.push_back(j.s);
-    const TraceTuning trace = traceFor(c, jobScenes.data(), jobScenes.size());
+    const TraceTuning trace = traceForBuilding(c, jobScenes.data(), jobScenes.size());
     // any GenericMaterial in the wave's scenes (otherwise the shade kernel without generic code runs)
     bool generic = false;
     for (auto& j : jobs)

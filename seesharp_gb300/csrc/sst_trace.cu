@@ -158,6 +158,52 @@ struct Bvh4 {
 };
 SST_D Bvh4 bvh4Of(const DevScene& sc) { return Bvh4{sc.nodes4, sc.triv, sc.nNodes4}; }
 
+// Paired single precision (sm_100 and later): fma.rn.f32x2 rounds each half exactly as fmaf does,
+// so the slab planes of two children cost one instruction instead of two.
+SST_D float2 fma2(float2 a, float2 b, float2 c) {
+    float2 d;
+    asm("{\n\t.reg .b64 pa, pb, pc, pd;\n\t"
+        "mov.b64 pa, {%2, %3};\n\tmov.b64 pb, {%4, %5};\n\tmov.b64 pc, {%6, %7};\n\t"
+        "fma.rn.f32x2 pd, pa, pb, pc;\n\tmov.b64 {%0, %1}, pd;\n\t}"
+        : "=f"(d.x), "=f"(d.y)
+        : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y), "f"(c.x), "f"(c.y));
+    return d;
+}
+// Three-operand minimum and maximum (sm_100 and later): like two fminf / fmaxf, a NaN operand is
+// ignored and the result is exact.
+SST_D float min3f(float a, float b, float c) {
+    float d;
+    asm("min.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+    return d;
+}
+SST_D float max3f(float a, float b, float c) {
+    float d;
+    asm("max.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+    return d;
+}
+// Entry and exit distances of four child boxes from their near- and far-plane rows (x, y, z each a
+// float4 over the children): paired fused multiply-adds per plane row, then the three-operand
+// max / min with the ray's interval.  Bitwise the scalar fmaf / fmaxf / fminf form.
+SST_D void slab4(float4 nx, float4 fx, float4 ny, float4 fy, float4 nz, float4 fz, float3 inv, float3 oi, float tmin, float tmax,
+                 float tn[4], float tf[4]) {
+    const float2 ix = make_float2(inv.x, inv.x), iy = make_float2(inv.y, inv.y), iz = make_float2(inv.z, inv.z);
+    const float2 ox = make_float2(oi.x, oi.x), oy = make_float2(oi.y, oi.y), oz = make_float2(oi.z, oi.z);
+    const float2 nx0 = fma2(make_float2(nx.x, nx.y), ix, ox), nx1 = fma2(make_float2(nx.z, nx.w), ix, ox);
+    const float2 ny0 = fma2(make_float2(ny.x, ny.y), iy, oy), ny1 = fma2(make_float2(ny.z, ny.w), iy, oy);
+    const float2 nz0 = fma2(make_float2(nz.x, nz.y), iz, oz), nz1 = fma2(make_float2(nz.z, nz.w), iz, oz);
+    const float2 fx0 = fma2(make_float2(fx.x, fx.y), ix, ox), fx1 = fma2(make_float2(fx.z, fx.w), ix, ox);
+    const float2 fy0 = fma2(make_float2(fy.x, fy.y), iy, oy), fy1 = fma2(make_float2(fy.z, fy.w), iy, oy);
+    const float2 fz0 = fma2(make_float2(fz.x, fz.y), iz, oz), fz1 = fma2(make_float2(fz.z, fz.w), iz, oz);
+    tn[0] = max3f(nx0.x, ny0.x, fmaxf(nz0.x, tmin));
+    tn[1] = max3f(nx0.y, ny0.y, fmaxf(nz0.y, tmin));
+    tn[2] = max3f(nx1.x, ny1.x, fmaxf(nz1.x, tmin));
+    tn[3] = max3f(nx1.y, ny1.y, fmaxf(nz1.y, tmin));
+    tf[0] = min3f(fx0.x, fy0.x, fminf(fz0.x, tmax));
+    tf[1] = min3f(fx0.y, fy0.y, fminf(fz0.y, tmax));
+    tf[2] = min3f(fx1.x, fy1.x, fminf(fz1.x, tmax));
+    tf[3] = min3f(fx1.y, fy1.y, fminf(fz1.y, tmax));
+}
+
 SST_D void cswap(float& ka, uint32_t& ra, float& kb, uint32_t& rb) {
     bool s = kb < ka;
     float k = s ? kb : ka;
@@ -228,15 +274,14 @@ SST_D bool trav4Run(Trav4& s, int* sstack, int* lstack, int* errFlags, int pause
             const float hitT = s.r.t * 1.0000004f;  // conservative far bound (box/triangle rounding)
             float key[4];
             uint32_t cr[4];
-            const float* NX = &nx.x; const float* FX = &fx.x; const float* NY = &ny.x; const float* FY = &fy.x;
-            const float* NZ = &nz.x; const float* FZ = &fz.x; const float* RF = &rf.x;
+            const float* RF = &rf.x;
+            float tn[4], tf[4];
+            slab4(nx, fx, ny, fy, nz, fz, s.inv, s.oi, s.tmin, hitT, tn, tf);
             int nh = 0;
 #pragma unroll
             for (int k = 0; k < 4; ++k) {
-                float tn = fmaxf(fmaxf(fmaf(NX[k], s.inv.x, s.oi.x), fmaf(NY[k], s.inv.y, s.oi.y)), fmaxf(fmaf(NZ[k], s.inv.z, s.oi.z), s.tmin));
-                float tf = fminf(fminf(fmaf(FX[k], s.inv.x, s.oi.x), fmaf(FY[k], s.inv.y, s.oi.y)), fminf(fmaf(FZ[k], s.inv.z, s.oi.z), hitT));
-                bool hit = k < cnt && tn <= tf * 1.0000004f;
-                key[k] = hit ? tn : CUDART_INF_F;
+                bool hit = k < cnt && tn[k] <= tf[k] * 1.0000004f;
+                key[k] = hit ? tn[k] : CUDART_INF_F;
                 cr[k] = __float_as_uint(RF[k]);
                 nh += hit ? 1 : 0;
             }
@@ -328,15 +373,10 @@ SST_D uint32_t visit8(const Trav8& s, uint32_t node) {
         const float4 nx = __ldg(nd + 2 * ox + h), fx = __ldg(nd + 2 - 2 * ox + h);
         const float4 ny = __ldg(nd + 4 + 2 * oy + h), fy = __ldg(nd + 6 - 2 * oy + h);
         const float4 nz = __ldg(nd + 8 + 2 * oz + h), fz = __ldg(nd + 10 - 2 * oz + h);
-        const float NX[4] = {nx.x, nx.y, nx.z, nx.w}, FX[4] = {fx.x, fx.y, fx.z, fx.w};
-        const float NY[4] = {ny.x, ny.y, ny.z, ny.w}, FY[4] = {fy.x, fy.y, fy.z, fy.w};
-        const float NZ[4] = {nz.x, nz.y, nz.z, nz.w}, FZ[4] = {fz.x, fz.y, fz.z, fz.w};
+        float tn[4], tf[4];
+        slab4(nx, fx, ny, fy, nz, fz, s.inv, s.oi, s.tmin, hitT, tn, tf);
 #pragma unroll
-        for (int k = 0; k < 4; ++k) {
-            const float tn = fmaxf(fmaxf(fmaf(NX[k], s.inv.x, s.oi.x), fmaf(NY[k], s.inv.y, s.oi.y)), fmaxf(fmaf(NZ[k], s.inv.z, s.oi.z), s.tmin));
-            const float tf = fminf(fminf(fmaf(FX[k], s.inv.x, s.oi.x), fmaf(FY[k], s.inv.y, s.oi.y)), fminf(fmaf(FZ[k], s.inv.z, s.oi.z), hitT));
-            hm |= (tn <= tf * 1.0000004f) ? (1u << (4 * h + k)) : 0u;
-        }
+        for (int k = 0; k < 4; ++k) hm |= (tn[k] <= tf[k] * 1.0000004f) ? (1u << (4 * h + k)) : 0u;
     }
     hm &= valid;
     // slot k -> bit k ^ oct
