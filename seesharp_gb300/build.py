@@ -24,6 +24,14 @@ HEADERS = ["sst_host.h", "sst_types.h", "sst_device.cuh", "sst_adjoint.cuh", "ss
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2", "--expt-relaxed-constexpr",
          "-diag-suppress", "177"]
+# The units holding the shading kernels (camera, shade, light paths, film fold) divide and take
+# square roots with the approximate single-precision forms (errors of a few ulp) instead of the
+# correctly rounded ones, whose slow-path subroutine calls cost the shade kernel a third of its
+# time.  Traversal and the BVH build keep the correctly rounded forms (the intersection criterion
+# is exact primitive ids); the RNG's float conversion and the environment-map tables use the
+# correctly rounded intrinsics explicitly (bit-exact streams, tables equal to a CPU build).
+SHADING_UNITS = {"sst_kernels.cu", "sst_shade_occ.cu", "sst_shade_split.cu", "sst_pyramid.cu", "sst_light.cu"}
+SHADING_FLAGS = ["-prec-div=false", "-prec-sqrt=false"]
 
 
 def nvcc():
@@ -49,7 +57,8 @@ def build(force=False, verbose=False):
 
     def compile_unit(u):
         obj = os.path.join(BUILD, u.replace(".cu", ".o"))
-        cmd = [cc] + ARCH + FLAGS + ["-I", os.path.join(ROOT, "include"), "-c", os.path.join(CSRC, u), "-o", obj]
+        extra = SHADING_FLAGS if u in SHADING_UNITS else []
+        cmd = [cc] + ARCH + FLAGS + extra + ["-I", os.path.join(ROOT, "include"), "-c", os.path.join(CSRC, u), "-o", obj]
         if verbose:
             print(" ".join(cmd), flush=True)
         subprocess.run(cmd, check=True)

@@ -35,7 +35,13 @@ SST_HD float3 operator/(float3 a, float s) { return mk(a.x / s, a.y / s, a.z / s
 SST_HD float dot(float3 a, float3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
 SST_HD float3 cross(float3 a, float3 b) { return mk(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x); }
 SST_D float len(float3 a) { return sqrtf(dot(a, a)); }
-SST_D float3 normalize(float3 a) { return a / len(a); }  // Vector3.Normalize: NaN for zero input
+// Vector3.Normalize (NaN for a zero input), correctly rounded even where the unit divides and takes
+// square roots with the approximate forms: a sharp microfacet lobe turns an ulp of a half vector or
+// of a sampled direction into a relative 1e-3 of its density.
+SST_D float3 normalize(float3 a) {
+    const float l = __fsqrt_rn(dot(a, a));
+    return mk(__fdiv_rn(a.x, l), __fdiv_rn(a.y, l), __fdiv_rn(a.z, l));
+}
 SST_HD float3 f3(float4 v) { return mk(v.x, v.y, v.z); }
 SST_HD bool isZero(float3 a) { return a.x == 0.f && a.y == 0.f && a.z == 0.f; }
 SST_HD bool isBlack(float3 a) { return a.x == 0.f && a.y == 0.f && a.z == 0.f; }

@@ -153,6 +153,8 @@ __device__ __forceinline__ void logNan(DevStats* st, int iteration, int pixel) {
     }
 }
 
+SST_D float3 divRn(float3 a, float b) { return mk(__fdiv_rn(a.x, b), __fdiv_rn(a.y, b), __fdiv_rn(a.z, b)); }
+
 __global__ void k_film_fold(const DevJob* __restrict__ jobs, const WaveChunk* __restrict__ chunks, const WaveDesc* waves, int* curWave,
                             const float* samples, DevStats* st, int advance) {
     const WaveDesc wd = waves[*curWave];
@@ -197,34 +199,36 @@ __global__ void k_film_fold(const DevJob* __restrict__ jobs, const WaveChunk* __
                 float* r = rec + 3 * ((size_t)iter * cfg.W * cfg.H + pix);
                 r[0] = v.x; r[1] = v.y; r[2] = v.z;
             }
-            float kf = (float)(iter + 1);
-            if (iter > 0) cur = cur * ((kf - 1.0f) / kf);
-            float a = avg3(v);
+            // the frame buffer's float arithmetic, correctly rounded whatever the unit's division flags
+            const float kf = (float)(iter + 1);
+            const float keep = __fdiv_rn(kf - 1.0f, kf);
+            if (iter > 0) cur = cur * keep;
+            float a = __fdiv_rn(v.x + v.y + v.z, 3.0f);  // RgbColor.Average
             bool finite = isfinite(a);
             if (!finite) logNan(st, (int)iter + 1, (int)pix);
             bool used = finite || !cfg.ignoreNan;
-            if (used) cur = cur + v / kf;
+            if (used) cur = cur + divRn(v, kf);
             if (finite && nOut > 0) outlierNotify(hw, hit, hcnt, nOut, a, (int)iter);
             if (lay.aovAlbedo) {
                 // RgbLayer running means (Images/Layer.cs:33-37, RgbLayer.cs:17-18)
                 const float* a6 = lay.aovSamples + 6 * ((size_t)ck.itemOffset + (size_t)m * ck.pixCount + p);
                 if (iter > 0) {
-                    alb = alb * ((kf - 1.0f) / kf);
-                    nrm = nrm * ((kf - 1.0f) / kf);
+                    alb = alb * keep;
+                    nrm = nrm * keep;
                 }
-                alb = alb + mk(a6[0], a6[1], a6[2]) / kf;
-                nrm = nrm + mk(a6[3], a6[4], a6[5]) / kf;
+                alb = alb + divRn(mk(a6[0], a6[1], a6[2]), kf);
+                nrm = nrm + divRn(mk(a6[3], a6[4], a6[5]), kf);
             }
             if (lay.varMean) {
                 // VarianceLayer (Images/VarianceLayer.cs:41-65): both images are running means of the
                 // iteration's splatted value (the sample's channel average, 0 if it was skipped)
                 float val = used ? a : 0.0f;
                 if (iter > 0) {
-                    vMoment = vMoment * ((kf - 1.0f) / kf);
-                    vMean = vMean * ((kf - 1.0f) / kf);
+                    vMoment = vMoment * keep;
+                    vMean = vMean * keep;
                 }
-                vMoment = vMoment + val * val / kf;
-                vMean = vMean + val / kf;
+                vMoment = vMoment + __fdiv_rn(val * val, kf);
+                vMean = vMean + __fdiv_rn(val, kf);
             }
             if (lay.ref) {
                 // FrameBuffer error metrics after iteration iter + 1 (FrameBuffer.cs:276-277, 378-383)
