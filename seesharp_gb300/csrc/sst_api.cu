@@ -38,6 +38,9 @@ int sst_create(int32_t device, sst_ctx** out) {
         CUDA_CHECK(cudaDeviceGetAttribute(&c->numSMs, cudaDevAttrMultiProcessorCount, device));
         CUDA_CHECK(cudaEventCreate(&c->ev0));
         CUDA_CHECK(cudaEventCreate(&c->ev1));
+        CUDA_CHECK(cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking));
+        CUDA_CHECK(cudaEventCreateWithFlags(&c->evShade, cudaEventDisableTiming));
+        CUDA_CHECK(cudaEventCreateWithFlags(&c->evShadow, cudaEventDisableTiming));
         CUDA_CHECK(cudaMallocHost(&c->pinnedCount, sizeof(int) * 4));
         *out = c.release();
     });
@@ -48,9 +51,13 @@ int sst_destroy(sst_ctx* ctx) {
         if (!ctx) return;
         cudaSetDevice(ctx->device);
         cudaStreamSynchronize(ctx->stream);
+        if (ctx->side) cudaStreamSynchronize(ctx->side);
         if (ctx->pinnedCount) cudaFreeHost(ctx->pinnedCount);
         if (ctx->ev0) cudaEventDestroy(ctx->ev0);
         if (ctx->ev1) cudaEventDestroy(ctx->ev1);
+        if (ctx->evShade) cudaEventDestroy(ctx->evShade);
+        if (ctx->evShadow) cudaEventDestroy(ctx->evShadow);
+        if (ctx->side) cudaStreamDestroy(ctx->side);
         cudaStreamDestroy(ctx->stream);
         delete ctx;
     });

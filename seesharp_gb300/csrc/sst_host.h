@@ -195,8 +195,8 @@ struct sst_ctx {
     // wavefront buffers
     DevBuf pathA[10], pathB[10];
     DevBuf hits, nee, shRo, shRd, shTgt, shJob, counters, samples, stats, film;
-    DevBuf shadeOrderBuf;
-    DevBuf shadeRec;       // the split shade form's hand-over record (kShadeRec * cap float4)  // k_partition's shade order of the current queue (cap ints)
+    DevBuf shadeOrderBuf;  // k_partition's shade order of the current queue (cap ints)
+    DevBuf shadeRec;       // the split shade form's hand-over record (kShadeRec * cap float4)
     DevBuf jobsBuf, chunksBuf, wavesBuf, curWave;
     DevBuf adjA[3], adjB[3], neeG;
     int cap = 0, shCap = 0, neeSlots = 0;
@@ -204,6 +204,10 @@ struct sst_ctx {
     // ray queries (sst_trace, sst_occluded): split rays, queue counters, traversal records, results
     DevBuf qRo, qRd, qCnt, qHits, qOut;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    // the wavefront's second stream: a bounce's shadow rays are traced on it beside the next bounce's
+    // closest hits (evShade: the bounce's shade is done; evShadow: its shadow rays are)
+    cudaStream_t side = nullptr;
+    cudaEvent_t evShade = nullptr, evShadow = nullptr;
     int* pinnedCount = nullptr;
     // light paths (sst_trace_light_paths)
     DevBuf lightA[9], lightB[9], lightHits, lightVerts, lightLengths, lightCnt;

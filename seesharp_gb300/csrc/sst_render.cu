@@ -218,7 +218,12 @@ void renderJobs(sst_ctx* c, std::vector<JobIn>& jobs, SstRenderStats* out, bool 
     int maxFold = 0;
     for (auto& wd : waves) maxFold = std::max(maxFold, wd.foldThreads);
 
-    // One wave: camera, then per bounce closest hit / shade / shadow rays, then the film fold.
+    // One wave: camera, then per bounce closest hit / shade / shadow rays, then the film fold.  A
+    // bounce's shadow rays only clear the next-event slots that the next bounce's shade reads, so
+    // they are traced on the side stream beside the next bounce's closest hits and shade order
+    // (each persistent traversal kernel's tail is filled by the other's blocks), and the next shade
+    // waits for them.  Kernel timing (profiling) keeps every launch on the one stream.
+    const bool overlap = !c->profiling;
     long long launches = 0;  // kernels issued (in graph mode: the nodes of one wave)
     auto issueWave = [&](int items, bool allowEarlyExit) {
         launches += 2;  // camera and film fold
@@ -260,6 +265,8 @@ void renderJobs(sst_ctx* c, std::vector<JobIn>& jobs, SstRenderStats* out, bool 
                     Ao.pyrGIn = c->pyrG.as<float4>() + ((d + 1) & 1) * pHalf;
                 }
                 curNee = neeOut;
+                // the previous bounce's shadow rays have cleared the slots this shade reads
+                if (overlap && d > 1) CUDA_CHECK(cudaStreamWaitEvent(st, c->evShadow, 0));
                 if (pyramid)
                     launch_shade_pyramid(ns, dj, Ao, B, w.wb.hits, neeOut, w.wb.cap, w.wb.shRo, w.wb.shRd, w.wb.shTgt, w.wb.shJob, cnt + kCntQueue + d,
                                          cnt + kCntQueue + d + 1, cnt + kCntShadow + d, c->samples.as<float>(), dstats,
@@ -270,8 +277,15 @@ void renderJobs(sst_ctx* c, std::vector<JobIn>& jobs, SstRenderStats* out, bool 
             }
             {
                 KTimer kt(c, 3);
+                cudaStream_t ss = st;
+                if (overlap) {
+                    CUDA_CHECK(cudaEventRecord(c->evShade, st));
+                    CUDA_CHECK(cudaStreamWaitEvent(c->side, c->evShade, 0));
+                    ss = c->side;
+                }
                 launch_trace_shadow(trace, dj, w.wb.shJob, w.wb.shRo, w.wb.shRd, w.wb.shTgt, cnt + kCntShadow + d, cnt + kCntWork + 2 * d + 1, curNee,
-                                    dstats, st);
+                                    dstats, ss);
+                if (overlap) CUDA_CHECK(cudaEventRecord(c->evShadow, c->side));
             }
             launches += (c->shadeOrder ? 4 : 3) + (split ? 1 : 0);  // closest hit, shade order, shade (one or two), shadow rays
             std::swap(A, B);
@@ -283,6 +297,7 @@ void renderJobs(sst_ctx* c, std::vector<JobIn>& jobs, SstRenderStats* out, bool 
                 maxItems = *c->pinnedCount;
             }
         }
+        if (overlap) CUDA_CHECK(cudaStreamWaitEvent(st, c->evShadow, 0));  // the last bounce's shadow rays
         {
             KTimer kt(c, 4);
             launch_film_fold(dj, dch, dwv, dcur, (replay || paths) ? nullptr : c->samples.as<float>(), dstats, maxFold, 1, st);
