@@ -38,9 +38,12 @@ int sst_create(int32_t device, sst_ctx** out) {
         CUDA_CHECK(cudaDeviceGetAttribute(&c->numSMs, cudaDevAttrMultiProcessorCount, device));
         CUDA_CHECK(cudaEventCreate(&c->ev0));
         CUDA_CHECK(cudaEventCreate(&c->ev1));
-        CUDA_CHECK(cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking));
-        CUDA_CHECK(cudaEventCreateWithFlags(&c->evShade, cudaEventDisableTiming));
-        CUDA_CHECK(cudaEventCreateWithFlags(&c->evShadow, cudaEventDisableTiming));
+        CUDA_CHECK(cudaEventCreateWithFlags(&c->evStart, cudaEventDisableTiming));
+        for (WaveStore& ws : c->store) {
+            CUDA_CHECK(cudaStreamCreateWithFlags(&ws.run, cudaStreamNonBlocking));
+            CUDA_CHECK(cudaStreamCreateWithFlags(&ws.side, cudaStreamNonBlocking));
+            for (cudaEvent_t* e : {&ws.evShade, &ws.evShadow, &ws.evDone, &ws.evFolded}) CUDA_CHECK(cudaEventCreateWithFlags(e, cudaEventDisableTiming));
+        }
         CUDA_CHECK(cudaMallocHost(&c->pinnedCount, sizeof(int) * 4));
         *out = c.release();
     });
@@ -51,13 +54,20 @@ int sst_destroy(sst_ctx* ctx) {
         if (!ctx) return;
         cudaSetDevice(ctx->device);
         cudaStreamSynchronize(ctx->stream);
-        if (ctx->side) cudaStreamSynchronize(ctx->side);
+        for (WaveStore& ws : ctx->store) {
+            if (ws.run) cudaStreamSynchronize(ws.run);
+            if (ws.side) cudaStreamSynchronize(ws.side);
+        }
         if (ctx->pinnedCount) cudaFreeHost(ctx->pinnedCount);
         if (ctx->ev0) cudaEventDestroy(ctx->ev0);
         if (ctx->ev1) cudaEventDestroy(ctx->ev1);
-        if (ctx->evShade) cudaEventDestroy(ctx->evShade);
-        if (ctx->evShadow) cudaEventDestroy(ctx->evShadow);
-        if (ctx->side) cudaStreamDestroy(ctx->side);
+        if (ctx->evStart) cudaEventDestroy(ctx->evStart);
+        for (WaveStore& ws : ctx->store) {
+            for (cudaEvent_t e : {ws.evShade, ws.evShadow, ws.evDone, ws.evFolded})
+                if (e) cudaEventDestroy(e);
+            if (ws.side) cudaStreamDestroy(ws.side);
+            if (ws.run) cudaStreamDestroy(ws.run);
+        }
         cudaStreamDestroy(ctx->stream);
         delete ctx;
     });

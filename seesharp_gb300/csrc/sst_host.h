@@ -184,6 +184,21 @@ struct BatchSig {
     SstCamera cam;
 };
 
+// One set of wavefront buffers: path state (A and B), hits, next-event slots, shadow-ray queue,
+// counters, shade order, per-item path estimates, the split shade form's record, the denoiser
+// feature samples and the job table that points at them.  The context keeps two, so that two
+// waves can be in flight.
+struct WaveStore {
+    DevBuf pathA[10], pathB[10];
+    DevBuf hits, nee, shRo, shRd, shTgt, shJob, counters, order, samples, rec, aov, jobs;
+    int cap = 0, neeSlots = 0;
+    // its streams: the bounces (and, with one wave in flight, everything) run on `run`, a bounce's
+    // shadow rays on `side` (evShade: the bounce's shade is done; evShadow: its shadow rays are;
+    // evDone: the wave's bounces are done)
+    cudaStream_t run = nullptr, side = nullptr;
+    cudaEvent_t evShade = nullptr, evShadow = nullptr, evDone = nullptr, evFolded = nullptr;
+};
+
 struct sst_ctx {
     int device = 0;
     cudaStream_t stream = nullptr;
@@ -192,27 +207,19 @@ struct sst_ctx {
     // (kept across commits: no allocation or device-wide free per Scene.Prepare once they fit)
     PinnedBuf commitStage;
     DevBuf commitTri[4], commitOrder, commitScratch, commitScratch4, commitScratch8;
-    // wavefront buffers
-    DevBuf pathA[10], pathB[10];
-    DevBuf hits, nee, shRo, shRd, shTgt, shJob, counters, samples, stats, film;
-    DevBuf shadeOrderBuf;  // k_partition's shade order of the current queue (cap ints)
-    DevBuf shadeRec;       // the split shade form's hand-over record (kShadeRec * cap float4)
-    DevBuf jobsBuf, chunksBuf, wavesBuf, curWave;
+    // wavefront buffers (store[1] only while two waves are in flight)
+    WaveStore store[2];
+    DevBuf stats, film;
+    DevBuf chunksBuf, wavesBuf, curWave;
     DevBuf adjA[3], adjB[3], neeG;
-    int cap = 0, shCap = 0, neeSlots = 0;
-    size_t sampleCap = 0;
     // ray queries (sst_trace, sst_occluded): split rays, queue counters, traversal records, results
     DevBuf qRo, qRd, qCnt, qHits, qOut;
-    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-    // the wavefront's second stream: a bounce's shadow rays are traced on it beside the next bounce's
-    // closest hits (evShade: the bounce's shade is done; evShadow: its shadow rays are)
-    cudaStream_t side = nullptr;
-    cudaEvent_t evShade = nullptr, evShadow = nullptr;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr, evStart = nullptr;
     int* pinnedCount = nullptr;
     // light paths (sst_trace_light_paths)
     DevBuf lightA[9], lightB[9], lightHits, lightVerts, lightLengths, lightCnt;
     // frame-buffer layers (sst_render_layers)
-    DevBuf layMean, layRef, layErr, layVar, laySum, layAlb, layNrm, aovSamples, layErrPix, layTrim, layOutW, layOutIt, layPyr, pyrG;
+    DevBuf layMean, layRef, layErr, layVar, laySum, layAlb, layNrm, layErrPix, layTrim, layOutW, layOutIt, layPyr, pyrG;
     // batched adjoint: the jobs of the last sst_forward_batch, their path radiance, dLoss/dImage
     std::vector<BatchSig> batchSig;
     std::vector<std::unique_ptr<DevBuf>> batchRecord, batchDLdI;
@@ -220,8 +227,8 @@ struct sst_ctx {
     TraceTuning trace;
     int waveCapacity = 0;  // 0: the default
     int shadeBlocks = 8;   // resident blocks per SM of the forward shade kernel with GenericMaterials: 8, 10, 12 or 14
-    int shadeOrder = 1;
-    int shadeSplit = 0;    // 1: the forward shade kernel runs as two kernels per bounce (sst_shade_split.cu)    // 1: each bounce's queue is shaded surface hits first (k_partition); 0: in queue order
+    int shadeOrder = 1;    // 1: each bounce's queue is shaded surface hits first (k_partition); 0: in queue order
+    int shadeSplit = 0;    // 1: the forward shade kernel runs as two kernels per bounce (sst_shade_split.cu)
     // ShadingStats counting (sst_set_shading_stats)
     bool shadingStats = false;
     // kernel timing (sst_set_profiling)
@@ -348,7 +355,7 @@ DevCamera makeCamera(const float w2c[16], float fovDeg, int W, int H);
 void commitScene(sst_scene* s, int W, int H);
 // sst_render.cu
 int defaultWaveCapacity();
-void ensureWave(sst_ctx* c, int cap, int ns, Wave& w);
+void ensureWave(sst_ctx* c, int cap, int ns, Wave& w, int set);
 void checkParams(const sst_scene* s, const SstPathTracerParams* p);
 void renderJobs(sst_ctx* c, std::vector<JobIn>& jobs, SstRenderStats* out, bool replay = false, const std::vector<WaveChunk>* paths = nullptr);
 size_t texPoolFloats(const sst_scene* s);

@@ -458,6 +458,12 @@ void launch_shade(int ns, bool adj, bool generic, int shadeBlocks, const DevJob*
 #undef SST_SHADE_CASE
 }
 
+// Advances a buffer set's wave index by `by` (the last node of its wave graph, two waves in flight).
+__global__ void k_wave_advance(int* wave, int by) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) *wave += by;
+}
+void launch_wave_advance(int* wave, int by, cudaStream_t s) { k_wave_advance<<<1, 32, 0, s>>>(wave, by); }
+
 void launch_camera(const DevJob* jobs, const WaveChunk* chunks, const WaveDesc* waves, const int* curWave, const PathBuf& A, int* qCount,
                    int maxItems, cudaStream_t s) {
     k_camera<<<std::max(1, (maxItems + 255) / 256), 256, 0, s>>>(jobs, chunks, waves, curWave, A, qCount);

@@ -44,6 +44,7 @@ void launch_trace_query(const TraceTuning& t, const DevJob* jobs, const float4* 
 // more spilling); one shadow ray per technique has every build, more shadow rays the default one.
 // The denser builds live in sst_shade_occ.cu.
 // Writes the shade order of a bounce's queue (surface hits first) into order[0, *nIn).
+void launch_wave_advance(int* wave, int by, cudaStream_t s);
 void launch_partition(const uint32_t* depth, const float4* hits, const int* nIn, int* order, int* counts, int maxItems, cudaStream_t s);
 bool shadeBlocksValid(int blocks);
 // The split form (sst_shade_split.cu), forward, GenericMaterials, one shadow ray per technique: two

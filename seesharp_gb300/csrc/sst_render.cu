@@ -34,33 +34,34 @@ int defaultWaveCapacity() {
     return 1 << 21;
 }
 
-void ensureWave(sst_ctx* c, int cap, int ns, Wave& w) {
-    if (cap > c->cap) {
+void ensureWave(sst_ctx* c, int cap, int ns, Wave& w, int set) {
+    WaveStore& ws = c->store[set];
+    if (cap > ws.cap) {
         // grow all path buffers
-        c->cap = cap;
-        c->hits.ensure(size_t(cap) * 16);
+        ws.cap = cap;
+        ws.hits.ensure(size_t(cap) * 16);
     }
-    bindPath(c->pathA, w.wb.a, c->cap);
-    bindPath(c->pathB, w.wb.b, c->cap);
-    c->neeSlots = std::max(c->neeSlots, 2 * ns);
-    c->nee.ensure(2 * size_t(c->cap) * 16 * c->neeSlots);  // two buffers: read and written bounce by bounce
-    size_t shCap = size_t(c->cap) * 2 * ns;
-    c->shRo.ensure(shCap * 16);
-    c->shRd.ensure(shCap * 16);
-    c->shTgt.ensure(shCap * 4);
-    c->shJob.ensure(shCap * 4);
-    c->counters.ensure(sizeof(int) * kNumCounters);
-    c->shadeOrderBuf.ensure(size_t(c->cap) * 4);
+    bindPath(ws.pathA, w.wb.a, ws.cap);
+    bindPath(ws.pathB, w.wb.b, ws.cap);
+    ws.neeSlots = std::max(ws.neeSlots, 2 * ns);
+    ws.nee.ensure(2 * size_t(ws.cap) * 16 * ws.neeSlots);  // two buffers: read and written bounce by bounce
+    size_t shCap = size_t(ws.cap) * 2 * ns;
+    ws.shRo.ensure(shCap * 16);
+    ws.shRd.ensure(shCap * 16);
+    ws.shTgt.ensure(shCap * 4);
+    ws.shJob.ensure(shCap * 4);
+    ws.counters.ensure(sizeof(int) * kNumCounters);
+    ws.order.ensure(size_t(ws.cap) * 4);
     c->stats.ensure(sizeof(DevStats));
-    w.wb.hits = c->hits.as<float4>();
-    w.wb.nee = c->nee.as<float4>();
-    w.wb.shRo = c->shRo.as<float4>();
-    w.wb.shRd = c->shRd.as<float4>();
-    w.wb.shTgt = c->shTgt.as<int>();
-    w.wb.shJob = c->shJob.as<uint32_t>();
-    w.wb.counters = c->counters.as<int>();
-    w.wb.order = c->shadeOrderBuf.as<int>();
-    w.wb.cap = c->cap;
+    w.wb.hits = ws.hits.as<float4>();
+    w.wb.nee = ws.nee.as<float4>();
+    w.wb.shRo = ws.shRo.as<float4>();
+    w.wb.shRd = ws.shRd.as<float4>();
+    w.wb.shTgt = ws.shTgt.as<int>();
+    w.wb.shJob = ws.shJob.as<uint32_t>();
+    w.wb.counters = ws.counters.as<int>();
+    w.wb.order = ws.order.as<int>();
+    w.wb.cap = ws.cap;
     w.wb.shCap = int(shCap);
 }
 
@@ -125,7 +126,7 @@ static void planWaves(std::vector<JobIn>& jobs, int cap, bool iterationPerWave, 
 // Renders the jobs' iterations [iterFirst, iterEnd) into their device films.
 // paths: instead of the jobs' iteration ranges, render exactly these single-path chunks (one
 // (pixel, iteration) each, at most one wave) without folding them into a film; each path's
-// estimate is left in c->samples at its chunk's item offset.
+// estimate is left in the first buffer set's samples at its chunk's item offset.
 void renderJobs(sst_ctx* c, std::vector<JobIn>& jobs, SstRenderStats* out, bool replay, const std::vector<WaveChunk>* paths) {
     cudaStream_t st = c->stream;
     if (jobs.empty()) return;
@@ -144,8 +145,9 @@ void renderJobs(sst_ctx* c, std::vector<JobIn>& jobs, SstRenderStats* out, bool 
     int cap = int(std::min<long long>(c->waveCapacity > 0 ? c->waveCapacity : defaultWaveCapacity(), totalItems));
     for (auto& j : jobs) cap = std::max(cap, 1);
     Wave w;
-    ensureWave(c, cap, ns, w);
-    c->samples.ensure(size_t(w.wb.cap) * 12);
+    ensureWave(c, cap, ns, w, 0);
+    WaveStore& s0 = c->store[0];
+    s0.samples.ensure(size_t(w.wb.cap) * 12);
     w.wb.a.adjL = w.wb.a.adjD = w.wb.a.adjP = nullptr;
     w.wb.b.adjL = w.wb.b.adjD = w.wb.b.adjP = nullptr;
     w.wb.neeG = nullptr;
@@ -175,13 +177,11 @@ void renderJobs(sst_ctx* c, std::vector<JobIn>& jobs, SstRenderStats* out, bool 
         anyAov |= j.lay.aovAlbedo != nullptr;
         pyramid |= j.lay.pyr != nullptr;
     }
-    if (anyAov) c->aovSamples.ensure(size_t(w.wb.cap) * 24);
     if (pyramid && replay) fail(SST_ERR_UNSUPPORTED, "the technique pyramid is not available in the adjoint replay");
     // technique pyramid: the payload of every NEE slot
     if (pyramid) c->pyrG.ensure(2 * size_t(w.wb.cap) * 16 * 2 * ns);
     // the split shade form: forward renders with one shadow ray per technique
     const bool split = c->shadeSplit && generic && !replay && !pyramid && ns == 1;
-    if (split) c->shadeRec.ensure(size_t(kShadeRec) * size_t(w.wb.cap) * 16);
     // job table
     std::vector<DevJob> hj(jobs.size());
     for (size_t k = 0; k < jobs.size(); ++k) {
@@ -189,7 +189,6 @@ void renderJobs(sst_ctx* c, std::vector<JobIn>& jobs, SstRenderStats* out, bool 
         hj[k].sc = jobs[k].s->dev;
         if (jobs[k].hasCam) hj[k].sc.cam = jobs[k].cam;
         hj[k].lay = jobs[k].lay;
-        if (hj[k].lay.aovAlbedo) hj[k].lay.aovSamples = c->aovSamples.as<float>();
         hj[k].cfg = PTConfig{P->width, P->height, P->maxDepth, P->minDepth, P->baseSeed, P->numShadowRays, P->enableBsdfDI, P->ignoreNanAndInf,
                              (c->shadingStats && !replay) ? 1 : 0};
         hj[k].adj = jobs[k].adj;
@@ -203,119 +202,194 @@ void renderJobs(sst_ctx* c, std::vector<JobIn>& jobs, SstRenderStats* out, bool 
     } else {
         planWaves(jobs, w.wb.cap, timeLimit, chunks, waves, iterEnds);
     }
-    c->jobsBuf.upload(hj, st);
+    const char* ge = getenv("SST_GRAPH");
+    const bool useGraph = !c->profiling && !timeLimit && maxDepth <= 32 && !(ge && std::string(ge) == "0") && waves.size() > 1;
+    // Two waves in flight: the bounces of consecutive waves alternate between the two buffer sets
+    // and their streams, so that one wave's last bounces (few paths, latency-bound) run beside the
+    // next wave's first ones; the film folds run in wave order on the context's stream.  Not for
+    // the adjoint replay and the technique pyramid (single-set buffers), nor without graphs.
+    const char* tw = getenv("SST_TWO_WAVES");
+    const bool twoSets = useGraph && waves.size() >= 2 && !replay && !pyramid && !paths && !(tw && std::string(tw) == "0");
+    const int nSets = twoSets ? 2 : 1;
+    Wave ws[2] = {w, w};
+    if (twoSets) {
+        ensureWave(c, w.wb.cap, ns, ws[1], 1);
+        ws[1].wb.a.adjL = ws[1].wb.a.adjD = ws[1].wb.a.adjP = nullptr;
+        ws[1].wb.b.adjL = ws[1].wb.b.adjD = ws[1].wb.b.adjP = nullptr;
+        ws[1].wb.neeG = nullptr;
+        c->store[1].samples.ensure(size_t(ws[1].wb.cap) * 12);
+    }
+    for (int k = 0; k < nSets; ++k) {
+        // sized by the set's own capacity (the sets grow separately), which indexes them
+        WaveStore& sk = c->store[k];
+        if (anyAov) sk.aov.ensure(size_t(ws[k].wb.cap) * 24);
+        if (split) sk.rec.ensure(size_t(kShadeRec) * size_t(ws[k].wb.cap) * 16);
+        // the set's job table: the denoiser feature samples of its waves
+        for (auto& j : hj)
+            if (j.lay.aovAlbedo) j.lay.aovSamples = sk.aov.as<float>();
+        sk.jobs.upload(hj, st);
+    }
     c->chunksBuf.upload(chunks, st);
     c->wavesBuf.upload(waves, st);
-    c->curWave.ensure(sizeof(int) * 2);
-    CUDA_CHECK(cudaMemsetAsync(c->curWave.p, 0, sizeof(int) * 2, st));
-    const DevJob* dj = c->jobsBuf.as<DevJob>();
+    // wave indices: [0] the wave being folded, [1] the fold's finished-block count, [2 + 2s] the wave
+    // whose bounces buffer set s runs (two waves in flight)
+    c->curWave.ensure(sizeof(int) * 6);
+    {
+        const int init[6] = {0, 0, 0, 0, 1, 0};
+        CUDA_CHECK(cudaMemcpyAsync(c->curWave.p, init, sizeof(init), cudaMemcpyHostToDevice, st));
+    }
     const WaveChunk* dch = c->chunksBuf.as<WaveChunk>();
     const WaveDesc* dwv = c->wavesBuf.as<WaveDesc>();
     int* dcur = c->curWave.as<int>();
     DevStats* dstats = c->stats.as<DevStats>();
     CUDA_CHECK(cudaMemsetAsync(dstats, 0, sizeof(DevStats), st));
-    int* cnt = w.wb.counters;
     int maxFold = 0;
     for (auto& wd : waves) maxFold = std::max(maxFold, wd.foldThreads);
 
-    // One wave: camera, then per bounce closest hit / shade / shadow rays, then the film fold.  A
-    // bounce's shadow rays only clear the next-event slots that the next bounce's shade reads, so
-    // they are traced on the side stream beside the next bounce's closest hits and shade order
-    // (each persistent traversal kernel's tail is filled by the other's blocks), and the next shade
-    // waits for them.  Kernel timing (profiling) keeps every launch on the one stream.
+    // One wave of buffer set `set`: camera, then per bounce closest hit / shade / shadow rays on
+    // stream `rs`, then (fold) the film fold.  A bounce's shadow rays only clear the next-event slots
+    // that the next bounce's shade reads, so they are traced on the set's side stream beside the
+    // next bounce's closest hits and shade order (each persistent traversal kernel's tail is filled
+    // by the other's blocks), and the next shade waits for them.  Kernel timing (profiling) keeps
+    // every launch on the one stream.  camWave: the wave index the camera (and the pyramid) read.
     const bool overlap = !c->profiling;
     long long launches = 0;  // kernels issued (in graph mode: the nodes of one wave)
-    auto issueWave = [&](int items, bool allowEarlyExit) {
-        launches += 2;  // camera and film fold
-        CUDA_CHECK(cudaMemsetAsync(cnt, 0, sizeof(int) * kNumCounters, st));
+    auto issueWave = [&](int set, cudaStream_t rs, int items, bool allowEarlyExit, bool fold, int* camWave) {
+        const WaveBuffers& wb = ws[set].wb;
+        WaveStore& sk = c->store[set];
+        const DevJob* dj = sk.jobs.as<DevJob>();
+        float* samples = sk.samples.as<float>();
+        launches += fold ? 2 : 1;  // camera and film fold
+        int* cnt = wb.counters;
+        CUDA_CHECK(cudaMemsetAsync(cnt, 0, sizeof(int) * kNumCounters, rs));
         {
             KTimer kt(c, 0);
-            launch_camera(dj, dch, dwv, dcur, w.wb.a, cnt + kCntQueue + 1, items, st);
+            launch_camera(dj, dch, dwv, camWave, wb.a, cnt + kCntQueue + 1, items, rs);
         }
-        PathBuf A = w.wb.a, B = w.wb.b;
+        PathBuf A = wb.a, B = wb.b;
         int maxItems = items;
-        float4* curNee = w.wb.nee;  // the next-event slots the current bounce writes
+        float4* curNee = wb.nee;  // the next-event slots the current bounce writes
         for (int d = 1; d <= maxDepth; ++d) {
             {
                 KTimer kt(c, 1);
-                launch_trace_closest(trace, dj, A.job, A.ro, A.rd, cnt + kCntQueue + d, cnt + kCntWork + 2 * d, w.wb.hits, dstats, st);
+                launch_trace_closest(trace, dj, A.job, A.ro, A.rd, cnt + kCntQueue + d, cnt + kCntWork + 2 * d, wb.hits, dstats, rs);
             }
             {
                 KTimer kt(c, 2);
                 PathBuf Ao = A;
-                if (split) Ao.rec = c->shadeRec.as<float4>();
+                if (split) Ao.rec = sk.rec.as<float4>();
                 if (c->shadeOrder) {
-                    launch_partition(A.depth, w.wb.hits, cnt + kCntQueue + d, w.wb.order, cnt + kCntPart + 2 * d, maxItems, st);
-                    Ao.order = w.wb.order;
+                    launch_partition(A.depth, wb.hits, cnt + kCntQueue + d, wb.order, cnt + kCntPart + 2 * d, maxItems, rs);
+                    Ao.order = wb.order;
                 }
                 // next-event slots: read the buffer the previous bounce wrote, write the other
-                const size_t neeHalf = size_t(w.wb.cap) * size_t(c->neeSlots);
-                float4* neeOut = w.wb.nee + (d & 1) * neeHalf;
-                Ao.neeIn = w.wb.nee + ((d + 1) & 1) * neeHalf;
+                const size_t neeHalf = size_t(wb.cap) * size_t(sk.neeSlots);
+                float4* neeOut = wb.nee + (d & 1) * neeHalf;
+                Ao.neeIn = wb.nee + ((d + 1) & 1) * neeHalf;
                 float4* neeGOut = nullptr;
-                if (w.wb.neeG) {
-                    const size_t gHalf = size_t(w.wb.cap) * 3 * 2 * size_t(ns);
-                    neeGOut = w.wb.neeG + (d & 1) * gHalf;
-                    Ao.neeGIn = w.wb.neeG + ((d + 1) & 1) * gHalf;
+                if (wb.neeG) {
+                    const size_t gHalf = size_t(wb.cap) * 3 * 2 * size_t(ns);
+                    neeGOut = wb.neeG + (d & 1) * gHalf;
+                    Ao.neeGIn = wb.neeG + ((d + 1) & 1) * gHalf;
                 }
                 float4* pyrGOut = nullptr;
                 if (pyramid) {
-                    const size_t pHalf = size_t(w.wb.cap) * 2 * size_t(ns);
+                    const size_t pHalf = size_t(wb.cap) * 2 * size_t(ns);
                     pyrGOut = c->pyrG.as<float4>() + (d & 1) * pHalf;
                     Ao.pyrGIn = c->pyrG.as<float4>() + ((d + 1) & 1) * pHalf;
                 }
                 curNee = neeOut;
                 // the previous bounce's shadow rays have cleared the slots this shade reads
-                if (overlap && d > 1) CUDA_CHECK(cudaStreamWaitEvent(st, c->evShadow, 0));
+                if (overlap && d > 1) CUDA_CHECK(cudaStreamWaitEvent(rs, sk.evShadow, 0));
                 if (pyramid)
-                    launch_shade_pyramid(ns, dj, Ao, B, w.wb.hits, neeOut, w.wb.cap, w.wb.shRo, w.wb.shRd, w.wb.shTgt, w.wb.shJob, cnt + kCntQueue + d,
-                                         cnt + kCntQueue + d + 1, cnt + kCntShadow + d, c->samples.as<float>(), dstats,
-                                         PyrArgs{dch, dwv, dcur, pyrGOut}, maxItems, st);
+                    launch_shade_pyramid(ns, dj, Ao, B, wb.hits, neeOut, wb.cap, wb.shRo, wb.shRd, wb.shTgt, wb.shJob, cnt + kCntQueue + d,
+                                         cnt + kCntQueue + d + 1, cnt + kCntShadow + d, samples, dstats, PyrArgs{dch, dwv, camWave, pyrGOut}, maxItems, rs);
                 else
-                    launch_shade(ns, replay, generic, c->shadeBlocks, dj, Ao, B, w.wb.hits, neeOut, neeGOut, w.wb.cap, w.wb.shRo, w.wb.shRd, w.wb.shTgt, w.wb.shJob,
-                                 cnt + kCntQueue + d, cnt + kCntQueue + d + 1, cnt + kCntShadow + d, c->samples.as<float>(), dstats, maxItems, st);
+                    launch_shade(ns, replay, generic, c->shadeBlocks, dj, Ao, B, wb.hits, neeOut, neeGOut, wb.cap, wb.shRo, wb.shRd, wb.shTgt, wb.shJob,
+                                 cnt + kCntQueue + d, cnt + kCntQueue + d + 1, cnt + kCntShadow + d, samples, dstats, maxItems, rs);
             }
             {
                 KTimer kt(c, 3);
-                cudaStream_t ss = st;
+                cudaStream_t ss = rs;
                 if (overlap) {
-                    CUDA_CHECK(cudaEventRecord(c->evShade, st));
-                    CUDA_CHECK(cudaStreamWaitEvent(c->side, c->evShade, 0));
-                    ss = c->side;
+                    CUDA_CHECK(cudaEventRecord(sk.evShade, rs));
+                    CUDA_CHECK(cudaStreamWaitEvent(sk.side, sk.evShade, 0));
+                    ss = sk.side;
                 }
-                launch_trace_shadow(trace, dj, w.wb.shJob, w.wb.shRo, w.wb.shRd, w.wb.shTgt, cnt + kCntShadow + d, cnt + kCntWork + 2 * d + 1, curNee,
-                                    dstats, ss);
-                if (overlap) CUDA_CHECK(cudaEventRecord(c->evShadow, c->side));
+                launch_trace_shadow(trace, dj, wb.shJob, wb.shRo, wb.shRd, wb.shTgt, cnt + kCntShadow + d, cnt + kCntWork + 2 * d + 1, curNee, dstats, ss);
+                if (overlap) CUDA_CHECK(cudaEventRecord(sk.evShadow, sk.side));
             }
             launches += (c->shadeOrder ? 4 : 3) + (split ? 1 : 0);  // closest hit, shade order, shade (one or two), shadow rays
             std::swap(A, B);
             if (allowEarlyExit && d >= 6 && d < maxDepth) {
                 // stop early once the queue is empty (long MaxDepth with Russian roulette)
-                CUDA_CHECK(cudaMemcpyAsync(c->pinnedCount, cnt + kCntQueue + d + 1, sizeof(int), cudaMemcpyDeviceToHost, st));
-                CUDA_CHECK(cudaStreamSynchronize(st));
+                CUDA_CHECK(cudaMemcpyAsync(c->pinnedCount, cnt + kCntQueue + d + 1, sizeof(int), cudaMemcpyDeviceToHost, rs));
+                CUDA_CHECK(cudaStreamSynchronize(rs));
                 if (*c->pinnedCount == 0) break;
                 maxItems = *c->pinnedCount;
             }
         }
-        if (overlap) CUDA_CHECK(cudaStreamWaitEvent(st, c->evShadow, 0));  // the last bounce's shadow rays
-        {
+        if (overlap) CUDA_CHECK(cudaStreamWaitEvent(rs, sk.evShadow, 0));  // the last bounce's shadow rays
+        if (fold) {
             KTimer kt(c, 4);
-            launch_film_fold(dj, dch, dwv, dcur, (replay || paths) ? nullptr : c->samples.as<float>(), dstats, maxFold, 1, st);
+            launch_film_fold(dj, dch, dwv, dcur, (replay || paths) ? nullptr : samples, dstats, maxFold, 1, rs);
+        } else {
+            launch_wave_advance(camWave, 2, rs);  // this set's next wave
+            ++launches;
         }
     };
 
-    const char* ge = getenv("SST_GRAPH");
-    bool useGraph = !c->profiling && !timeLimit && maxDepth <= 32 && !(ge && std::string(ge) == "0") && waves.size() > 1;
     CUDA_CHECK(cudaEventRecord(c->ev0, st));
     auto t0 = std::chrono::steady_clock::now();
     int wavesDone = 0;
-    if (useGraph) {
+    if (twoSets) {
+        // one graph per buffer set: camera, the bounces and the advance of the set's wave index; the
+        // folds are plain launches on the context's stream, in wave order, each after its wave's
+        // bounces (evDone) and before the set's next wave reuses the estimates (evFolded)
+        cudaGraph_t graph[2];
+        cudaGraphExec_t exec[2] = {nullptr, nullptr};
+        long long perWave = 0;
+        for (int k = 0; k < 2; ++k) {
+            cudaStream_t rs = c->store[k].run;
+            launches = 0;
+            CUDA_CHECK(cudaStreamBeginCapture(rs, cudaStreamCaptureModeThreadLocal));
+            try {
+                issueWave(k, rs, w.wb.cap, false, false, dcur + 2 + 2 * k);
+            } catch (...) {
+                cudaStreamEndCapture(rs, &graph[k]);
+                throw;
+            }
+            CUDA_CHECK(cudaStreamEndCapture(rs, &graph[k]));
+            CUDA_CHECK(cudaGraphInstantiate(&exec[k], graph[k], 0));
+            perWave = launches;
+        }
+        // the sets' streams start after the context stream's uploads and resets
+        CUDA_CHECK(cudaEventRecord(c->evStart, st));
+        for (int k = 0; k < 2; ++k) CUDA_CHECK(cudaStreamWaitEvent(c->store[k].run, c->evStart, 0));
+        for (size_t k = 0; k < waves.size(); ++k) {
+            WaveStore& sk = c->store[k & 1];
+            if (k >= 2) CUDA_CHECK(cudaStreamWaitEvent(sk.run, sk.evFolded, 0));
+            CUDA_CHECK(cudaGraphLaunch(exec[k & 1], sk.run));
+            CUDA_CHECK(cudaEventRecord(sk.evDone, sk.run));
+            CUDA_CHECK(cudaStreamWaitEvent(st, sk.evDone, 0));
+            launch_film_fold(sk.jobs.as<DevJob>(), dch, dwv, dcur, sk.samples.as<float>(), dstats, maxFold, 1, st);
+            CUDA_CHECK(cudaEventRecord(sk.evFolded, st));
+        }
+        launches = (perWave + 1) * (long long)waves.size();
+        CUDA_CHECK(cudaGetLastError());
+        CUDA_CHECK(cudaStreamSynchronize(st));
+        for (int k = 0; k < 2; ++k) {
+            cudaGraphExecDestroy(exec[k]);
+            cudaGraphDestroy(graph[k]);
+        }
+        wavesDone = int(waves.size());
+    } else if (useGraph) {
         // capture one wave (fixed grid sizes; wave parameters are read from device memory)
         cudaGraph_t graph;
         cudaGraphExec_t exec;
         CUDA_CHECK(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
         try {
-            issueWave(w.wb.cap, false);
+            issueWave(0, st, w.wb.cap, false, true, dcur);
         } catch (...) {
             cudaStreamEndCapture(st, &graph);
             throw;
@@ -337,11 +411,11 @@ void renderJobs(sst_ctx* c, std::vector<JobIn>& jobs, SstRenderStats* out, bool 
                 double per = ms / double(k);
                 if (ms + per > double(jobs[0].p.maximumRenderTimeMs)) break;  // PathTracer.cs:221-227
             }
-            issueWave(waves[k].items, true);
+            issueWave(0, st, waves[k].items, true, true, dcur);
             CUDA_CHECK(cudaGetLastError());
             if (c->profiling) {
                 std::vector<int> hc(kNumCounters);
-                CUDA_CHECK(cudaMemcpyAsync(hc.data(), cnt, sizeof(int) * kNumCounters, cudaMemcpyDeviceToHost, st));
+                CUDA_CHECK(cudaMemcpyAsync(hc.data(), w.wb.counters, sizeof(int) * kNumCounters, cudaMemcpyDeviceToHost, st));
                 flushTimers(c);
                 c->kItems[0] += waves[k].items;
                 c->kItems[4] += waves[k].foldThreads;
@@ -562,7 +636,7 @@ int sst_render_paths(sst_scene* s, const SstPathTracerParams* p, const int32_t* 
             jobs[0].iterEnd = 1;
             renderJobs(c, jobs, &local, false, &chunks);
             const cudaMemcpyKind k = memory == SST_MEM_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
-            CUDA_CHECK(cudaMemcpyAsync(rgb + 3 * size_t(b0), c->samples.p, size_t(cnt) * 12, k, c->stream));
+            CUDA_CHECK(cudaMemcpyAsync(rgb + 3 * size_t(b0), c->store[0].samples.p, size_t(cnt) * 12, k, c->stream));
             CUDA_CHECK(cudaStreamSynchronize(c->stream));
         }
         local.numIterations = 0;
