@@ -14,7 +14,7 @@ namespace cg = cooperative_groups;
 // Minimum resident 128-thread blocks per SM the shade kernel is compiled for (its register
 // budget).  The kernel is latency-bound: on GB300, 8 blocks (64 registers, some spilled to L1)
 // shade 18% faster than the unconstrained 131-register build on the 1M-triangle scene and are
-// the fastest cap on the Cornell box; the adjoint variant is fastest at 16 blocks (32 registers).
+// the fastest cap on the Cornell box (the adjoint variant's cap is below).
 // SST_SHADE_MIN_BLOCKS is the cap of the variant without GenericMaterials (8 is fastest there:
 // 10, 12 and 16 blocks shade the Cornell box 15-42% slower).  The forward variant with
 // GenericMaterials is compiled twice, and the launch tuning picks one per context: for
@@ -30,8 +30,11 @@ namespace cg = cooperative_groups;
 #ifndef SST_SHADE_GEN_DENSE_BLOCKS
 #define SST_SHADE_GEN_DENSE_BLOCKS 14
 #endif
+// The adjoint replay's shade kernel: 8 resident blocks (64 registers).  With the approximate
+// division of the shading units it replays the differentiable Cornell box 13% and the large
+// combined job 10% faster than the 16-block build (32 registers) that was faster before.
 #ifndef SST_SHADE_ADJ_MIN_BLOCKS
-#define SST_SHADE_ADJ_MIN_BLOCKS 16
+#define SST_SHADE_ADJ_MIN_BLOCKS 8
 #endif
 
 namespace sst {
