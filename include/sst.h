@@ -200,10 +200,10 @@ typedef struct SstTuning {
                                  registers: more warps, more spilling; one shadow ray per technique only) */
     int32_t shadeOrder;       /* 1 (the default): each bounce's paths are shaded surface hits first, misses and
                                  finished paths after them; 0: in queue order */
-    int32_t shadeSplit;       /* 1: forward renders with GenericMaterials and one shadow ray per technique shade each
-                                 bounce with two kernels (hit, emitter MIS, Russian roulette and next-event
-                                 estimation; then BSDF sampling and the queue compaction), built for 8 blocks, or
-                                 for 14 when shadeBlocks is 14; 0 (the default): one fused kernel */
+    int32_t shadeSplit;       /* 1 (the default): forward renders with GenericMaterials and one shadow ray per
+                                 technique shade each bounce with two kernels (hit, emitter MIS, Russian roulette
+                                 and next-event estimation; then BSDF sampling and the queue compaction), built for
+                                 8 blocks, or for 14 when shadeBlocks is 14; 0: one fused kernel */
 } SstTuning;
 int sst_get_tuning(sst_ctx* ctx, SstTuning* out);
 /* Invalid values return SST_ERR_INVALID_ARGUMENT and leave the setting unchanged. */

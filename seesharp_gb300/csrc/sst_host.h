@@ -228,7 +228,7 @@ struct sst_ctx {
     int waveCapacity = 0;  // 0: the default
     int shadeBlocks = 8;   // resident blocks per SM of the forward shade kernel with GenericMaterials: 8, 10, 12 or 14
     int shadeOrder = 1;    // 1: each bounce's queue is shaded surface hits first (k_partition); 0: in queue order
-    int shadeSplit = 0;    // 1: the forward shade kernel runs as two kernels per bounce (sst_shade_split.cu)
+    int shadeSplit = 1;    // 1: the forward shade kernel with GenericMaterials runs as two kernels per bounce (sst_shade_split.cu)
     // ShadingStats counting (sst_set_shading_stats)
     bool shadingStats = false;
     // kernel timing (sst_set_profiling)

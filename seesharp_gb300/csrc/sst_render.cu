@@ -678,7 +678,7 @@ int sst_autotune(sst_scene* s, const SstPathTracerParams* p, int32_t trialIterat
         film.ensure(size_t(tp.width) * tp.height * 3 * sizeof(float));
         const bool prof = c->profiling;
         c->profiling = false;
-        // one candidate: the faster of two trial renders of `iters` iterations
+        // one candidate: the fastest of three trial renders of `iters` iterations
         auto trial = [&](const SstTuning& t, int iters) {
             c->trace = toTrace(t);
             c->waveCapacity = t.waveCapacity;
@@ -686,7 +686,7 @@ int sst_autotune(sst_scene* s, const SstPathTracerParams* p, int32_t trialIterat
             c->shadeOrder = t.shadeOrder;
             c->shadeSplit = t.shadeSplit;
             double best = 1e300;
-            for (int r = 0; r < 2; ++r) {
+            for (int r = 0; r < 3; ++r) {
                 std::vector<JobIn> jobs(1);
                 jobs[0].s = s;
                 jobs[0].p = tp;

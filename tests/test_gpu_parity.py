@@ -592,6 +592,8 @@ def test_tuning_and_autotune_leave_images_and_queries_unchanged():
     rays[:, 4:7] = d / np.linalg.norm(d, axis=1, keepdims=True)
     rays[:, 7] = np.inf
     try:
+        # the fused shade kernel for the entries below (the split form has its own test)
+        _native.set_tuning(ctx, **dict(base, shadeSplit=0))
         ref, st0 = render_gpu(sc, 4, 6)
         hits0, occ0 = sc.native.trace(rays), sc.native.occluded(rays)
         assert st0.numKernelLaunches > 0
