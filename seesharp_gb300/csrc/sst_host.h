@@ -186,8 +186,9 @@ struct BatchSig {
 
 // One set of wavefront buffers: path state (A and B), hits, next-event slots, shadow-ray queue,
 // counters, shade order, per-item path estimates, the split shade form's record, the denoiser
-// feature samples and the job table that points at them.  The context keeps two, so that two
-// waves can be in flight.
+// feature samples and the job table that points at them.  The context keeps kMaxWaveSets, so
+// that that many waves can be in flight.
+constexpr int kMaxWaveSets = 3;
 struct WaveStore {
     DevBuf pathA[10], pathB[10];
     DevBuf hits, nee, shRo, shRd, shTgt, shJob, counters, order, samples, rec, aov, jobs;
@@ -207,8 +208,8 @@ struct sst_ctx {
     // (kept across commits: no allocation or device-wide free per Scene.Prepare once they fit)
     PinnedBuf commitStage;
     DevBuf commitTri[4], commitOrder, commitScratch, commitScratch4, commitScratch8;
-    // wavefront buffers (store[1] only while two waves are in flight)
-    WaveStore store[2];
+    // wavefront buffers (store[1..] only while several waves are in flight)
+    WaveStore store[kMaxWaveSets];
     DevBuf stats, film;
     DevBuf chunksBuf, wavesBuf, curWave;
     DevBuf adjA[3], adjB[3], neeG;
