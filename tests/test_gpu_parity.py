@@ -559,6 +559,34 @@ def test_split_shade_agrees_with_the_fused_kernel():
         _native.set_tuning(ctx, **base)
 
 
+def test_waves_in_flight_leave_films_and_layers_unchanged():
+    """One, two or three waves in flight (SST_WAVES_IN_FLIGHT: the waves take turns over that many
+    buffer sets and streams, the folds stay in wave order) change when the kernels run, not what
+    they compute: the film, the denoiser's albedo and normal layers and the variance layer are
+    bitwise the same.  Waves of 4096 paths make about twenty waves of the 80x64, 16-spp render."""
+    import os
+    from seesharp_gb300 import FrameBuffer
+    sc = workloads.sphere_field(12, 80, 64, level=3)
+    sc.FrameBuffer = FrameBuffer(80, 64, flags=FrameBuffer.Flags.Recommended | FrameBuffer.Flags.EstimatePixelVariance)
+    sc.Prepare()
+    ctx = sc.native.ctx
+    base = _native.get_tuning(ctx)
+    out = {}
+    try:
+        _native.set_tuning(ctx, **dict(base, waveCapacity=4096))
+        for n in ("1", "2", "3"):
+            os.environ["SST_WAVES_IN_FLIGHT"] = n
+            img, st = render_gpu(sc, 16, 6)
+            fb = sc.FrameBuffer
+            out[n] = [img] + [fb.layers[k].Image.data.copy() for k in sorted(fb.layers)]
+            assert len(out[n]) >= 3, sorted(fb.layers)
+    finally:
+        os.environ.pop("SST_WAVES_IN_FLIGHT", None)
+        _native.set_tuning(ctx, **base)
+    for n in ("2", "3"):
+        assert all(np.array_equal(a, b) for a, b in zip(out[n], out["1"])), n
+
+
 def test_graph_replay_equals_plain_launches():
     import os
     sc = workloads.cornell_box(64, 64)
