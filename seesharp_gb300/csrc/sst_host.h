@@ -192,6 +192,7 @@ constexpr int kMaxWaveSets = 3;
 struct WaveStore {
     DevBuf pathA[10], pathB[10];
     DevBuf hits, nee, shRo, shRd, shTgt, shJob, counters, order, samples, rec, aov, jobs;
+    DevBuf adjA[3], adjB[3], neeG;  // the adjoint replay's per-path state and next-event payloads
     int cap = 0, neeSlots = 0;
     // its streams: the bounces (and, with one wave in flight, everything) run on `run`, a bounce's
     // shadow rays on `side` (evShade: the bounce's shade is done; evShadow: its shadow rays are;
@@ -212,7 +213,6 @@ struct sst_ctx {
     WaveStore store[kMaxWaveSets];
     DevBuf stats, film;
     DevBuf chunksBuf, wavesBuf, curWave;
-    DevBuf adjA[3], adjB[3], neeG;
     // ray queries (sst_trace, sst_occluded): split rays, queue counters, traversal records, results
     DevBuf qRo, qRd, qCnt, qHits, qOut;
     cudaEvent_t ev0 = nullptr, ev1 = nullptr, evStart = nullptr;

@@ -151,16 +151,19 @@ void renderJobs(sst_ctx* c, std::vector<JobIn>& jobs, SstRenderStats* out, bool 
     w.wb.a.adjL = w.wb.a.adjD = w.wb.a.adjP = nullptr;
     w.wb.b.adjL = w.wb.b.adjD = w.wb.b.adjP = nullptr;
     w.wb.neeG = nullptr;
-    if (replay) {
-        size_t cp = size_t(w.wb.cap);
-        for (int k = 0; k < 2; ++k) { c->adjA[k].ensure(cp * 16); c->adjB[k].ensure(cp * 16); }
-        c->adjA[2].ensure(cp * 48);
-        c->adjB[2].ensure(cp * 48);
-        c->neeG.ensure(2 * cp * 48 * 2 * ns);
-        w.wb.a.adjL = c->adjA[0].as<float4>(); w.wb.a.adjD = c->adjA[1].as<float4>(); w.wb.a.adjP = c->adjA[2].as<float4>();
-        w.wb.b.adjL = c->adjB[0].as<float4>(); w.wb.b.adjD = c->adjB[1].as<float4>(); w.wb.b.adjP = c->adjB[2].as<float4>();
-        w.wb.neeG = c->neeG.as<float4>();
-    }
+    // the adjoint replay's per-path state of a buffer set (sized by the set's capacity)
+    auto bindAdj = [&](Wave& x, int set) {
+        WaveStore& sk = c->store[set];
+        const size_t cp = size_t(x.wb.cap);
+        for (int k = 0; k < 2; ++k) { sk.adjA[k].ensure(cp * 16); sk.adjB[k].ensure(cp * 16); }
+        sk.adjA[2].ensure(cp * 48);
+        sk.adjB[2].ensure(cp * 48);
+        sk.neeG.ensure(2 * cp * 48 * 2 * ns);
+        x.wb.a.adjL = sk.adjA[0].as<float4>(); x.wb.a.adjD = sk.adjA[1].as<float4>(); x.wb.a.adjP = sk.adjA[2].as<float4>();
+        x.wb.b.adjL = sk.adjB[0].as<float4>(); x.wb.b.adjD = sk.adjB[1].as<float4>(); x.wb.b.adjP = sk.adjB[2].as<float4>();
+        x.wb.neeG = sk.neeG.as<float4>();
+    };
+    if (replay) bindAdj(w, 0);
     std::vector<sst_scene*> jobScenes;
     for (auto& j : jobs) jobScenes.push_back(j.s);
     const TraceTuning trace = traceForBuilding(c, jobScenes.data(), jobScenes.size());
@@ -207,11 +210,11 @@ void renderJobs(sst_ctx* c, std::vector<JobIn>& jobs, SstRenderStats* out, bool 
     // Several waves in flight: consecutive waves take turns over nSets buffer sets and their
     // streams, so that one wave's last bounces (few paths, latency-bound) run beside the next
     // wave's first ones; the film folds run in wave order on the context's stream.  Not for the
-    // adjoint replay and the technique pyramid (single-set buffers), nor without graphs.
+    // technique pyramid (single-set buffers) and without graphs.
     // SST_WAVES_IN_FLIGHT: 1 to kMaxWaveSets (default 2).
     const char* wf = getenv("SST_WAVES_IN_FLIGHT");
     const int wantSets = std::min(kMaxWaveSets, std::max(1, wf ? atoi(wf) : 2));
-    const int nSets = (useGraph && !replay && !pyramid && !paths) ? int(std::min<size_t>(size_t(wantSets), waves.size())) : 1;
+    const int nSets = (useGraph && !pyramid && !paths) ? int(std::min<size_t>(size_t(wantSets), waves.size())) : 1;
     const bool multiSets = nSets > 1;
     Wave ws[kMaxWaveSets];
     for (auto& x : ws) x = w;
@@ -220,6 +223,7 @@ void renderJobs(sst_ctx* c, std::vector<JobIn>& jobs, SstRenderStats* out, bool 
         ws[k].wb.a.adjL = ws[k].wb.a.adjD = ws[k].wb.a.adjP = nullptr;
         ws[k].wb.b.adjL = ws[k].wb.b.adjD = ws[k].wb.b.adjP = nullptr;
         ws[k].wb.neeG = nullptr;
+        if (replay) bindAdj(ws[k], k);
         c->store[k].samples.ensure(size_t(ws[k].wb.cap) * 12);
     }
     for (int k = 0; k < nSets; ++k) {
@@ -377,7 +381,7 @@ void renderJobs(sst_ctx* c, std::vector<JobIn>& jobs, SstRenderStats* out, bool 
             CUDA_CHECK(cudaGraphLaunch(exec[set], sk.run));
             CUDA_CHECK(cudaEventRecord(sk.evDone, sk.run));
             CUDA_CHECK(cudaStreamWaitEvent(st, sk.evDone, 0));
-            launch_film_fold(sk.jobs.as<DevJob>(), dch, dwv, dcur, sk.samples.as<float>(), dstats, maxFold, 1, st);
+            launch_film_fold(sk.jobs.as<DevJob>(), dch, dwv, dcur, replay ? nullptr : sk.samples.as<float>(), dstats, maxFold, 1, st);
             CUDA_CHECK(cudaEventRecord(sk.evFolded, st));
         }
         launches = (perWave + 1) * (long long)waves.size();
