@@ -354,8 +354,17 @@ void renderJobs(sst_ctx* c, std::vector<JobIn>& jobs, SstRenderStats* out, bool 
         // one graph per buffer set: camera, the bounces and the advance of the set's wave index; the
         // folds are plain launches on the context's stream, in wave order, each after its wave's
         // bounces (evDone) and before the set's next wave reuses the estimates (evFolded)
-        cudaGraph_t graph[kMaxWaveSets];
-        cudaGraphExec_t exec[kMaxWaveSets] = {};
+        // the graphs and their executables, released on every way out
+        struct Graphs {
+            cudaGraph_t g[kMaxWaveSets] = {};
+            cudaGraphExec_t e[kMaxWaveSets] = {};
+            ~Graphs() {
+                for (int k = 0; k < kMaxWaveSets; ++k) {
+                    if (e[k]) cudaGraphExecDestroy(e[k]);
+                    if (g[k]) cudaGraphDestroy(g[k]);
+                }
+            }
+        } gr;
         long long perWave = 0;
         for (int k = 0; k < nSets; ++k) {
             cudaStream_t rs = c->store[k].run;
@@ -364,11 +373,11 @@ void renderJobs(sst_ctx* c, std::vector<JobIn>& jobs, SstRenderStats* out, bool 
             try {
                 issueWave(k, rs, w.wb.cap, false, false, dcur + 2 + 2 * k);
             } catch (...) {
-                cudaStreamEndCapture(rs, &graph[k]);
+                cudaStreamEndCapture(rs, &gr.g[k]);
                 throw;
             }
-            CUDA_CHECK(cudaStreamEndCapture(rs, &graph[k]));
-            CUDA_CHECK(cudaGraphInstantiate(&exec[k], graph[k], 0));
+            CUDA_CHECK(cudaStreamEndCapture(rs, &gr.g[k]));
+            CUDA_CHECK(cudaGraphInstantiate(&gr.e[k], gr.g[k], 0));
             perWave = launches;
         }
         // the sets' streams start after the context stream's uploads and resets
@@ -378,7 +387,7 @@ void renderJobs(sst_ctx* c, std::vector<JobIn>& jobs, SstRenderStats* out, bool 
             const int set = int(k % size_t(nSets));
             WaveStore& sk = c->store[set];
             if (k >= size_t(nSets)) CUDA_CHECK(cudaStreamWaitEvent(sk.run, sk.evFolded, 0));
-            CUDA_CHECK(cudaGraphLaunch(exec[set], sk.run));
+            CUDA_CHECK(cudaGraphLaunch(gr.e[set], sk.run));
             CUDA_CHECK(cudaEventRecord(sk.evDone, sk.run));
             CUDA_CHECK(cudaStreamWaitEvent(st, sk.evDone, 0));
             launch_film_fold(sk.jobs.as<DevJob>(), dch, dwv, dcur, replay ? nullptr : sk.samples.as<float>(), dstats, maxFold, 1, st);
@@ -387,10 +396,6 @@ void renderJobs(sst_ctx* c, std::vector<JobIn>& jobs, SstRenderStats* out, bool 
         launches = (perWave + 1) * (long long)waves.size();
         CUDA_CHECK(cudaGetLastError());
         CUDA_CHECK(cudaStreamSynchronize(st));
-        for (int k = 0; k < nSets; ++k) {
-            cudaGraphExecDestroy(exec[k]);
-            cudaGraphDestroy(graph[k]);
-        }
         wavesDone = int(waves.size());
     } else if (useGraph) {
         // capture one wave (fixed grid sizes; wave parameters are read from device memory)
