@@ -10,9 +10,9 @@
  *
  * One host thread at a time per context.  Calls are synchronous: they return after the GPU work
  * they issued has finished.  Device arrays (SST_MEM_DEVICE) are read and written on the context's
- * own stream, which is not ordered with the caller's streams: the caller finishes its writes to an
- * input before the call (for example by synchronizing the stream that wrote it), and the outputs are
- * complete when the call returns.
+ * own streams, which are not ordered with the caller's streams: the caller finishes its writes to
+ * an input before the call (for example by synchronizing the stream that wrote it), and the outputs
+ * are complete when the call returns.
  *
  * Each declaration names the SeeSharp interface it replaces (paths relative to the SeeSharp
  * project root).
