@@ -188,7 +188,8 @@ typedef struct SstTuning {
     int32_t waveCapacity;     /* paths in flight per wave; 0 = the default (2^21) */
     int32_t traceBlock;       /* threads per traversal block: 64, 128 (the default) or 256 */
     int32_t traceStackShared; /* traversal stack entries per thread kept in shared memory: 16, 24 (the default) or 32 */
-    int32_t traceBlocksPerSM; /* resident traversal blocks per SM; 0 = as many as fit */
+    int32_t traceBlocksPerSM; /* resident traversal blocks per SM; 0 = as many as fit (three quarters of that while
+                                 several waves are in flight) */
     int32_t traceBvhWidth;    /* BVH traversed: 2 (binary), 4 (4-wide, same leaves; the default) or 8 (8-wide, same leaves,
                                  children in octant slots; built for a scene by the first render or query that
                                  traverses it with this setting, and until then sst_occluded_noalloc, which

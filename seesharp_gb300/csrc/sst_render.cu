@@ -216,6 +216,12 @@ void renderJobs(sst_ctx* c, std::vector<JobIn>& jobs, SstRenderStats* out, bool 
     const int wantSets = std::min(kMaxWaveSets, std::max(1, wf ? atoi(wf) : 2));
     const int nSets = (useGraph && !pyramid && !paths) ? int(std::min<size_t>(size_t(wantSets), waves.size())) : 1;
     const bool multiSets = nSets > 1;
+    // the persistent traversal grids: with several waves in flight, three quarters of the resident
+    // blocks unless the tuning fixes them, so that the traversal kernels of two waves run side by
+    // side instead of one waiting for the other's last blocks (1M-triangle scene, 64-thread blocks:
+    // 12 of 16 blocks 318.6 Msamples/s, 10 316.7, 14 315.7, 16 313.4)
+    TraceTuning traceRun = trace;
+    if (multiSets && traceRun.blocksPerSM == 0) traceRun.blocksPerSM = std::max(1, (3 * traceMaxBlocksPerSM(trace)) / 4);
     Wave ws[kMaxWaveSets];
     for (auto& x : ws) x = w;
     for (int k = 1; k < nSets; ++k) {
@@ -280,7 +286,7 @@ void renderJobs(sst_ctx* c, std::vector<JobIn>& jobs, SstRenderStats* out, bool 
         for (int d = 1; d <= maxDepth; ++d) {
             {
                 KTimer kt(c, 1);
-                launch_trace_closest(trace, dj, A.job, A.ro, A.rd, cnt + kCntQueue + d, cnt + kCntWork + 2 * d, wb.hits, dstats, rs);
+                launch_trace_closest(traceRun, dj, A.job, A.ro, A.rd, cnt + kCntQueue + d, cnt + kCntWork + 2 * d, wb.hits, dstats, rs);
             }
             {
                 KTimer kt(c, 2);
@@ -324,7 +330,7 @@ void renderJobs(sst_ctx* c, std::vector<JobIn>& jobs, SstRenderStats* out, bool 
                     CUDA_CHECK(cudaStreamWaitEvent(sk.side, sk.evShade, 0));
                     ss = sk.side;
                 }
-                launch_trace_shadow(trace, dj, wb.shJob, wb.shRo, wb.shRd, wb.shTgt, cnt + kCntShadow + d, cnt + kCntWork + 2 * d + 1, curNee, dstats, ss);
+                launch_trace_shadow(traceRun, dj, wb.shJob, wb.shRo, wb.shRd, wb.shTgt, cnt + kCntShadow + d, cnt + kCntWork + 2 * d + 1, curNee, dstats, ss);
                 if (overlap) CUDA_CHECK(cudaEventRecord(sk.evShadow, sk.side));
             }
             launches += (c->shadeOrder ? 4 : 3) + (split ? 1 : 0);  // closest hit, shade order, shade (one or two), shadow rays
