@@ -100,8 +100,12 @@ __global__ void __launch_bounds__(128, MINB) k_shade(const DevJob* __restrict__ 
                                                                    float4* shRo, float4* shRd, int* shTgt, uint32_t* shJob, const int* nIn,
                                                                    int* nOut, int* nSh, float* samples, DevStats* stats, PyrArgs pyrA) {
     const int n = *nIn;
-    if ((int)(blockIdx.x * blockDim.x) >= n) return;
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    // a grid-stride loop over whole blocks of the queue: a late bounce's launch caps its grid below
+    // the wave capacity (every thread of a block takes the same turns, so the warp-wide ballots below
+    // see whole warps)
+    for (int blk = blockIdx.x * blockDim.x; blk < n; blk += gridDim.x * blockDim.x) {
+
+    const int t = blk + threadIdx.x;
     const bool valid = t < n;
     const int i = (valid && A.order) ? A.order[t] : t;  // the queued path this thread shades
 
@@ -488,16 +492,16 @@ __global__ void __launch_bounds__(128, MINB) k_shade(const DevJob* __restrict__ 
         if ((threadIdx.x & 31) == 0 && te) atomicAdd(&stats->matEvalPdf, (unsigned long long)te);
         if ((threadIdx.x & 31) == 0 && ts) atomicAdd(&stats->matSample, (unsigned long long)ts);
     }
-    if constexpr (SPLIT) return;  // k_shade_sample compacts the queue
+    if constexpr (SPLIT) continue;  // k_shade_sample compacts the queue
 
     // K7: warp ballot / popc compaction into the next queue
     unsigned m = __ballot_sync(0xffffffffu, cont);
-    if (m == 0) return;
+    if (m == 0) continue;
     int lane = threadIdx.x & 31;
     int base = 0;
     if (lane == 0) base = atomicAdd(nOut, __popc(m));
     base = __shfl_sync(0xffffffffu, base, 0);
-    if (!cont) return;
+    if (!cont) continue;
     int j = base + __popc(m & ((1u << lane) - 1u));
     B.job[j] = job;
     B.pix[j] = pix;
@@ -518,6 +522,7 @@ __global__ void __launch_bounds__(128, MINB) k_shade(const DevJob* __restrict__ 
     }
     // the next-event slots of this vertex were written at this path's index in the current queue
     if (pend) B.neeFrom[j] = (uint32_t)i;
+    }
 }
 
 
@@ -530,8 +535,12 @@ template <bool GEN, int MINB>
 __global__ void __launch_bounds__(128, MINB) k_shade_sample(const DevJob* __restrict__ jobs, PathBuf A, PathBuf B, int cap, const int* nIn,
                                                            int* nOut, float* samples, DevStats* stats) {
     const int n = *nIn;
-    if ((int)(blockIdx.x * blockDim.x) >= n) return;
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    // a grid-stride loop over whole blocks of the queue: a late bounce's launch caps its grid below
+    // the wave capacity (every thread of a block takes the same turns, so the warp-wide ballots below
+    // see whole warps)
+    for (int blk = blockIdx.x * blockDim.x; blk < n; blk += gridDim.x * blockDim.x) {
+
+    const int t = blk + threadIdx.x;
     const bool valid = t < n;
     const int i = (valid && A.order) ? A.order[t] : t;
     bool cont = false;
@@ -607,12 +616,12 @@ __global__ void __launch_bounds__(128, MINB) k_shade_sample(const DevJob* __rest
     if ((threadIdx.x & 31) == 0 && ts) atomicAdd(&stats->matSample, (unsigned long long)ts);
     // warp ballot / popc compaction into the next queue
     unsigned msk = __ballot_sync(0xffffffffu, cont);
-    if (msk == 0) return;
+    if (msk == 0) continue;
     const int lane = threadIdx.x & 31;
     int base = 0;
     if (lane == 0) base = atomicAdd(nOut, __popc(msk));
     base = __shfl_sync(0xffffffffu, base, 0);
-    if (!cont) return;
+    if (!cont) continue;
     const int j = base + __popc(msk & ((1u << lane) - 1u));
     B.job[j] = job;
     B.pix[j] = pix;
@@ -624,6 +633,7 @@ __global__ void __launch_bounds__(128, MINB) k_shade_sample(const DevJob* __rest
     B.ro[j] = make_float4(nRo.x, nRo.y, nRo.z, 0.f);
     B.rd[j] = make_float4(nRd.x, nRd.y, nRd.z, (outDepth & kDoneFlag) ? -1.0f : CUDART_INF_F);
     if (pend) B.neeFrom[j] = (uint32_t)i;
+    }
 }
 
 }  // namespace sst
