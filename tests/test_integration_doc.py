@@ -1,11 +1,12 @@
-"""The C# binding shown in INTEGRATION.md against include/sst.h: every entry point the header
-declares has exactly one LibraryImport, with the same name, the same number of arguments and
-matching types (the C# side cannot be compiled here; this is the check that it binds what the
+"""The C# binding of the repository's integration guide against include/sst.h: every entry point
+the header declares has exactly one LibraryImport, with the same name, the same number of arguments
+and matching types (the C# side cannot be compiled here; this is the check that it binds what the
 library exports)."""
 import os
 import re
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+GUIDE = os.path.join(ROOT, "INTEGRATION.md")
 
 # C# parameter type -> canonical type
 CS = {
@@ -41,7 +42,7 @@ def header_signatures():
 
 
 def csharp_signatures():
-    text = open(os.path.join(ROOT, "INTEGRATION.md")).read()
+    text = open(GUIDE).read()
     out = {}
     for m in re.finditer(r"\[LibraryImport\(Lib\)\] public static partial int (sst_\w+)\((.*?)\);", text):
         name = m.group(1)
@@ -69,5 +70,5 @@ def test_library_import_signatures_match_the_header():
 def test_binding_uses_no_setter_the_reference_lacks():
     """FrameBuffer.Image has a private setter and no SetImage in the reference
     (Images/FrameBuffer.cs:25); the binding writes pixels through the image's indexer."""
-    text = open(os.path.join(ROOT, "INTEGRATION.md")).read()
+    text = open(GUIDE).read()
     assert "SetImage(" not in text and "AddMaterial(" not in text
