@@ -237,10 +237,13 @@ void renderJobs(sst_ctx* c, std::vector<JobIn>& jobs, SstRenderStats* out, bool 
         WaveStore& sk = c->store[k];
         if (anyAov) sk.aov.ensure(size_t(ws[k].wb.cap) * 24);
         if (split) sk.rec.ensure(size_t(kShadeRec) * size_t(ws[k].wb.cap) * 16);
-        // the set's job table: the denoiser feature samples of its waves
-        for (auto& j : hj)
+        // the set's job table (its own host copy, so that no upload depends on when the copy of the
+        // host vector completes): the denoiser feature samples of its waves
+        std::vector<DevJob> hs = hj;
+        for (auto& j : hs)
             if (j.lay.aovAlbedo) j.lay.aovSamples = sk.aov.as<float>();
-        sk.jobs.upload(hj, st);
+        sk.jobs.upload(hs, st);
+        CUDA_CHECK(cudaStreamSynchronize(st));
     }
     c->chunksBuf.upload(chunks, st);
     c->wavesBuf.upload(waves, st);
